@@ -1,0 +1,618 @@
+// C ABI of the GB300 hard-sphere Monte Carlo engine (include/hsmc_gpu.h).
+//
+// A context owns one system on the current device: positions in the
+// reference's double[N][4] layout, two fixed-capacity cell layouts that the
+// sweeps alternate between, the box, and a device state block with the
+// counters and the random-stream position.  Sweeps run as CUDA graphs of
+// (build + 8 move passes) x S sweeps; every call is synchronous on the
+// context's stream.
+#include <cuda_runtime.h>
+
+#include <cmath>
+#include <cstddef>
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <vector>
+
+#include "../../include/hsmc_gpu.h"
+#include "engine.cuh"
+
+using namespace hsmc;
+
+namespace {
+
+constexpr int kGraphSweeps = 8;
+
+struct Scratch {
+  void *ptr = nullptr;
+  size_t bytes = 0;
+  cudaError_t ensure(size_t want) {
+    if (want <= bytes) return cudaSuccess;
+    if (ptr) cudaFree(ptr);
+    ptr = nullptr;
+    bytes = 0;
+    cudaError_t e = cudaMalloc(&ptr, want);
+    if (e == cudaSuccess) bytes = want;
+    return e;
+  }
+  void release() {
+    if (ptr) cudaFree(ptr);
+    ptr = nullptr;
+    bytes = 0;
+  }
+};
+
+}  // namespace
+
+struct hsmc_ctx {
+  hsmc_params prm{};
+  int n = 0;
+  int num_sms = 0;
+  int group = 8;
+  int pass_grid = 1;
+  cudaStream_t stream = nullptr;
+  SysPtrs sp{};
+  Box hbox{};
+  unsigned long long sweep_base = 1;  // host mirror of DevState::sweep_base
+  unsigned long long widom_seq = 0;
+  bool uploaded = false;
+  bool profiling = false;
+  cudaGraphExec_t graph = nullptr;
+  cudaEvent_t ev_start = nullptr, ev_stop = nullptr;
+  std::vector<cudaEvent_t> ev_pass;
+  double last_total_ms = 0.0, last_move_ms = 0.0;
+  int last_move_launches = 0;
+  Scratch hist, qbuf, flags, qpos, qids, trace;
+};
+
+// ----------------------------------------------------------------- helpers
+
+static int cuda_status(cudaError_t e) {
+  if (e == cudaSuccess) return HSMC_OK;
+  fprintf(stderr, "hsmc_gpu: CUDA error %s\n", cudaGetErrorString(e));
+  return HSMC_ERR_CUDA;
+}
+
+#define HSMC_CUDA(call)                      \
+  do {                                       \
+    cudaError_t e_ = (call);                 \
+    if (e_ != cudaSuccess) return cuda_status(e_); \
+  } while (0)
+
+static int status_to_code(int st) {
+  if (st & ST_CELL_OVERFLOW) return HSMC_ERR_CELL_OVERFLOW;
+  if (st & ST_BAD_BIN) return HSMC_ERR_BAD_BIN;
+  if (st & ST_OUT_OF_BOX) return HSMC_ERR_OUT_OF_BOX;
+  if (st & ST_TRACE_FULL) return HSMC_ERR_INVALID_ARG;
+  if (st & ST_BAD_CELL) return HSMC_ERR_CELL_OVERFLOW;
+  return HSMC_OK;
+}
+
+// Cell grid for a box: an even number of cells per axis, each edge at least
+// 1 + margin, the margin covering single-precision rounding of coordinates
+// up to the box length.
+static int make_box(const double len[3], double rho, Box &b, int &cap) {
+  double lmax = len[0];
+  for (int d = 1; d < 3; d++) lmax = len[d] > lmax ? len[d] : lmax;
+  const double u = 5.9604644775390625e-08;  // 2^-24
+  const double margin = u * (64.0 * lmax + 64.0);
+  double wmax = 0.0;
+  for (int d = 0; d < 3; d++) {
+    int nc = 2 * (int)std::floor(len[d] / (2.0 * (1.0 + margin)));
+    if (nc < 4) return HSMC_ERR_CELL_TOO_SMALL;
+    b.len[d] = len[d];
+    b.half[d] = len[d] / 2.0;
+    b.len32[d] = (float)len[d];
+    b.inv_w32[d] = (float)(nc / len[d]);
+    b.w32[d] = (float)(len[d] / nc);
+    b.nc[d] = nc;
+    const double w = len[d] / nc;
+    wmax = w > wmax ? w : wmax;
+  }
+  b.ncell = b.nc[0] * b.nc[1] * b.nc[2];
+  b.vol = len[0] * len[1] * len[2];
+  b.rho = rho;
+  // |error of r^2| of the screen: about 3.5 * 2^-24 * (11 L + 2); doubled.
+  b.band = (float)(u * (48.0 * lmax + 16.0) + 1e-6);
+  b.pad = 0;
+  // Points at mutual distance >= 1 in a cube of edge w: at most 8 below
+  // 2/sqrt(3), at most 14 below sqrt(2).
+  cap = wmax < 1.15 ? 8 : (wmax < 1.41 ? 16 : 32);
+  return HSMC_OK;
+}
+
+static int stencil_for(const Box &b, double cut, int k[3]) {
+  for (int d = 0; d < 3; d++) {
+    const double w = b.len[d] / b.nc[d];
+    int kk = (int)std::ceil((cut + 1e-3) / w);
+    if (kk < 1) kk = 1;
+    k[d] = (2 * kk + 1 >= b.nc[d]) ? -1 : kk;
+  }
+  return 0;
+}
+
+static int read_state(hsmc_ctx *ctx, DevState &out) {
+  HSMC_CUDA(cudaMemcpyAsync(&out, ctx->sp.st, sizeof(DevState), cudaMemcpyDeviceToHost, ctx->stream));
+  HSMC_CUDA(cudaStreamSynchronize(ctx->stream));
+  return HSMC_OK;
+}
+
+static int check_kernels(hsmc_ctx *ctx) {
+  HSMC_CUDA(cudaGetLastError());
+  HSMC_CUDA(cudaStreamSynchronize(ctx->stream));
+  return HSMC_OK;
+}
+
+static void clear_counters_async(hsmc_ctx *ctx) {
+  // acc .. vol_acc, trace_count, widom_ok, scan_mask: one contiguous run
+  cudaMemsetAsync(&ctx->sp.st->acc, 0, offsetof(DevState, dr_max) - offsetof(DevState, acc), ctx->stream);
+}
+
+// ------------------------------------------------------------------- ABI
+
+extern "C" {
+
+const char *hsmc_gpu_strerror(int status) {
+  switch (status) {
+    case HSMC_OK: return "ok";
+    case HSMC_ERR_INVALID_ARG: return "ERROR: invalid argument";
+    case HSMC_ERR_CUDA: return "ERROR: CUDA runtime failure";
+    case HSMC_ERR_NO_DEVICE: return "ERROR: no sm_103 GPU available";
+    case HSMC_ERR_CELL_OVERFLOW: return "ERROR: More than the allowed number of particles in one cell";
+    case HSMC_ERR_CELL_TOO_SMALL:
+      return "ERROR: size of cells in cell list is smaller than the size of the particles";
+    case HSMC_ERR_BAD_BIN: return "ERROR: pair distance outside the histogram (overlapping configuration)";
+    case HSMC_ERR_TIMEOUT: return "ERROR: device wait timed out";
+    case HSMC_ERR_OUT_OF_BOX: return "ERROR: coordinate outside the simulation box";
+    case HSMC_ERR_OVERLAP: return "Overlap in the initial configuration";
+    default: return "ERROR: unknown status";
+  }
+}
+
+int hsmc_gpu_create(const hsmc_params *prm, hsmc_ctx **out) {
+  if (!prm || !out) return HSMC_ERR_INVALID_ARG;
+  *out = nullptr;
+  if (prm->n_particles <= 0 || !(prm->box[0] > 0) || !(prm->box[1] > 0) || !(prm->box[2] > 0) ||
+      !(prm->dr_max >= 0) || !(prm->dv_max >= 0))
+    return HSMC_ERR_INVALID_ARG;
+  for (int d = 0; d < 3; d++)
+    if (!(prm->dr_max < prm->box[d])) return HSMC_ERR_INVALID_ARG;
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess) return HSMC_ERR_NO_DEVICE;
+  cudaDeviceProp p{};
+  if (cudaGetDeviceProperties(&p, dev) != cudaSuccess) return HSMC_ERR_NO_DEVICE;
+  if (!(p.major == 10 && p.minor == 3)) {
+    fprintf(stderr, "hsmc_gpu: device %s is sm_%d%d; this build targets sm_103a\n", p.name, p.major, p.minor);
+    return HSMC_ERR_NO_DEVICE;
+  }
+  Box b{};
+  int cap = 8;
+  const double rho = prm->n_particles / (prm->box[0] * prm->box[1] * prm->box[2]);
+  int e = make_box(prm->box, prm->rho > 0 ? prm->rho : rho, b, cap);
+  if (e) return e;
+  if (prm->cell_capacity > 0) {
+    if (prm->cell_capacity > 32) return HSMC_ERR_INVALID_ARG;
+    cap = prm->cell_capacity <= 8 ? 8 : (prm->cell_capacity <= 16 ? 16 : 32);
+  }
+
+  hsmc_ctx *ctx = new hsmc_ctx();
+  ctx->prm = *prm;
+  ctx->n = prm->n_particles;
+  ctx->num_sms = p.multiProcessorCount;
+  ctx->hbox = b;
+  ctx->group = cap;
+  SysPtrs &sp = ctx->sp;
+  sp.n = ctx->n;
+  sp.cap = cap;
+  sp.ncell_alloc = b.ncell;
+  auto fail = [&](cudaError_t err) {
+    hsmc_gpu_destroy(ctx);
+    return cuda_status(err);
+  };
+  cudaError_t ce;
+  if ((ce = cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking)) != cudaSuccess) return fail(ce);
+  if ((ce = cudaMalloc(&sp.pos, sizeof(double) * 4 * (size_t)ctx->n)) != cudaSuccess) return fail(ce);
+  for (int l = 0; l < 2; l++) {
+    if ((ce = cudaMalloc(&sp.cnt[l], sizeof(int) * (size_t)sp.ncell_alloc)) != cudaSuccess) return fail(ce);
+    if ((ce = cudaMalloc(&sp.slot[l], sizeof(Slot) * (size_t)sp.ncell_alloc * cap)) != cudaSuccess) return fail(ce);
+    if ((ce = cudaMemset(sp.cnt[l], 0, sizeof(int) * (size_t)sp.ncell_alloc)) != cudaSuccess) return fail(ce);
+  }
+  if ((ce = cudaMalloc(&sp.box, sizeof(Box))) != cudaSuccess) return fail(ce);
+  if ((ce = cudaMalloc(&sp.st, sizeof(DevState))) != cudaSuccess) return fail(ce);
+  if ((ce = cudaMemcpy(sp.box, &b, sizeof(Box), cudaMemcpyHostToDevice)) != cudaSuccess) return fail(ce);
+  DevState s0{};
+  s0.sweep_base = ctx->sweep_base;
+  s0.dr_max = prm->dr_max;
+  s0.dv_max = prm->dv_max;
+  s0.pressure = prm->pressure;
+  s0.seed = prm->seed;
+  if ((ce = cudaMemcpy(sp.st, &s0, sizeof(DevState), cudaMemcpyHostToDevice)) != cudaSuccess) return fail(ce);
+  if ((ce = cudaEventCreate(&ctx->ev_start)) != cudaSuccess) return fail(ce);
+  if ((ce = cudaEventCreate(&ctx->ev_stop)) != cudaSuccess) return fail(ce);
+  ctx->pass_grid = move_pass_grid(ctx->group, cap, sp.ncell_alloc, ctx->num_sms);
+  *out = ctx;
+  return HSMC_OK;
+}
+
+void hsmc_gpu_destroy(hsmc_ctx *ctx) {
+  if (!ctx) return;
+  if (ctx->stream) cudaStreamSynchronize(ctx->stream);
+  if (ctx->graph) cudaGraphExecDestroy(ctx->graph);
+  SysPtrs &sp = ctx->sp;
+  cudaFree(sp.pos);
+  for (int l = 0; l < 2; l++) {
+    cudaFree(sp.cnt[l]);
+    cudaFree(sp.slot[l]);
+  }
+  cudaFree(sp.box);
+  cudaFree(sp.st);
+  ctx->hist.release();
+  ctx->qbuf.release();
+  ctx->flags.release();
+  ctx->qpos.release();
+  ctx->qids.release();
+  ctx->trace.release();
+  if (ctx->ev_start) cudaEventDestroy(ctx->ev_start);
+  if (ctx->ev_stop) cudaEventDestroy(ctx->ev_stop);
+  for (cudaEvent_t e : ctx->ev_pass) cudaEventDestroy(e);
+  if (ctx->stream) cudaStreamDestroy(ctx->stream);
+  delete ctx;
+}
+
+int hsmc_gpu_upload_config(hsmc_ctx *ctx, const double (*conf)[4], int n) {
+  if (!ctx || !conf || n != ctx->n) return HSMC_ERR_INVALID_ARG;
+  const Box &b = ctx->hbox;
+  for (int i = 0; i < n; i++) {
+    if (conf[i][0] != (double)i) return HSMC_ERR_INVALID_ARG;
+    for (int d = 0; d < 3; d++) {
+      const double x = conf[i][1 + d];
+      if (!(x >= 0.0 && x <= b.len[d])) return HSMC_ERR_OUT_OF_BOX;
+    }
+  }
+  SysPtrs &sp = ctx->sp;
+  HSMC_CUDA(cudaMemcpyAsync(sp.pos, conf, sizeof(double) * 4 * (size_t)n, cudaMemcpyHostToDevice, ctx->stream));
+  for (int l = 0; l < 2; l++)
+    HSMC_CUDA(cudaMemsetAsync(sp.cnt[l], 0, sizeof(int) * (size_t)sp.ncell_alloc, ctx->stream));
+  HSMC_CUDA(cudaMemsetAsync(&sp.st->status, 0, sizeof(int), ctx->stream));
+  launch_build(sp, -1, ctx->num_sms, ctx->stream);
+  int e = check_kernels(ctx);
+  if (e) return e;
+  DevState s;
+  if ((e = read_state(ctx, s))) return e;
+  if (s.status) return status_to_code(s.status);
+  ctx->uploaded = true;
+  return HSMC_OK;
+}
+
+int hsmc_gpu_download_config(hsmc_ctx *ctx, double (*conf)[4], int n) {
+  if (!ctx || !conf || n != ctx->n) return HSMC_ERR_INVALID_ARG;
+  HSMC_CUDA(cudaMemcpyAsync(conf, ctx->sp.pos, sizeof(double) * 4 * (size_t)n, cudaMemcpyDeviceToHost, ctx->stream));
+  HSMC_CUDA(cudaStreamSynchronize(ctx->stream));
+  return HSMC_OK;
+}
+
+int hsmc_gpu_set_step(hsmc_ctx *ctx, double dr_max, double dv_max) {
+  if (!ctx || !(dr_max >= 0) || !(dv_max >= 0)) return HSMC_ERR_INVALID_ARG;
+  // A displacement of at most dr_max/2 per axis must stay within one periodic
+  // wrap (apply_pbc wraps once).
+  for (int d = 0; d < 3; d++)
+    if (!(dr_max < ctx->hbox.len[d])) return HSMC_ERR_INVALID_ARG;
+  ctx->prm.dr_max = dr_max;
+  ctx->prm.dv_max = dv_max;
+  double v[2] = {dr_max, dv_max};
+  HSMC_CUDA(cudaMemcpyAsync(&ctx->sp.st->dr_max, v, sizeof(v), cudaMemcpyHostToDevice, ctx->stream));
+  HSMC_CUDA(cudaStreamSynchronize(ctx->stream));
+  return HSMC_OK;
+}
+
+int hsmc_gpu_set_profiling(hsmc_ctx *ctx, int on) {
+  if (!ctx) return HSMC_ERR_INVALID_ARG;
+  ctx->profiling = on != 0;
+  return HSMC_OK;
+}
+
+int hsmc_gpu_last_timing(hsmc_ctx *ctx, double *total_ms, double *move_kernel_ms, int *move_launches) {
+  if (!ctx) return HSMC_ERR_INVALID_ARG;
+  if (total_ms) *total_ms = ctx->last_total_ms;
+  if (move_kernel_ms) *move_kernel_ms = ctx->last_move_ms;
+  if (move_launches) *move_launches = ctx->last_move_launches;
+  return HSMC_OK;
+}
+
+static void enqueue_sweep(hsmc_ctx *ctx, long long offset, bool trace) {
+  launch_build(ctx->sp, offset, ctx->num_sms, ctx->stream);
+  for (int k = 0; k < 8; k++) launch_move_pass(ctx->sp, k, ctx->group, trace, ctx->pass_grid, ctx->stream);
+}
+
+static int ensure_graph(hsmc_ctx *ctx) {
+  if (ctx->graph) return HSMC_OK;
+  cudaGraph_t g = nullptr;
+  HSMC_CUDA(cudaStreamBeginCapture(ctx->stream, cudaStreamCaptureModeThreadLocal));
+  for (int s = 0; s < kGraphSweeps; s++) enqueue_sweep(ctx, s, false);
+  launch_advance(ctx->sp, kGraphSweeps, ctx->stream);
+  cudaError_t e = cudaStreamEndCapture(ctx->stream, &g);
+  if (e != cudaSuccess) return cuda_status(e);
+  e = cudaGraphInstantiate(&ctx->graph, g, 0);
+  cudaGraphDestroy(g);
+  if (e != cudaSuccess) {
+    ctx->graph = nullptr;
+    return cuda_status(e);
+  }
+  return HSMC_OK;
+}
+
+static int run_sweeps(hsmc_ctx *ctx, int n_sweeps, bool trace, uint64_t counters[6]) {
+  if (!ctx || n_sweeps < 0) return HSMC_ERR_INVALID_ARG;
+  if (!ctx->uploaded) return HSMC_ERR_INVALID_ARG;
+  clear_counters_async(ctx);
+  HSMC_CUDA(cudaMemsetAsync(&ctx->sp.st->status, 0, sizeof(int), ctx->stream));
+  ctx->last_move_ms = 0.0;
+  ctx->last_move_launches = 0;
+  const bool direct = trace || ctx->profiling;
+  if (!direct) {
+    int e = ensure_graph(ctx);
+    if (e) return e;
+  }
+  if (ctx->profiling && !trace) {
+    const size_t need = 16 * (size_t)n_sweeps;
+    while (ctx->ev_pass.size() < need) {
+      cudaEvent_t ev;
+      HSMC_CUDA(cudaEventCreate(&ev));
+      ctx->ev_pass.push_back(ev);
+    }
+  }
+  HSMC_CUDA(cudaEventRecord(ctx->ev_start, ctx->stream));
+  int done = 0;
+  if (!direct) {
+    while (n_sweeps - done >= kGraphSweeps) {
+      HSMC_CUDA(cudaGraphLaunch(ctx->graph, ctx->stream));
+      done += kGraphSweeps;
+    }
+  }
+  const int rest = n_sweeps - done;
+  for (int s = 0; s < rest; s++) {
+    launch_build(ctx->sp, s, ctx->num_sms, ctx->stream);
+    for (int k = 0; k < 8; k++) {
+      if (ctx->profiling && !trace) HSMC_CUDA(cudaEventRecord(ctx->ev_pass[16 * s + 2 * k], ctx->stream));
+      launch_move_pass(ctx->sp, k, ctx->group, trace, ctx->pass_grid, ctx->stream);
+      if (ctx->profiling && !trace) HSMC_CUDA(cudaEventRecord(ctx->ev_pass[16 * s + 2 * k + 1], ctx->stream));
+    }
+  }
+  if (rest > 0) launch_advance(ctx->sp, rest, ctx->stream);
+  HSMC_CUDA(cudaEventRecord(ctx->ev_stop, ctx->stream));
+  int e = check_kernels(ctx);
+  if (e) return e;
+  ctx->sweep_base += (unsigned long long)n_sweeps;
+  float ms = 0.f;
+  HSMC_CUDA(cudaEventElapsedTime(&ms, ctx->ev_start, ctx->ev_stop));
+  ctx->last_total_ms = ms;
+  if (ctx->profiling && !trace) {
+    double sum = 0.0;
+    for (int s = 0; s < rest; s++)
+      for (int k = 0; k < 8; k++) {
+        float t = 0.f;
+        HSMC_CUDA(cudaEventElapsedTime(&t, ctx->ev_pass[16 * s + 2 * k], ctx->ev_pass[16 * s + 2 * k + 1]));
+        sum += t;
+      }
+    ctx->last_move_ms = sum;
+    ctx->last_move_launches = 8 * rest;
+  }
+  DevState s;
+  if ((e = read_state(ctx, s))) return e;
+  if (counters) {
+    const uint64_t moves = (uint64_t)ctx->n * (uint64_t)n_sweeps;
+    counters[HSMC_CNT_MOVES] = moves;
+    counters[HSMC_CNT_ACCEPTED] = s.acc;
+    counters[HSMC_CNT_REJECTED] = moves - s.acc;
+    counters[HSMC_CNT_VOL_MOVES] = s.vol_moves;
+    counters[HSMC_CNT_VOL_ACCEPTED] = s.vol_acc;
+    counters[HSMC_CNT_VOL_REJECTED] = s.vol_moves - s.vol_acc;
+  }
+  if (s.status && !(trace && s.status == ST_TRACE_FULL)) return status_to_code(s.status);
+  return HSMC_OK;
+}
+
+int hsmc_gpu_sweeps(hsmc_ctx *ctx, int n_sweeps, uint64_t counters[6]) {
+  if (!ctx || ctx->prm.pressure > 0) return HSMC_ERR_INVALID_ARG;
+  return run_sweeps(ctx, n_sweeps, false, counters);
+}
+
+int hsmc_gpu_npt_sweeps(hsmc_ctx *ctx, int n_sweeps, uint64_t counters[6]) {
+  (void)ctx;
+  (void)n_sweeps;
+  (void)counters;
+  return HSMC_ERR_INVALID_ARG;  // provided by the NpT driver
+}
+
+int hsmc_gpu_sweeps_traced(hsmc_ctx *ctx, int n_sweeps, uint32_t *rec, int64_t capacity, int64_t *n_rec,
+                           uint64_t counters[6]) {
+  if (!ctx || !rec || capacity <= 0 || !n_rec) return HSMC_ERR_INVALID_ARG;
+  HSMC_CUDA(ctx->trace.ensure(sizeof(uint32_t) * 12 * (size_t)capacity));
+  ctx->sp.trace = (uint32_t *)ctx->trace.ptr;
+  ctx->sp.trace_cap = (unsigned long long)capacity;
+  int e = run_sweeps(ctx, n_sweeps, true, counters);
+  ctx->sp.trace = nullptr;
+  ctx->sp.trace_cap = 0;
+  DevState s;
+  int e2 = read_state(ctx, s);
+  if (e2) return e2;
+  const unsigned long long got = s.trace_count;
+  *n_rec = (int64_t)got;
+  if (got > (unsigned long long)capacity) return HSMC_ERR_INVALID_ARG;
+  HSMC_CUDA(cudaMemcpy(rec, ctx->trace.ptr, sizeof(uint32_t) * 12 * got, cudaMemcpyDeviceToHost));
+  return e;
+}
+
+int hsmc_gpu_get_box(hsmc_ctx *ctx, double out[5]) {
+  if (!ctx || !out) return HSMC_ERR_INVALID_ARG;
+  Box b;
+  HSMC_CUDA(cudaMemcpyAsync(&b, ctx->sp.box, sizeof(Box), cudaMemcpyDeviceToHost, ctx->stream));
+  HSMC_CUDA(cudaStreamSynchronize(ctx->stream));
+  out[0] = b.len[0];
+  out[1] = b.len[1];
+  out[2] = b.len[2];
+  out[3] = b.vol;
+  out[4] = b.rho;
+  return HSMC_OK;
+}
+
+int hsmc_gpu_grid_info(hsmc_ctx *ctx, int nc[3], float len32[3], float inv_w32[3], int *capacity) {
+  if (!ctx) return HSMC_ERR_INVALID_ARG;
+  for (int d = 0; d < 3; d++) {
+    if (nc) nc[d] = ctx->hbox.nc[d];
+    if (len32) len32[d] = ctx->hbox.len32[d];
+    if (inv_w32) inv_w32[d] = ctx->hbox.inv_w32[d];
+  }
+  if (capacity) *capacity = ctx->sp.cap;
+  return HSMC_OK;
+}
+
+static int pair_counts(hsmc_ctx *ctx, double dr, double rmax, int nbins, uint64_t *counts) {
+  if (!ctx || !counts || nbins <= 0 || !(dr > 0) || !(rmax > 1.0) || !ctx->uploaded) return HSMC_ERR_INVALID_ARG;
+  HSMC_CUDA(ctx->hist.ensure(sizeof(unsigned long long) * (size_t)nbins));
+  auto *d = (unsigned long long *)ctx->hist.ptr;
+  HSMC_CUDA(cudaMemsetAsync(d, 0, sizeof(unsigned long long) * (size_t)nbins, ctx->stream));
+  HSMC_CUDA(cudaMemsetAsync(&ctx->sp.st->status, 0, sizeof(int), ctx->stream));
+  int k[3];
+  stencil_for(ctx->hbox, rmax, k);
+  launch_pair_hist(ctx->sp, dr, rmax, nbins, d, k, ctx->stream);
+  int e = check_kernels(ctx);
+  if (e) return e;
+  HSMC_CUDA(cudaMemcpy(counts, d, sizeof(uint64_t) * (size_t)nbins, cudaMemcpyDeviceToHost));
+  DevState s;
+  if ((e = read_state(ctx, s))) return e;
+  return s.status ? status_to_code(s.status) : HSMC_OK;
+}
+
+int hsmc_gpu_rdf(hsmc_ctx *ctx, double dr, double rmax, int nbins, uint64_t *counts) {
+  return pair_counts(ctx, dr, rmax, nbins, counts);
+}
+
+int hsmc_gpu_pressv(hsmc_ctx *ctx, double dr, double rmax, int nbins, uint64_t *counts) {
+  return pair_counts(ctx, dr, rmax, nbins, counts);
+}
+
+static int scaled_scan(hsmc_ctx *ctx, const double *sf, int n_sf, unsigned long long mask[4]) {
+  if (!ctx || !sf || n_sf <= 0 || n_sf > 256 || !ctx->uploaded) return HSMC_ERR_INVALID_ARG;
+  double smallest = 1.0;
+  for (int k = 0; k < n_sf; k++) {
+    if (!(sf[k] > 0.5 && sf[k] <= 1.0)) return HSMC_ERR_INVALID_ARG;
+    smallest = sf[k] < smallest ? sf[k] : smallest;
+  }
+  clear_counters_async(ctx);
+  int k[3];
+  stencil_for(ctx->hbox, 1.0 / smallest, k);
+  launch_scaled_scan(ctx->sp, sf, n_sf, k, ctx->stream);
+  int e = check_kernels(ctx);
+  if (e) return e;
+  DevState s;
+  if ((e = read_state(ctx, s))) return e;
+  for (int w = 0; w < 4; w++) mask[w] = s.scan_mask[w];
+  return HSMC_OK;
+}
+
+int hsmc_gpu_presst(hsmc_ctx *ctx, const double *sf, int n_sf, uint64_t *nonoverlap) {
+  if (!nonoverlap) return HSMC_ERR_INVALID_ARG;
+  unsigned long long m[4];
+  int e = scaled_scan(ctx, sf, n_sf, m);
+  if (e) return e;
+  for (int k = 0; k < n_sf; k++) nonoverlap[k] = ((m[k >> 6] >> (k & 63)) & 1ull) ? 0 : 1;
+  return HSMC_OK;
+}
+
+int hsmc_gpu_scan_overlap(hsmc_ctx *ctx, double sf, int *overlap) {
+  if (!overlap) return HSMC_ERR_INVALID_ARG;
+  if (sf >= 1.0) {  // expansion: scaled distances never shrink
+    *overlap = 0;
+    return HSMC_OK;
+  }
+  unsigned long long m[4];
+  int e = scaled_scan(ctx, &sf, 1, m);
+  if (e) return e;
+  *overlap = (int)(m[0] & 1ull);
+  return HSMC_OK;
+}
+
+int hsmc_gpu_widom(hsmc_ctx *ctx, int64_t n_insertions, uint64_t *accepted) {
+  if (!ctx || !accepted || n_insertions < 0 || !ctx->uploaded) return HSMC_ERR_INVALID_ARG;
+  clear_counters_async(ctx);
+  launch_widom(ctx->sp, n_insertions, ctx->widom_seq, nullptr, nullptr, ctx->stream);
+  int e = check_kernels(ctx);
+  if (e) return e;
+  ctx->widom_seq++;
+  DevState s;
+  if ((e = read_state(ctx, s))) return e;
+  *accepted = s.widom_ok;
+  return HSMC_OK;
+}
+
+int hsmc_gpu_widom_replay(hsmc_ctx *ctx, const double *pos, int n, uint8_t *overlap) {
+  if (!ctx || !pos || !overlap || n < 0 || !ctx->uploaded) return HSMC_ERR_INVALID_ARG;
+  if (n == 0) return HSMC_OK;
+  HSMC_CUDA(ctx->qpos.ensure(sizeof(double) * 3 * (size_t)n));
+  HSMC_CUDA(ctx->flags.ensure((size_t)n));
+  HSMC_CUDA(cudaMemcpyAsync(ctx->qpos.ptr, pos, sizeof(double) * 3 * (size_t)n, cudaMemcpyHostToDevice, ctx->stream));
+  clear_counters_async(ctx);
+  launch_widom(ctx->sp, n, 0, (const double *)ctx->qpos.ptr, (uint8_t *)ctx->flags.ptr, ctx->stream);
+  int e = check_kernels(ctx);
+  if (e) return e;
+  HSMC_CUDA(cudaMemcpy(overlap, ctx->flags.ptr, (size_t)n, cudaMemcpyDeviceToHost));
+  return HSMC_OK;
+}
+
+int hsmc_gpu_overlap_replay(hsmc_ctx *ctx, const int *ids, const double *pos, int n, uint8_t *overlap) {
+  if (!ctx || !ids || !pos || !overlap || n < 0 || !ctx->uploaded) return HSMC_ERR_INVALID_ARG;
+  if (n == 0) return HSMC_OK;
+  for (int k = 0; k < n; k++)
+    if (ids[k] < 0 || ids[k] >= ctx->n) return HSMC_ERR_INVALID_ARG;
+  HSMC_CUDA(ctx->qpos.ensure(sizeof(double) * 3 * (size_t)n));
+  HSMC_CUDA(ctx->qids.ensure(sizeof(int) * (size_t)n));
+  HSMC_CUDA(ctx->flags.ensure((size_t)n));
+  HSMC_CUDA(cudaMemcpyAsync(ctx->qpos.ptr, pos, sizeof(double) * 3 * (size_t)n, cudaMemcpyHostToDevice, ctx->stream));
+  HSMC_CUDA(cudaMemcpyAsync(ctx->qids.ptr, ids, sizeof(int) * (size_t)n, cudaMemcpyHostToDevice, ctx->stream));
+  launch_overlap_replay(ctx->sp, (const int *)ctx->qids.ptr, (const double *)ctx->qpos.ptr, n,
+                        (uint8_t *)ctx->flags.ptr, ctx->stream);
+  int e = check_kernels(ctx);
+  if (e) return e;
+  HSMC_CUDA(cudaMemcpy(overlap, ctx->flags.ptr, (size_t)n, cudaMemcpyDeviceToHost));
+  return HSMC_OK;
+}
+
+int hsmc_gpu_ql(hsmc_ctx *ctx, int l, double rc, double *ql_mean, double *per_particle) {
+  if (!ctx || !ql_mean || l < 0 || l > 12 || !(rc > 0) || !ctx->uploaded) return HSMC_ERR_INVALID_ARG;
+  HSMC_CUDA(ctx->qbuf.ensure(sizeof(double) * ((size_t)ctx->n + 1)));
+  double *q = (double *)ctx->qbuf.ptr;
+  int k[3];
+  stencil_for(ctx->hbox, rc, k);
+  launch_ql(ctx->sp, l, rc, k, q, q + ctx->n, ctx->stream);
+  int e = check_kernels(ctx);
+  if (e) return e;
+  double sum = 0.0;
+  HSMC_CUDA(cudaMemcpy(&sum, q + ctx->n, sizeof(double), cudaMemcpyDeviceToHost));
+  if (per_particle) HSMC_CUDA(cudaMemcpy(per_particle, q, sizeof(double) * (size_t)ctx->n, cudaMemcpyDeviceToHost));
+  *ql_mean = sum / ctx->n;
+  return HSMC_OK;
+}
+
+int hsmc_gpu_rng_state(hsmc_ctx *ctx, uint64_t out[4]) {
+  if (!ctx || !out) return HSMC_ERR_INVALID_ARG;
+  out[0] = ctx->prm.seed;
+  out[1] = ctx->sweep_base;
+  out[2] = ctx->widom_seq;
+  out[3] = 0;
+  return HSMC_OK;
+}
+
+int hsmc_gpu_rng_set_state(hsmc_ctx *ctx, const uint64_t st[4]) {
+  if (!ctx || !st || st[1] == 0) return HSMC_ERR_INVALID_ARG;
+  ctx->prm.seed = st[0];
+  ctx->sweep_base = st[1];
+  ctx->widom_seq = st[2];
+  HSMC_CUDA(cudaMemcpyAsync(&ctx->sp.st->seed, &st[0], sizeof(uint64_t), cudaMemcpyHostToDevice, ctx->stream));
+  HSMC_CUDA(cudaMemcpyAsync(&ctx->sp.st->sweep_base, &st[1], sizeof(uint64_t), cudaMemcpyHostToDevice, ctx->stream));
+  HSMC_CUDA(cudaStreamSynchronize(ctx->stream));
+  return HSMC_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,43 @@
+// Internal interface between the C ABI (api.cu) and the kernel files.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "common.cuh"
+
+namespace hsmc {
+
+// Pointers every kernel of one system needs.  All are device addresses that
+// stay fixed for the life of a context, so captured CUDA graphs stay valid.
+struct SysPtrs {
+  double *pos;         // N x 4 doubles: (id, x, y, z), the reference's layout
+  int *cnt[2];         // per-cell particle counts, one array per layout
+  Slot *slot[2];       // per-cell slots, capacity `cap`, one array per layout
+  Box *box;            // box and cell grid
+  DevState *st;        // counters, parameters, status
+  uint32_t *trace;     // trace records (12 words each) or nullptr
+  unsigned long long trace_cap;
+  int n;               // particles
+  int cap;             // slots per cell
+  int ncell_alloc;     // cells allocated per layout
+};
+
+// sweep.cu
+void launch_build(const SysPtrs &p, long long sweep_offset, int num_sms, cudaStream_t s);
+void launch_move_pass(const SysPtrs &p, int pass, int group, bool trace, int grid, cudaStream_t s);
+void launch_advance(const SysPtrs &p, int n_sweeps, cudaStream_t s);
+int move_pass_grid(int group, int cap, int ncell_alloc, int num_sms);
+
+// observables.cu
+void launch_pair_hist(const SysPtrs &p, double bin, double rmax, int nbins, unsigned long long *counts,
+                      int stencil[3], cudaStream_t s);
+void launch_scaled_scan(const SysPtrs &p, const double *sf, int n_sf, int stencil[3], cudaStream_t s);
+void launch_widom(const SysPtrs &p, long long n, unsigned long long seq, const double *pos_in, uint8_t *ov_out,
+                  cudaStream_t s);
+void launch_overlap_replay(const SysPtrs &p, const int *ids, const double *pos_in, int n, uint8_t *ov_out,
+                           cudaStream_t s);
+void launch_ql(const SysPtrs &p, int l, double rc, int stencil[3], double *per_particle, double *sum,
+               cudaStream_t s);
+
+}  // namespace hsmc

@@ -1,0 +1,397 @@
+// Observables sampled between sweeps, all computed on the current cell
+// layout of the sweep grid with a stencil wide enough for their cutoff:
+//   k_pair_hist     g(r) and the virial contact histogram: integer pair
+//                   counts, warp-aggregated into shared-memory bins
+//                   (rdf_hist_compute src/compute_rdf.c:110-128,
+//                   pressv_compute_hist src/compute_press.c:123-165)
+//   k_scaled_scan   overlap of the configuration scaled by sf < 1, for the
+//                   thermodynamic pressure and the NpT volume move
+//                   (presst_compute_hist src/compute_press.c:243-273,
+//                   vol_move src/moves.c:104-112)
+//   k_widom         test-particle insertions (src/compute_widom_chem_pot.c:44-120)
+//   k_replay        check_overlap on given trial positions (src/moves.c:157-212)
+//   k_ql            Steinhardt q_l per particle (src/compute_order_parameter.c:99-229)
+// Every decision that the reference takes in FP64 is taken here in FP64 with
+// its operation order; single precision only discards pairs that are
+// clearly beyond the cutoff.
+#include <cooperative_groups.h>
+
+#include "engine.cuh"
+
+namespace cg = cooperative_groups;
+
+namespace hsmc {
+
+struct Stencil {
+  int k[3];  // half-width in cells per axis; -1 means every cell of the axis
+};
+
+struct CellView {
+  const int *cnt;
+  const Slot *slot;
+  int cap;
+  int nc[3];
+  float sh[3], L32[3], iw[3];
+};
+
+__device__ __forceinline__ CellView current_view(const SysPtrs &p) {
+  CellView v;
+  const DevState *st = p.st;
+  const Box *bx = p.box;
+  const int layout = (int)(st->params.sweep & 1ull);
+  v.cnt = p.cnt[layout];
+  v.slot = p.slot[layout];
+  v.cap = p.cap;
+  for (int d = 0; d < 3; d++) {
+    v.nc[d] = bx->nc[d];
+    v.sh[d] = st->params.shift32[d];
+    v.L32[d] = bx->len32[d];
+    v.iw[d] = bx->inv_w32[d];
+  }
+  return v;
+}
+
+// Visit every particle in the stencil of the cell holding (x, y, z).
+template <class F>
+__device__ __forceinline__ void for_each_near(const CellView &v, const Stencil &s, double x, double y, double z,
+                                              F &&visit) {
+  int ci[3];
+  float t;
+  axis_cell(__double2float_rn(x), v.sh[0], v.L32[0], v.iw[0], v.nc[0], ci[0], t);
+  axis_cell(__double2float_rn(y), v.sh[1], v.L32[1], v.iw[1], v.nc[1], ci[1], t);
+  axis_cell(__double2float_rn(z), v.sh[2], v.L32[2], v.iw[2], v.nc[2], ci[2], t);
+  int lo[3], span[3];
+  for (int d = 0; d < 3; d++) {
+    if (s.k[d] < 0) {
+      lo[d] = 0;
+      span[d] = v.nc[d];
+    } else {
+      lo[d] = ci[d] - s.k[d];
+      span[d] = 2 * s.k[d] + 1;
+    }
+  }
+  for (int a = 0; a < span[2]; a++) {
+    int cz = lo[2] + a;
+    cz = (cz % v.nc[2] + v.nc[2]) % v.nc[2];
+    for (int b = 0; b < span[1]; b++) {
+      int cy = lo[1] + b;
+      cy = (cy % v.nc[1] + v.nc[1]) % v.nc[1];
+      for (int e = 0; e < span[0]; e++) {
+        int cx = lo[0] + e;
+        cx = (cx % v.nc[0] + v.nc[0]) % v.nc[0];
+        const int c = cx + v.nc[0] * (cy + v.nc[1] * cz);
+        const int m = v.cnt[c];
+        const int n = m < v.cap ? m : v.cap;  // an overfull cell was flagged by the build
+        const Slot *sl = v.slot + (size_t)c * v.cap;
+        for (int q = 0; q < n; q++) visit(sl[q]);
+      }
+    }
+  }
+}
+
+__device__ __forceinline__ void load_pos(const double *pos, int id, double &x, double &y, double &z) {
+  const double2 a = *reinterpret_cast<const double2 *>(pos + 4 * (size_t)id);
+  const double2 b = *reinterpret_cast<const double2 *>(pos + 4 * (size_t)id + 2);
+  x = a.y;
+  y = b.x;
+  z = b.y;
+}
+
+// Single-precision squared minimum-image distance, for discarding far pairs.
+__device__ __forceinline__ float approx_r2(float ax, float ay, float az, const Slot &o, const float *L32) {
+  float dx = ax - o.x, dy = ay - o.y, dz = az - o.z;
+  dx -= L32[0] * rintf(dx / L32[0]);
+  dy -= L32[1] * rintf(dy / L32[1]);
+  dz -= L32[2] * rintf(dz / L32[2]);
+  return dx * dx + dy * dy + dz * dz;
+}
+
+// ------------------------------------------------------------ pair counts
+constexpr int HIST_SMEM_BINS = 4096;
+
+__global__ void __launch_bounds__(256) k_pair_hist(SysPtrs p, Stencil s, double bin, double rmax, int nbins,
+                                                   unsigned long long *counts, float cut2) {
+  __shared__ unsigned int sh[HIST_SMEM_BINS];
+  const bool use_sh = nbins <= HIST_SMEM_BINS;
+  if (use_sh)
+    for (int b = threadIdx.x; b < nbins; b += blockDim.x) sh[b] = 0;
+  __syncthreads();
+  const CellView v = current_view(p);
+  const Box *bx = p.box;
+  const double len[3] = {bx->len[0], bx->len[1], bx->len[2]};
+  const double half[3] = {bx->half[0], bx->half[1], bx->half[2]};
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  bool bad = false;
+  if (i < p.n) {
+    double x, y, z;
+    load_pos(p.pos, i, x, y, z);
+    const float x32 = __double2float_rn(x), y32 = __double2float_rn(y), z32 = __double2float_rn(z);
+    for_each_near(v, s, x, y, z, [&](const Slot &o) {
+      if (o.id == i) return;
+      if (approx_r2(x32, y32, z32, o, v.L32) > cut2) return;
+      double ox, oy, oz;
+      load_pos(p.pos, o.id, ox, oy, oz);
+      const double r = __dsqrt_rn(ref_r2(x, y, z, ox, oy, oz, len, half));
+      if (r < rmax) {
+        const int b = (int)__ddiv_rn(__dsub_rn(r, 1.0), bin);
+        if (b < 0 || b >= nbins) {
+          bad = true;
+          return;
+        }
+        if (use_sh) {
+          // warp aggregation: one shared-memory atomic per distinct bin
+          cg::coalesced_group active = cg::coalesced_threads();
+          cg::coalesced_group same = cg::labeled_partition(active, b);
+          if (same.thread_rank() == 0) atomicAdd(&sh[b], same.size());
+        } else {
+          atomicAdd(counts + b, 1ull);
+        }
+      }
+    });
+  }
+  if (bad) atomicOr(&p.st->status, ST_BAD_BIN);
+  __syncthreads();
+  if (use_sh)
+    for (int b = threadIdx.x; b < nbins; b += blockDim.x)
+      if (sh[b]) atomicAdd(counts + b, (unsigned long long)sh[b]);
+}
+
+void launch_pair_hist(const SysPtrs &p, double bin, double rmax, int nbins, unsigned long long *counts,
+                      int stencil[3], cudaStream_t st) {
+  Stencil s{{stencil[0], stencil[1], stencil[2]}};
+  const float cut = (float)rmax + 1e-3f;
+  const int blocks = (p.n + 255) / 256;
+  k_pair_hist<<<blocks > 0 ? blocks : 1, 256, 0, st>>>(p, s, bin, rmax, nbins, counts, cut * cut);
+}
+
+// ------------------------------------------------------- scaled overlap
+constexpr int MAX_SF = 256;
+__constant__ double c_sf[MAX_SF];
+
+__global__ void __launch_bounds__(256) k_scaled_scan(SysPtrs p, Stencil s, int n_sf, float cut2) {
+  const CellView v = current_view(p);
+  const Box *bx = p.box;
+  const double len[3] = {bx->len[0], bx->len[1], bx->len[2]};
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  unsigned long long m[4] = {0ull, 0ull, 0ull, 0ull};
+  if (i < p.n) {
+    double x, y, z;
+    load_pos(p.pos, i, x, y, z);
+    const float x32 = __double2float_rn(x), y32 = __double2float_rn(y), z32 = __double2float_rn(z);
+    for_each_near(v, s, x, y, z, [&](const Slot &o) {
+      if (o.id == i) return;
+      if (approx_r2(x32, y32, z32, o, v.L32) > cut2) return;
+      double ox, oy, oz;
+      load_pos(p.pos, o.id, ox, oy, oz);
+      for (int k = 0; k < n_sf; k++) {
+        const unsigned long long bit = 1ull << (k & 63);
+        if (m[k >> 6] & bit) continue;
+        if (ref_r2_scaled(x, y, z, ox, oy, oz, len, c_sf[k]) < 1.0) m[k >> 6] |= bit;
+      }
+    });
+  }
+  for (int w = 0; w < 4; w++) {
+    unsigned long long r = m[w];
+    for (int o = 16; o > 0; o >>= 1) r |= __shfl_xor_sync(0xffffffffu, r, o);
+    if ((threadIdx.x & 31) == 0 && r) atomicOr(&p.st->scan_mask[w], r);
+  }
+}
+
+void launch_scaled_scan(const SysPtrs &p, const double *sf, int n_sf, int stencil[3], cudaStream_t st) {
+  double smallest = 1.0;
+  for (int k = 0; k < n_sf; k++) smallest = sf[k] < smallest ? sf[k] : smallest;
+  cudaMemcpyToSymbolAsync(c_sf, sf, sizeof(double) * (size_t)n_sf, 0, cudaMemcpyHostToDevice, st);
+  Stencil s{{stencil[0], stencil[1], stencil[2]}};
+  const float cut = (float)(1.0 / smallest) + 1e-3f;
+  const int blocks = (p.n + 255) / 256;
+  k_scaled_scan<<<blocks > 0 ? blocks : 1, 256, 0, st>>>(p, s, n_sf, cut * cut);
+}
+
+// ----------------------------------------------------------------- Widom
+// widom_rand_pos (src/compute_widom_chem_pot.c:73-80): x = u * L with u the
+// reference's closed uniform; widom_compute_dist (:130-160): insertion minus
+// particle, one minimum-image branch, overlap when r < 1.
+__device__ __forceinline__ bool point_overlaps(const CellView &v, const SysPtrs &p, const Stencil &s, double x,
+                                               double y, double z, int skip, const double *len,
+                                               const double *half) {
+  const float x32 = __double2float_rn(x), y32 = __double2float_rn(y), z32 = __double2float_rn(z);
+  bool ov = false;
+  for_each_near(v, s, x, y, z, [&](const Slot &o) {
+    if (ov || o.id == skip) return;
+    const float r2 = approx_r2(x32, y32, z32, o, v.L32);
+    if (r2 > 1.01f) return;
+    double ox, oy, oz;
+    load_pos(p.pos, o.id, ox, oy, oz);
+    if (ref_r2(x, y, z, ox, oy, oz, len, half) < 1.0) ov = true;
+  });
+  return ov;
+}
+
+__global__ void __launch_bounds__(256) k_widom(SysPtrs p, long long n, unsigned long long seq, const double *pos_in,
+                                               uint8_t *ov_out) {
+  const CellView v = current_view(p);
+  const Box *bx = p.box;
+  const double len[3] = {bx->len[0], bx->len[1], bx->len[2]};
+  const double half[3] = {bx->half[0], bx->half[1], bx->half[2]};
+  const Stencil s{{1, 1, 1}};
+  const unsigned long long seed = p.st->seed;
+  unsigned long long ok = 0;
+  for (long long k = blockIdx.x * (long long)blockDim.x + threadIdx.x; k < n; k += (long long)gridDim.x * blockDim.x) {
+    double x, y, z;
+    if (pos_in) {
+      x = pos_in[3 * k];
+      y = pos_in[3 * k + 1];
+      z = pos_in[3 * k + 2];
+    } else {
+      const U32x4 r = draw4(seed, (uint32_t)k, (uint32_t)(k >> 32), seq, TAG_WIDOM);
+      x = __dmul_rn(unit_closed(r.x), len[0]);
+      y = __dmul_rn(unit_closed(r.y), len[1]);
+      z = __dmul_rn(unit_closed(r.z), len[2]);
+    }
+    const bool ov = point_overlaps(v, p, s, x, y, z, -1, len, half);
+    if (ov_out) ov_out[k] = ov ? 1 : 0;
+    ok += ov ? 0 : 1;
+  }
+  ok = warp_sum_u64(ok);
+  if ((threadIdx.x & 31) == 0 && ok) atomicAdd(&p.st->widom_ok, ok);
+}
+
+void launch_widom(const SysPtrs &p, long long n, unsigned long long seq, const double *pos_in, uint8_t *ov_out,
+                  cudaStream_t st) {
+  long long blocks = (n + 255) / 256;
+  if (blocks > 152 * 16) blocks = 152 * 16;
+  if (blocks < 1) blocks = 1;
+  k_widom<<<(int)blocks, 256, 0, st>>>(p, n, seq, pos_in, ov_out);
+}
+
+// ----------------------------------------------------------------- replay
+__global__ void __launch_bounds__(256) k_replay(SysPtrs p, const int *ids, const double *pos_in, int n,
+                                                uint8_t *ov_out) {
+  const CellView v = current_view(p);
+  const Box *bx = p.box;
+  const double len[3] = {bx->len[0], bx->len[1], bx->len[2]};
+  const double half[3] = {bx->half[0], bx->half[1], bx->half[2]};
+  const Stencil s{{1, 1, 1}};
+  const int k = blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= n) return;
+  ov_out[k] = point_overlaps(v, p, s, pos_in[3 * k], pos_in[3 * k + 1], pos_in[3 * k + 2], ids[k], len, half) ? 1 : 0;
+}
+
+void launch_overlap_replay(const SysPtrs &p, const int *ids, const double *pos_in, int n, uint8_t *ov_out,
+                           cudaStream_t st) {
+  const int blocks = (n + 255) / 256;
+  k_replay<<<blocks > 0 ? blocks : 1, 256, 0, st>>>(p, ids, pos_in, n, ov_out);
+}
+
+// -------------------------------------------------------------------- q_l
+// Normalised associated Legendre functions by the standard recurrences
+// (Pbar_m^m from Pbar_{m-1}^{m-1}, Pbar_{m+1}^m, then the three-term
+// recurrence in l), with the coefficients tabulated on the host per call.
+constexpr int QL_LMAX = 12;
+struct QlCoef {
+  double diag[QL_LMAX + 1];                   // sqrt((2m+1)/(2m)), m >= 1
+  double first[QL_LMAX + 1];                  // sqrt(2m+3)
+  double a[QL_LMAX + 1][QL_LMAX + 1];         // a[l][m]
+  double b[QL_LMAX + 1][QL_LMAX + 1];         // b[l][m]
+};
+__constant__ QlCoef c_ql;
+
+__global__ void __launch_bounds__(128) k_ql(SysPtrs p, Stencil s, int l, double rc, float cut2, double *q_out) {
+  const CellView v = current_view(p);
+  const Box *bx = p.box;
+  const double len[3] = {bx->len[0], bx->len[1], bx->len[2]};
+  const double half[3] = {bx->half[0], bx->half[1], bx->half[2]};
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= p.n) return;
+  double x, y, z;
+  load_pos(p.pos, i, x, y, z);
+  const float x32 = __double2float_rn(x), y32 = __double2float_rn(y), z32 = __double2float_rn(z);
+  double re[QL_LMAX + 1], im[QL_LMAX + 1];
+  for (int m = 0; m <= QL_LMAX; m++) re[m] = im[m] = 0.0;
+  int bonds = 0;
+  const double inv_sqrt_4pi = 0.28209479177387814;
+  for_each_near(v, s, x, y, z, [&](const Slot &o) {
+    if (o.id == i) return;
+    if (approx_r2(x32, y32, z32, o, v.L32) > cut2) return;
+    double ox, oy, oz;
+    load_pos(p.pos, o.id, ox, oy, oz);
+    const double dx = min_image(__dsub_rn(x, ox), len[0], half[0]);
+    const double dy = min_image(__dsub_rn(y, oy), len[1], half[1]);
+    const double dz = min_image(__dsub_rn(z, oz), len[2], half[2]);
+    const double r = __dsqrt_rn(__dadd_rn(__dadd_rn(__dmul_rn(dx, dx), __dmul_rn(dy, dy)), __dmul_rn(dz, dz)));
+    if (!(r <= rc)) return;
+    bonds++;
+    const double ct = dz / r;
+    const double st = sqrt((1.0 - ct) * (1.0 + ct));
+    const double rho = sqrt(dx * dx + dy * dy);
+    const double cp = rho > 0.0 ? dx / rho : 1.0, sp = rho > 0.0 ? dy / rho : 0.0;
+    double pmm = inv_sqrt_4pi, cm = 1.0, sm = 0.0;
+    for (int m = 0; m <= l; m++) {
+      if (m > 0) {
+        pmm *= -c_ql.diag[m] * st;
+        const double c2 = cm * cp - sm * sp;
+        sm = sm * cp + cm * sp;
+        cm = c2;
+      }
+      double plm = pmm;
+      if (l > m) {
+        double p2 = pmm, p1 = ct * c_ql.first[m] * pmm;
+        for (int ll = m + 2; ll <= l; ll++) {
+          const double pn = c_ql.a[ll][m] * (ct * p1 - c_ql.b[ll][m] * p2);
+          p2 = p1;
+          p1 = pn;
+        }
+        plm = p1;
+      }
+      re[m] += plm * cm;
+      im[m] += plm * sm;
+    }
+  });
+  double sum = 0.0;
+  if (bonds > 0) {
+    const double inv = 1.0 / bonds;
+    for (int m = 0; m <= l; m++) {
+      const double a = re[m] * inv, b = im[m] * inv;
+      sum += (m == 0 ? 1.0 : 2.0) * (a * a + b * b);
+    }
+  }
+  q_out[i] = sqrt(sum * (4.0 * 3.14159265358979323846 / (2 * l + 1)));
+}
+
+// Deterministic mean: one block sums in a fixed order.
+__global__ void __launch_bounds__(1024) k_sum(const double *q, int n, double *out) {
+  __shared__ double part[1024];
+  double a = 0.0;
+  for (int i = threadIdx.x; i < n; i += blockDim.x) a += q[i];
+  part[threadIdx.x] = a;
+  __syncthreads();
+  for (int w = blockDim.x / 2; w > 0; w >>= 1) {
+    if ((int)threadIdx.x < w) part[threadIdx.x] += part[threadIdx.x + w];
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) *out = part[0];
+}
+
+void launch_ql(const SysPtrs &p, int l, double rc, int stencil[3], double *per_particle, double *sum,
+               cudaStream_t st) {
+  QlCoef h;
+  for (int m = 0; m <= QL_LMAX; m++) {
+    h.diag[m] = m > 0 ? sqrt((2.0 * m + 1.0) / (2.0 * m)) : 0.0;
+    h.first[m] = sqrt(2.0 * m + 3.0);
+    for (int ll = 0; ll <= QL_LMAX; ll++) {
+      const double den = (double)ll * ll - (double)m * m;
+      h.a[ll][m] = den > 0 ? sqrt((4.0 * ll * ll - 1.0) / den) : 0.0;
+      const double nb = (ll - 1.0) * (ll - 1.0) - (double)m * m;
+      const double db = 4.0 * (ll - 1.0) * (ll - 1.0) - 1.0;
+      h.b[ll][m] = (nb >= 0 && db > 0) ? sqrt(nb / db) : 0.0;
+    }
+  }
+  cudaMemcpyToSymbolAsync(c_ql, &h, sizeof(h), 0, cudaMemcpyHostToDevice, st);
+  Stencil s{{stencil[0], stencil[1], stencil[2]}};
+  const float cut = (float)rc + 1e-3f;
+  const int blocks = (p.n + 127) / 128;
+  k_ql<<<blocks > 0 ? blocks : 1, 128, 0, st>>>(p, s, l, rc, cut * cut, per_particle);
+  k_sum<<<1, 1024, 0, st>>>(per_particle, p.n, sum);
+}
+
+}  // namespace hsmc

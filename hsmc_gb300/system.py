@@ -1,0 +1,274 @@
+"""Python mirror of the HSMC reference's local-move driver on the GB300 engine.
+
+``HardSphereSystem`` follows the reference's flow and names:
+
+* construction = ``sim_box_init`` + ``part_alloc`` + ``part_init`` +
+  ``cell_list_init`` (src/sim_info.c:32-156, src/cell_list.c:33-58)
+* ``sweep_nvt(n)`` = n calls of ``sweep_nvt`` (src/nvt.c:201-209)
+* ``get_moves_counters()`` = the six move counters (src/moves.c:231-241),
+  64-bit and cumulative since ``reset_moves_counters()``
+* ``compute_rdf_counts``, ``compute_pressv_counts``, ``compute_presst``,
+  ``widom_insertion``, ``global_ql`` = the fill steps of the observables
+  (src/compute_rdf.c:110-128, src/compute_press.c:123-165 and :243-273,
+  src/compute_widom_chem_pot.c:44-71, src/compute_order_parameter.c:82-94)
+
+Every call goes through the C ABI in ``include/hsmc_gpu.h``; errors raise
+``HsmcError`` carrying the reference's message for the failure.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import math
+
+import numpy as np
+
+from . import _native
+
+
+class HsmcError(RuntimeError):
+    def __init__(self, code: int, where: str):
+        lib = _native.load()
+        msg = lib.hsmc_gpu_strerror(code).decode()
+        super().__init__(f"{where}: {_native.STATUS_NAMES.get(code, code)}: {msg}")
+        self.code = code
+
+
+def _check(code: int, where: str) -> None:
+    if code != _native.HSMC_OK:
+        raise HsmcError(code, where)
+
+
+def box_from_lattice(rho: float, cells, lattice_type: int = 2):
+    """sim_box_init (src/sim_info.c:32-71): per-cell volume part_cell/rho,
+    side n * cell_size with cell_size = pow(cell_vol, 1/3)."""
+    per_cell = 1 if lattice_type == 1 else 4
+    cell_vol = per_cell / rho
+    cell_size = math.pow(cell_vol, 1.0 / 3.0)
+    nx, ny, nz = cells
+    box = (nx * cell_size, ny * cell_size, nz * cell_size)
+    vol = (nx * ny * nz) * cell_vol
+    return box, vol, cell_size
+
+
+def lattice_config(rho: float, cells, lattice_type: int = 2) -> np.ndarray:
+    """part_init_sc / part_init_fcc (src/sim_info.c:120-156) as double[N][4]
+    rows (id, x, y, z) in the reference's order."""
+    (_, _, _), _, a = box_from_lattice(rho, cells, lattice_type)
+    nx, ny, nz = cells
+    if lattice_type == 1:
+        if a < 1:
+            raise HsmcError(9, "lattice_config")
+        sites = [(0.0, 0.0, 0.0)]
+    else:
+        if a / math.sqrt(2.0) < 1:
+            raise HsmcError(9, "lattice_config")
+        sites = [(0.0, 0.0, 0.0), (0.5, 0.5, 0.0), (0.5, 0.0, 0.5), (0.0, 0.5, 0.5)]
+    ii, jj, kk = np.meshgrid(np.arange(nx, dtype=np.float64), np.arange(ny, dtype=np.float64),
+                             np.arange(nz, dtype=np.float64), indexing="ij")
+    blocks = []
+    for (sx, sy, sz) in sites:
+        blocks.append(np.stack([(ii + sx) * a if sx else ii * a, (jj + sy) * a if sy else jj * a,
+                                (kk + sz) * a if sz else kk * a], axis=-1).reshape(-1, 3))
+    xyz = np.stack(blocks, axis=1).reshape(-1, 3)
+    conf = np.empty((xyz.shape[0], 4), dtype=np.float64)
+    conf[:, 0] = np.arange(xyz.shape[0], dtype=np.float64)
+    conf[:, 1:] = xyz
+    return conf
+
+
+class HardSphereSystem:
+    """One periodic hard-sphere system on the GPU."""
+
+    def __init__(self, rho: float, cells, lattice_type: int = 2, dr_max: float = 0.05, dv_max: float = 0.001,
+                 pressure: float = 0.0, seed: int = 0, conf: np.ndarray | None = None, cell_capacity: int = 0,
+                 box=None):
+        lib = _native.load()
+        self._lib = lib
+        if np.isscalar(cells):
+            cells = (int(cells),) * 3
+        self.cells = tuple(int(c) for c in cells)
+        self.lattice_type = lattice_type
+        self.rho = float(rho)
+        if box is None:
+            box, vol, _ = box_from_lattice(rho, self.cells, lattice_type)
+        else:
+            vol = box[0] * box[1] * box[2]
+        self.box = tuple(float(b) for b in box)
+        self.vol = vol
+        if conf is None:
+            conf = lattice_config(rho, self.cells, lattice_type)
+        conf = np.ascontiguousarray(conf, dtype=np.float64)
+        self.n = conf.shape[0]
+        p = _native.HsmcParams()
+        p.n_particles = self.n
+        p.lattice_type = lattice_type
+        for d in range(3):
+            p.cells[d] = self.cells[d]
+            p.box[d] = self.box[d]
+        p.rho = self.rho
+        p.dr_max = dr_max
+        p.dv_max = dv_max
+        p.pressure = pressure
+        p.seed = seed
+        p.cell_capacity = cell_capacity
+        h = C.c_void_p()
+        _check(lib.hsmc_gpu_create(C.byref(p), C.byref(h)), "hsmc_gpu_create")
+        self._h = h
+        self.dr_max = dr_max
+        self.dv_max = dv_max
+        self._counters = np.zeros(6, dtype=np.uint64)
+        self.upload(conf)
+
+    # -- lifecycle -----------------------------------------------------------
+    def close(self) -> None:
+        h = getattr(self, "_h", None)
+        if h:
+            self._lib.hsmc_gpu_destroy(h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    # -- configuration -------------------------------------------------------
+    def upload(self, conf: np.ndarray) -> None:
+        conf = np.ascontiguousarray(conf, dtype=np.float64)
+        if conf.shape != (self.n, 4):
+            raise ValueError("configuration must be double[N][4]")
+        _check(self._lib.hsmc_gpu_upload_config(self._h, conf.ctypes.data, self.n), "hsmc_gpu_upload_config")
+
+    def download(self, out: np.ndarray | None = None) -> np.ndarray:
+        if out is None:
+            out = np.empty((self.n, 4), dtype=np.float64)
+        _check(self._lib.hsmc_gpu_download_config(self._h, out.ctypes.data, self.n), "hsmc_gpu_download_config")
+        return out
+
+    part_config_get = download
+
+    def set_step(self, dr_max: float, dv_max: float | None = None) -> None:
+        self.dr_max = dr_max
+        if dv_max is not None:
+            self.dv_max = dv_max
+        _check(self._lib.hsmc_gpu_set_step(self._h, self.dr_max, self.dv_max), "hsmc_gpu_set_step")
+
+    # -- moves ---------------------------------------------------------------
+    def sweep_nvt(self, n_sweeps: int = 1) -> np.ndarray:
+        c = np.zeros(6, dtype=np.uint64)
+        _check(self._lib.hsmc_gpu_sweeps(self._h, n_sweeps, c.ctypes.data), "hsmc_gpu_sweeps")
+        self._counters += c
+        return c
+
+    def sweep_npt(self, n_sweeps: int = 1) -> np.ndarray:
+        c = np.zeros(6, dtype=np.uint64)
+        _check(self._lib.hsmc_gpu_npt_sweeps(self._h, n_sweeps, c.ctypes.data), "hsmc_gpu_npt_sweeps")
+        self._counters += c
+        return c
+
+    def sweeps_traced(self, n_sweeps: int, capacity: int | None = None):
+        if capacity is None:
+            capacity = self.n * n_sweeps + 16
+        rec = np.zeros((capacity, 12), dtype=np.uint32)
+        got = C.c_int64(0)
+        c = np.zeros(6, dtype=np.uint64)
+        _check(self._lib.hsmc_gpu_sweeps_traced(self._h, n_sweeps, rec.ctypes.data, capacity, C.byref(got),
+                                                c.ctypes.data), "hsmc_gpu_sweeps_traced")
+        self._counters += c
+        return rec[: got.value].copy(), c
+
+    def get_moves_counters(self) -> np.ndarray:
+        return self._counters.copy()
+
+    def reset_moves_counters(self) -> None:
+        self._counters[:] = 0
+
+    def grid_info(self):
+        nc = np.zeros(3, dtype=np.int32)
+        l32 = np.zeros(3, dtype=np.float32)
+        iw = np.zeros(3, dtype=np.float32)
+        cap = C.c_int()
+        _check(self._lib.hsmc_gpu_grid_info(self._h, nc.ctypes.data, l32.ctypes.data, iw.ctypes.data,
+                                            C.byref(cap)), "hsmc_gpu_grid_info")
+        return nc, l32, iw, cap.value
+
+    def get_box(self):
+        out = np.zeros(5, dtype=np.float64)
+        _check(self._lib.hsmc_gpu_get_box(self._h, out.ctypes.data), "hsmc_gpu_get_box")
+        return out
+
+    # -- observables -----------------------------------------------------------
+    def compute_rdf_counts(self, dr: float, rmax: float, nbins: int) -> np.ndarray:
+        out = np.zeros(nbins, dtype=np.uint64)
+        _check(self._lib.hsmc_gpu_rdf(self._h, dr, rmax, nbins, out.ctypes.data), "hsmc_gpu_rdf")
+        return out
+
+    def compute_pressv_counts(self, dr: float, rmax: float, nbins: int) -> np.ndarray:
+        out = np.zeros(nbins, dtype=np.uint64)
+        _check(self._lib.hsmc_gpu_pressv(self._h, dr, rmax, nbins, out.ctypes.data), "hsmc_gpu_pressv")
+        return out
+
+    def compute_presst(self, sf) -> np.ndarray:
+        sf = np.ascontiguousarray(sf, dtype=np.float64)
+        out = np.zeros(sf.size, dtype=np.uint64)
+        _check(self._lib.hsmc_gpu_presst(self._h, sf.ctypes.data, sf.size, out.ctypes.data), "hsmc_gpu_presst")
+        return out
+
+    def scan_overlap(self, sf: float) -> int:
+        ov = C.c_int()
+        _check(self._lib.hsmc_gpu_scan_overlap(self._h, sf, C.byref(ov)), "hsmc_gpu_scan_overlap")
+        return ov.value
+
+    def widom_insertion(self, n: int) -> int:
+        acc = C.c_uint64()
+        _check(self._lib.hsmc_gpu_widom(self._h, n, C.byref(acc)), "hsmc_gpu_widom")
+        return int(acc.value)
+
+    def global_ql(self, l: int, rc: float, per_particle: bool = False):
+        mean = C.c_double()
+        per = np.zeros(self.n, dtype=np.float64) if per_particle else None
+        _check(self._lib.hsmc_gpu_ql(self._h, l, rc, C.byref(mean), per.ctypes.data if per is not None else None),
+               "hsmc_gpu_ql")
+        return (mean.value, per) if per_particle else mean.value
+
+    # -- replay ------------------------------------------------------------------
+    def overlap_replay(self, ids, pos) -> np.ndarray:
+        ids = np.ascontiguousarray(ids, dtype=np.int32)
+        pos = np.ascontiguousarray(pos, dtype=np.float64).reshape(-1, 3)
+        out = np.zeros(ids.size, dtype=np.uint8)
+        _check(self._lib.hsmc_gpu_overlap_replay(self._h, ids.ctypes.data, pos.ctypes.data, ids.size,
+                                                 out.ctypes.data), "hsmc_gpu_overlap_replay")
+        return out
+
+    def widom_replay(self, pos) -> np.ndarray:
+        pos = np.ascontiguousarray(pos, dtype=np.float64).reshape(-1, 3)
+        out = np.zeros(pos.shape[0], dtype=np.uint8)
+        _check(self._lib.hsmc_gpu_widom_replay(self._h, pos.ctypes.data, pos.shape[0], out.ctypes.data),
+               "hsmc_gpu_widom_replay")
+        return out
+
+    # -- rng / timing ----------------------------------------------------------
+    def rng_state(self) -> np.ndarray:
+        out = np.zeros(4, dtype=np.uint64)
+        _check(self._lib.hsmc_gpu_rng_state(self._h, out.ctypes.data), "hsmc_gpu_rng_state")
+        return out
+
+    def rng_set_state(self, st) -> None:
+        st = np.ascontiguousarray(st, dtype=np.uint64)
+        _check(self._lib.hsmc_gpu_rng_set_state(self._h, st.ctypes.data), "hsmc_gpu_rng_set_state")
+
+    def set_profiling(self, on: bool) -> None:
+        _check(self._lib.hsmc_gpu_set_profiling(self._h, 1 if on else 0), "hsmc_gpu_set_profiling")
+
+    def last_timing(self):
+        t = C.c_double()
+        m = C.c_double()
+        k = C.c_int()
+        _check(self._lib.hsmc_gpu_last_timing(self._h, C.byref(t), C.byref(m), C.byref(k)), "hsmc_gpu_last_timing")
+        return t.value, m.value, k.value

@@ -1,0 +1,191 @@
+/*
+ * hsmc_gpu.h -- C ABI of the GB300 (sm_103a) hard-sphere Monte Carlo engine.
+ *
+ * This is the boundary a host program in C calls in place of the HSMC
+ * reference's local-move hot path.  Plain pointers and sizes only; every call
+ * is synchronous on the context's own CUDA stream and returns 0 (HSMC_OK) or
+ * one of the error codes below.  hsmc_gpu_strerror() gives the reference's
+ * message for an error, so a host shim can print it and exit as the
+ * reference does.
+ *
+ * Ownership: the device owns positions, the cell layout and the random stream
+ * between calls.  Host buffers are always caller-owned; the host-side
+ * configuration keeps the reference's double[N][4] layout (id, x, y, z)
+ * (src/sim_info.h:20), so write_config / write_restart work unchanged on a
+ * downloaded copy.
+ *
+ * Threading: one host thread per context.  A process may hold several
+ * contexts (independent systems).
+ *
+ * Reference interfaces each entry point replaces are cited beside it
+ * (paths relative to the reference project).
+ */
+#ifndef HSMC_GPU_H
+#define HSMC_GPU_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---------------------------------------------------------------- errors */
+enum hsmc_status {
+  HSMC_OK = 0,
+  HSMC_ERR_INVALID_ARG = 1,   /* bad size, pointer or parameter */
+  HSMC_ERR_CUDA = 2,          /* a CUDA runtime call failed */
+  HSMC_ERR_NO_DEVICE = 3,     /* no usable sm_103 device */
+  HSMC_ERR_CELL_OVERFLOW = 4, /* more particles in one cell than it holds (src/cell_list.c:228-231) */
+  HSMC_ERR_CELL_TOO_SMALL = 5,/* box too small for the cell grid (src/cell_list.c:126-129) */
+  HSMC_ERR_BAD_BIN = 6,       /* a pair fell outside its histogram (r < 1: overlapping input) */
+  HSMC_ERR_TIMEOUT = 7,       /* a bounded device wait gave up */
+  HSMC_ERR_OUT_OF_BOX = 8,    /* a coordinate outside [0, L] on upload */
+  HSMC_ERR_OVERLAP = 9        /* the configuration contains an overlapping pair */
+};
+
+typedef struct hsmc_ctx hsmc_ctx;
+
+/* Parameters of one system.  The box is the reference's rectangular periodic
+ * box (src/sim_info.c:32-71); n_particles and the lattice counts follow its
+ * input keywords (src/read_input.c:138-192). */
+typedef struct {
+  int n_particles;      /* N */
+  int lattice_type;     /* 1 = simple cubic, 2 = FCC (keyword "type") */
+  int cells[3];         /* lattice cell counts (keywords cells_x/y/z) */
+  double rho;           /* number density (keyword "rho") */
+  double box[3];        /* box sides lx, ly, lz */
+  double dr_max;        /* maximum particle displacement (keyword "dr_max") */
+  double dv_max;        /* maximum ln V change for NpT (keyword "npt", 2nd value) */
+  double pressure;      /* beta*P for NpT, 0 for NVT (keyword "npt", 1st value) */
+  uint64_t seed;        /* random stream key (keyword "seed") */
+  int cell_capacity;    /* particles per device cell; 0 chooses from the cell size */
+  int reserved[7];
+} hsmc_params;
+
+/* Replaces the set-up in hs_nvt / hs_npt (src/nvt.c:30-62, src/npt.c:25-70):
+ * allocates device state for one system.  Positions start undefined; call
+ * hsmc_gpu_upload_config next. */
+int hsmc_gpu_create(const hsmc_params *params, hsmc_ctx **out);
+
+/* Frees everything the context holds (src/nvt.c:97-100). */
+void hsmc_gpu_destroy(hsmc_ctx *ctx);
+
+/* Copies a host configuration double[n][4] = (id, x, y, z) to the device and
+ * builds the cell layout (src/cell_list.c:142-175).  conf[i][0] must equal i
+ * and coordinates must lie in [0, L]. */
+int hsmc_gpu_upload_config(hsmc_ctx *ctx, const double (*conf)[4], int n);
+
+/* Copies the device configuration back into double[n][4]
+ * (the array part_config_get returns, src/sim_info.c:187-190). */
+int hsmc_gpu_download_config(hsmc_ctx *ctx, double (*conf)[4], int n);
+
+/* Sets the maximum displacement and volume step (G_IN.dr_max / G_IN.dv_max,
+ * written by the optimiser, src/optimizer.c:23-166). */
+int hsmc_gpu_set_step(hsmc_ctx *ctx, double dr_max, double dv_max);
+
+/* Counter order used by the sweep calls: the six move counters of
+ * get_moves_counters (src/moves.c:231-241), 64-bit, for this call only. */
+enum {
+  HSMC_CNT_MOVES = 0,
+  HSMC_CNT_ACCEPTED = 1,
+  HSMC_CNT_REJECTED = 2,
+  HSMC_CNT_VOL_MOVES = 3,
+  HSMC_CNT_VOL_ACCEPTED = 4,
+  HSMC_CNT_VOL_REJECTED = 5
+};
+
+/* NVT: n_sweeps sweeps of N trial moves each (sweep_nvt, src/nvt.c:201-209,
+ * part_move src/moves.c:27-80).  counters may be NULL. */
+int hsmc_gpu_sweeps(hsmc_ctx *ctx, int n_sweeps, uint64_t counters[6]);
+
+/* NpT: n_sweeps sweeps, each N trial particle moves and one trial volume
+ * move on average (sweep_npt, src/npt.c:177-196; vol_move src/moves.c:83-153). */
+int hsmc_gpu_npt_sweeps(hsmc_ctx *ctx, int n_sweeps, uint64_t counters[6]);
+
+/* Current box: out[0..2] = lx, ly, lz, out[3] = volume, out[4] = density
+ * (sim_box_info_get, src/sim_info.c:179-181; G_IN.rho after volume moves). */
+int hsmc_gpu_get_box(hsmc_ctx *ctx, double out[5]);
+
+/* g(r) pair counts before normalisation (rdf_hist_compute,
+ * src/compute_rdf.c:110-128): counts[b] = number of ordered pairs (i, j != i)
+ * with r < rmax and (int)((r - 1)/dr) == b, which equals the reference's
+ * histogram value (2 per unordered pair).  rmax must already be the adjusted
+ * cutoff dr*nbins + 1 (src/compute_rdf.c:104) and at most half the box. */
+int hsmc_gpu_rdf(hsmc_ctx *ctx, double dr, double rmax, int nbins, uint64_t *counts);
+
+/* Virial-route contact histogram, the same counting on [1, rmax)
+ * (pressv_compute_hist, src/compute_press.c:123-165). */
+int hsmc_gpu_pressv(hsmc_ctx *ctx, double dr, double rmax, int nbins, uint64_t *counts);
+
+/* Thermodynamic route: for each scale factor sf[k] < 1, nonoverlap[k] = 1 when
+ * no pair overlaps with all distances scaled by sf[k], else 0
+ * (presst_compute_hist, src/compute_press.c:243-273; sf = (1 - xi)^(1/3)
+ * computed by the caller as the reference does). */
+int hsmc_gpu_presst(hsmc_ctx *ctx, const double *sf, int n_sf, uint64_t *nonoverlap);
+
+/* Full scaled overlap scan of a trial volume move (src/moves.c:104-112):
+ * *overlap = 1 when any pair is closer than 1 after scaling by sf. */
+int hsmc_gpu_scan_overlap(hsmc_ctx *ctx, double sf, int *overlap);
+
+/* Widom test-particle insertions at uniform points (widom_insertion,
+ * src/compute_widom_chem_pot.c:44-71): *accepted = insertions without overlap.
+ * The host forms mu = -ln(accepted/n) as the reference does. */
+int hsmc_gpu_widom(hsmc_ctx *ctx, int64_t n_insertions, uint64_t *accepted);
+
+/* Mean Steinhardt q_l over all particles (global_ql_compute,
+ * src/compute_order_parameter.c:82-94); rc is the bond cutoff after the
+ * reference's clipping to its cell size (src/compute_order_parameter.c:31-40).
+ * per_particle may be NULL or an array of N doubles. */
+int hsmc_gpu_ql(hsmc_ctx *ctx, int l, double rc, double *ql_mean, double *per_particle);
+
+/* Random stream position for restart files, replacing the GSL state block of
+ * write_restart / read_restart (src/io_config.c:61-62, 115-116):
+ * state[0] = seed, state[1] = sweeps done, state[2] = Widom calls done,
+ * state[3] = reserved (0). */
+int hsmc_gpu_rng_state(hsmc_ctx *ctx, uint64_t out[4]);
+int hsmc_gpu_rng_set_state(hsmc_ctx *ctx, const uint64_t state[4]);
+
+/* Reference message for a status code (the printf text the reference emits
+ * before exit(EXIT_FAILURE)); never NULL. */
+const char *hsmc_gpu_strerror(int status);
+
+/* ----------------------------------------------------- replay and checks
+ * Entry points that evaluate the reference's decisions on given inputs
+ * without advancing the chain.  They exist so a caller (or a test) can compare
+ * decisions with the reference's own code on the same proposals. */
+
+/* Overlap decision of check_overlap (src/moves.c:157-212) for particle ids[k]
+ * placed at pos[3k..3k+2], each against the current configuration (no
+ * update between entries).  overlap[k] = 1 when rejected. */
+int hsmc_gpu_overlap_replay(hsmc_ctx *ctx, const int *ids, const double *pos, int n, uint8_t *overlap);
+
+/* Widom decisions (widom_check_overlap, src/compute_widom_chem_pot.c:82-120)
+ * for insertion points pos[3k..3k+2]. */
+int hsmc_gpu_widom_replay(hsmc_ctx *ctx, const double *pos, int n, uint8_t *overlap);
+
+/* Sweeps that also record every trial move:
+ * rec[k] = {pass, cell, trial, id, draw_x, draw_y, draw_z, decision,
+ *           shift_x, shift_y, shift_z (float bits), flags}
+ * (12 x uint32 per move; decision 0 accepted, 1 overlap, 2 left its cell).
+ * capacity is in records; *n_rec receives the count (HSMC_ERR_INVALID_ARG if
+ * it would exceed capacity). */
+int hsmc_gpu_sweeps_traced(hsmc_ctx *ctx, int n_sweeps, uint32_t *rec, int64_t capacity, int64_t *n_rec,
+                           uint64_t counters[6]);
+
+/* Geometry of the device cell grid used by the sweeps: nc[3], len32[3] and
+ * inv_w32[3] (float), capacity; for checking traced moves. */
+int hsmc_gpu_grid_info(hsmc_ctx *ctx, int nc[3], float len32[3], float inv_w32[3], int *capacity);
+
+/* Timing of the last sweep call, from CUDA events on the context's stream:
+ * total device time, and (only with profiling on) the summed time and count
+ * of the move-pass kernel launches.  With profiling on, sweeps are launched
+ * one kernel at a time with an event pair around each move pass instead of
+ * as a CUDA graph. */
+int hsmc_gpu_set_profiling(hsmc_ctx *ctx, int on);
+int hsmc_gpu_last_timing(hsmc_ctx *ctx, double *total_ms, double *move_kernel_ms, int *move_launches);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif

@@ -1,0 +1,162 @@
+"""GPU parity against the CPU oracle (the reference algorithm restated in C,
+pinned to the reference's own code by tests/test_oracle.py).
+
+Decisions and integer counts must be bit-identical; q_l, a floating-point
+mean, must agree to 1e-12 relative.  Every call goes through the C ABI.
+"""
+import math
+
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+
+def fluid(oracle_mod, gpu, rho, n, seed, dr, sweeps=30, neigh_dr=1.05):
+    """An oracle system run from the lattice (the reference's own chain) and a
+    GPU system started from the same configuration."""
+    o = oracle_mod.OracleSim(rho=rho, n_cells=n, seed=seed, dr_max=dr, neigh_dr=neigh_dr)
+    if sweeps:
+        o.sweeps_nvt(sweeps)
+    conf = o.get_config()
+    g = gpu.HardSphereSystem(rho=rho, cells=n, dr_max=dr, seed=seed + 1000, conf=conf)
+    return o, g, conf
+
+
+CASES = [(0.50, 5, 1, 0.3), (0.85, 6, 7, 0.12), (0.94, 5, 3, 0.08)]
+
+
+@pytest.mark.parametrize("rho,n,seed,dr", CASES)
+def test_overlap_decisions_bit_exact(oracle_mod, gpu_lib, rho, n, seed, dr):
+    o, g, conf = fluid(oracle_mod, gpu_lib, rho, n, seed, dr)
+    L = o.box()["lx"]
+    rng = np.random.default_rng(seed)
+    ids, pos = [], []
+    # ordinary trial moves (part_move arithmetic) ...
+    for _ in range(3000):
+        i = int(rng.integers(0, o.n))
+        u = rng.integers(0, 2**32 - 1, size=3, dtype=np.uint64).astype(np.float64) / 4294967295.0
+        p = conf[i, 1:] + (u - 0.5) * dr
+        p = np.where(p > L, p - L, np.where(p < 0.0, p + L, p))
+        ids.append(i)
+        pos.append(p)
+    # ... and adversarial ones at |r| = 1 within a few ulps of a neighbour
+    for _ in range(3000):
+        i = int(rng.integers(0, o.n))
+        j = int(rng.integers(0, o.n))
+        d = rng.normal(size=3)
+        d /= np.linalg.norm(d)
+        d *= 1.0 + rng.integers(-4, 5) * 2.0**-52
+        p = np.mod(conf[j, 1:] + d, L)
+        ids.append(i)
+        pos.append(p)
+    ids = np.array(ids, dtype=np.int32)
+    pos = np.array(pos)
+    got = g.overlap_replay(ids, pos)
+    want = np.array([o.check_overlap_at(int(i), *p) for i, p in zip(ids, pos)], dtype=np.uint8)
+    assert np.array_equal(got, want)
+    assert 0 < want.sum() < len(want)
+
+
+@pytest.mark.parametrize("rho,n,seed,dr", CASES + [(0.70, 10, 5, 0.2)])
+def test_traced_sweeps_replay_bit_exact(oracle_mod, gpu_lib, rho, n, seed, dr):
+    from oracle.philox import TAG_MOVE, draw4
+
+    o, g, conf = fluid(oracle_mod, gpu_lib, rho, n, seed, dr, sweeps=10)
+    sweeps = 4
+    rec, cnt = g.sweeps_traced(sweeps)
+    assert len(rec) == o.n * sweeps
+    assert cnt[0] == o.n * sweeps
+    order = np.lexsort((rec[:, 2], rec[:, 1], rec[:, 0]))
+    rec = rec[order]
+    # the recorded draws are the Philox stream the kernel was meant to use
+    r = draw4(seed + 1000, rec[:, 2], rec[:, 1], rec[:, 0].astype(np.uint64) + (np.uint64(0)), TAG_MOVE)
+    assert np.array_equal(rec[:, 4], r[1]) and np.array_equal(rec[:, 5], r[2]) and np.array_equal(rec[:, 6], r[3])
+    nc, l32, iw, _ = g.grid_info()
+    shifts = rec[:, 8:11].copy().view(np.float32)
+    o.reset_counters()
+    dec = o.replay_checkerboard(rec[:, 3].astype(np.int32), rec[:, 4:7], rec[:, 1], shifts, nc, l32, iw)
+    assert not np.any(dec == 3), "a traced particle was not in its cell"
+    assert np.array_equal(dec, rec[:, 7].astype(np.int32))
+    assert np.array_equal(o.get_config(), g.download())
+    assert cnt[1] == np.sum(dec == 0)
+
+
+@pytest.mark.parametrize("rho,n,seed,dr", CASES)
+def test_rdf_and_virial_counts_bit_exact(oracle_mod, gpu_lib, rho, n, seed, dr):
+    o, g, conf = fluid(oracle_mod, gpu_lib, rho, n, seed, dr)
+    hist, rmax = o.rdf_counts(0.01, 5.0)
+    got = g.compute_rdf_counts(0.01, rmax, len(hist))
+    assert np.array_equal(got, hist.astype(np.uint64))
+    assert np.array_equal(got, oracle_mod.OracleSim.brute_pair_hist(conf, [o.box()["lx"]] * 3, 0.01, rmax, len(hist)))
+    pv, prmax = o.pressv_counts(0.01)
+    gpv = g.compute_pressv_counts(0.01, prmax, len(pv))
+    assert np.array_equal(gpv, pv.astype(np.uint64))
+
+
+@pytest.mark.parametrize("rho,n,seed,dr", CASES)
+def test_thermo_pressure_scan_bit_exact(oracle_mod, gpu_lib, rho, n, seed, dr):
+    o, g, _ = fluid(oracle_mod, gpu_lib, rho, n, seed, dr)
+    xi = [(k + 1) * 0.0001 for k in range(int(0.002 / 0.0001))]
+    sf = np.array([math.pow(1 - x, 1.0 / 3.0) for x in xi])
+    assert np.array_equal(g.compute_presst(sf), o.presst_counts_sf(sf).astype(np.uint64))
+    assert np.array_equal(o.presst_counts_sf(sf), o.presst_counts(0.0001, 0.002))
+    for s in (0.99999, 0.9999, 0.999, 0.99):
+        assert g.scan_overlap(s) == o.scan_overlap(s)
+
+
+@pytest.mark.parametrize("rho,n,seed,dr", CASES)
+def test_widom_decisions_bit_exact(oracle_mod, gpu_lib, rho, n, seed, dr):
+    o, g, _ = fluid(oracle_mod, gpu_lib, rho, n, seed, dr)
+    L = o.box()["lx"]
+    raw = np.random.default_rng(seed).integers(0, 2**32 - 1, size=3 * 20000, dtype=np.uint32)
+    pos = (raw.astype(np.float64) / 4294967295.0 * L).reshape(-1, 3)
+    assert np.array_equal(g.widom_replay(pos), o.widom_decisions(raw))
+
+
+@pytest.mark.parametrize("rho,n,seed,dr", CASES)
+def test_ql_matches(oracle_mod, gpu_lib, rho, n, seed, dr):
+    o, g, _ = fluid(oracle_mod, gpu_lib, rho, n, seed, dr, neigh_dr=1.5)
+    for l in (4, 6):
+        mean, per, rc = o.ql(l, 1.5)
+        gm, gper = g.global_ql(l, rc, per_particle=True)
+        assert abs(gm - mean) <= 1e-12 * abs(mean)
+        assert np.max(np.abs(gper - per)) <= 1e-12
+
+
+def test_large_system_stays_overlap_free(oracle_mod, gpu_lib):
+    """N = 256,000 at rho = 0.85 from the FCC lattice: after sweeps every
+    particle passes the reference overlap test at its own position."""
+    g = gpu_lib.HardSphereSystem(rho=0.85, cells=40, dr_max=0.12, seed=11)
+    c = g.sweep_nvt(20)
+    assert c[0] == 256000 * 20
+    acc = c[1] / c[0]
+    assert 0.2 < acc < 0.9
+    conf = g.download()
+    ids = np.arange(g.n, dtype=np.int32)
+    assert g.overlap_replay(ids, conf[:, 1:]).sum() == 0
+    o = oracle_mod.OracleSim(rho=0.85, n_cells=40, seed=1, dr_max=0.12)
+    o.set_config(conf)
+    rng = np.random.default_rng(0)
+    for i in rng.integers(0, g.n, size=500):
+        assert o.check_overlap_at(int(i), *conf[i, 1:]) == 0
+    # integer g(r) counts of the full system: every pair counted from both ends
+    hist = g.compute_rdf_counts(0.01, 5.0, 400)
+    assert hist.sum() % 2 == 0 and hist[0] > 0
+
+
+def test_error_paths_report_reference_messages(gpu_lib):
+    conf = gpu_lib.lattice_config(0.5, (5, 5, 5))
+    g = gpu_lib.HardSphereSystem(rho=0.5, cells=5, conf=conf)
+    bad = conf.copy()
+    bad[3, 1] = -0.5
+    with pytest.raises(gpu_lib.HsmcError) as ei:
+        g.upload(bad)
+    assert ei.value.code == 8
+    crowd = conf.copy()
+    crowd[:, 1:] = 1.0  # every particle in one cell
+    with pytest.raises(gpu_lib.HsmcError) as ei:
+        g.upload(crowd)
+    assert ei.value.code == 4
+    g.upload(conf)
+    g.sweep_nvt(2)
