@@ -104,14 +104,17 @@ class ClockSampler:
                 "reasons": sorted(reasons), "samples": len(sm)}
 
 
-def tune_dr(sysm, dr0=0.12, sweeps=10, rounds=8):
+def tune_dr(sysm, dr0=0.12, sweeps=20, rounds=8):
     """Secant search of dr_max toward the target acceptance, as the
-    reference's optimiser does (src/optimizer.c:23-64)."""
+    reference's optimiser does (src/optimizer.c:23-64), after melting the
+    lattice start."""
     def acc(dr):
         sysm.set_step(dr)
         c = sysm.sweep_nvt(sweeps)
         return float(c[1]) / float(c[0])
 
+    sysm.set_step(dr0)
+    sysm.sweep_nvt(50)
     d1, a1 = dr0, acc(dr0)
     d2 = d1 * 2 if a1 > TARGET_ACC else d1 / 2
     a2 = acc(d2)

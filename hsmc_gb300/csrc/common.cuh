@@ -52,17 +52,53 @@ __host__ __device__ inline U32x4 draw4(uint64_t seed, uint32_t a, uint32_t b, ui
   return philox4x32_10(c, (uint32_t)seed, (uint32_t)(seed >> 32));
 }
 
-// The reference's uniform in [0, 1]: draw / (2^32 - 1) (src/rng.c:29-31).
-__device__ __forceinline__ double unit_closed(uint32_t r) { return __ddiv_rn((double)r, 4294967295.0); }
+// Exact dyadic numbers built from a 32-bit draw with integer operations only
+// (GB300 has a narrow FP64 pipe; none of this touches it).
+//   centred_offset(r) = (2r - 2^32 + 1) * 2^-33, odd multiples of 2^-33 in
+//                       (-1/2, 1/2), symmetric about 0: the trial step factor
+//                       (u - 0.5) of part_move (src/moves.c:52-54)
+//   open_unit(r)      = (2r + 1) * 2^-33 in (0, 1): the uniform of
+//                       widom_rand_pos and vol_move (src/compute_widom_chem_pot.c:76-78,
+//                       src/moves.c:91)
+// The reference draws u = r / (2^32 - 1) in [0, 1]; the same u is obtained
+// from the reference's own code with a generator maximum of 2^33 and the
+// draw 2r + 1, which is how the replay harness feeds it.
+__device__ __forceinline__ double dyadic_2m33(uint64_t mag, bool neg) {
+  // mag in [1, 2^33): value = mag * 2^-33, exactly representable
+  const int p = 63 - __clzll((long long)mag);              // leading bit, 0..32
+  const uint64_t mant = (mag << (52 - p)) & 0x000FFFFFFFFFFFFFull;
+  const uint64_t expo = (uint64_t)(p - 33 + 1023);
+  return __longlong_as_double((long long)(((uint64_t)neg << 63) | (expo << 52) | mant));
+}
+
+__device__ __forceinline__ double centred_offset(uint32_t r) {
+  const long long v = 2ll * (long long)r - 4294967295ll;  // odd, |v| < 2^32
+  return dyadic_2m33((uint64_t)(v < 0 ? -v : v), v < 0);
+}
+
+__device__ __forceinline__ double open_unit(uint32_t r) { return dyadic_2m33(2ull * r + 1ull, false); }
+
+// x < y for doubles by their bit patterns when y > 0 is finite: negative x
+// (sign bit set, not -0.0) is below; otherwise the patterns order as integers.
+__device__ __forceinline__ bool gt_pos(double x, double y) {
+  const long long a = __double_as_longlong(x), b = __double_as_longlong(y);
+  return a > b;  // x with sign bit set is a negative integer pattern: never > b > 0
+}
+
+__device__ __forceinline__ bool lt_zero(double x) {
+  const long long a = __double_as_longlong(x);
+  return a < 0 && (a & 0x7FFFFFFFFFFFFFFFll) != 0;  // -0.0 is not below zero
+}
 
 // ------------------------------------------------- reference arithmetic
 // Trial position x + (u - 0.5) * dr_max with no contraction
-// (src/moves.c:52-54), then the single periodic wrap of apply_pbc
-// (src/moves.c:215-226).
-__device__ __forceinline__ double propose_axis(double x, double u, double dr_max, double len) {
-  double v = __dadd_rn(x, __dmul_rn(__dsub_rn(u, 0.5), dr_max));
-  if (v > len) v = __dsub_rn(v, len);
-  else if (v < 0.0) v = __dadd_rn(v, len);
+// (src/moves.c:52-54), t = u - 0.5 given exactly, then the single periodic
+// wrap of apply_pbc (src/moves.c:215-226) with the comparisons done on bit
+// patterns: two FP64 operations per axis on the common path.
+__device__ __forceinline__ double propose_axis(double x, double t, double dr_max, double len) {
+  double v = __dadd_rn(x, __dmul_rn(t, dr_max));
+  if (gt_pos(v, len)) v = __dsub_rn(v, len);
+  else if (lt_zero(v)) v = __dadd_rn(v, len);
   return v;
 }
 

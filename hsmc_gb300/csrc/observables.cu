@@ -244,9 +244,9 @@ __global__ void __launch_bounds__(256) k_widom(SysPtrs p, long long n, unsigned 
       z = pos_in[3 * k + 2];
     } else {
       const U32x4 r = draw4(seed, (uint32_t)k, (uint32_t)(k >> 32), seq, TAG_WIDOM);
-      x = __dmul_rn(unit_closed(r.x), len[0]);
-      y = __dmul_rn(unit_closed(r.y), len[1]);
-      z = __dmul_rn(unit_closed(r.z), len[2]);
+      x = __dmul_rn(open_unit(r.x), len[0]);
+      y = __dmul_rn(open_unit(r.y), len[1]);
+      z = __dmul_rn(open_unit(r.z), len[2]);
     }
     const bool ov = point_overlaps(v, p, s, x, y, z, -1, len, half);
     if (ov_out) ov_out[k] = ov ? 1 : 0;

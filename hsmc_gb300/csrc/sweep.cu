@@ -240,9 +240,9 @@ __global__ void __launch_bounds__(256) k_move_pass(SysPtrs p, int pass) {
       const double mx = __shfl_sync(gmask, px, ml, G);
       const double my = __shfl_sync(gmask, py, ml, G);
       const double mz = __shfl_sync(gmask, pz, ml, G);
-      const double qx = propose_axis(mx, unit_closed(r.y), dr, len[0]);
-      const double qy = propose_axis(my, unit_closed(r.z), dr, len[1]);
-      const double qz = propose_axis(mz, unit_closed(r.w), dr, len[2]);
+      const double qx = propose_axis(mx, centred_offset(r.y), dr, len[0]);
+      const double qy = propose_axis(my, centred_offset(r.z), dr, len[1]);
+      const double qz = propose_axis(mz, centred_offset(r.w), dr, len[2]);
       int c0, c1, c2;
       float ux, uy, uz;
       axis_cell(__double2float_rn(qx), sh0, L32[0], iw[0], nc[0], c0, ux);

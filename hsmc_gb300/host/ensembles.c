@@ -1,0 +1,233 @@
+/*
+ * Ensemble drivers of the drop-in program: hs_nvt / run_nvt
+ * (src/nvt.c:30-199), hs_npt / run_npt (src/npt.c:25-175) and the
+ * displacement optimiser (src/optimizer.c:23-166), with the sweeps on the
+ * device.  Sampling happens before the sweep of the same index, as in the
+ * reference; consecutive sweeps with nothing to sample between them go to
+ * the device as one call.
+ */
+#include <stdio.h>
+#include <stdlib.h>
+#include <string.h>
+#include <time.h>
+
+#include "hsmc_host.h"
+
+static double wall_seconds(void) {
+  struct timespec ts;
+  clock_gettime(CLOCK_MONOTONIC, &ts);
+  return ts.tv_sec + 1e-9 * ts.tv_nsec;
+}
+
+static bool every(int ii, int interval) { return interval > 0 && ii % interval == 0; }
+
+/* Anything at sweep ii that needs the device state up to date? */
+static bool sampling_due(const host_input *in, int ii, bool prod, bool npt) {
+  if (every(ii, in->restart_write)) return true;
+  if (npt && every(ii, in->output_int)) return true; /* prints the density */
+  if (!prod) return false;
+  if (every(ii, in->config_write) || every(ii, in->presst_sample_int) || every(ii, in->ql_sample_int)) return true;
+  if (!npt && (every(ii, in->pressv_sample_int) || every(ii, in->mu_sample_int) || every(ii, in->rdf_sample_int)))
+    return true;
+  return false;
+}
+
+static void run_block(host_run *r, bool prod, int offset, bool npt) {
+  const host_input *in = &r->in;
+  if (in->output_int <= 0) {
+    printf("ERROR: the output interval (keyword out) must be positive\n");
+    exit(EXIT_FAILURE);
+  }
+  int n = prod ? in->sweep_stat : in->sweep_eq;
+  host_obs_state obs;
+  host_obs_begin(&obs);
+  int pending = 0;
+  for (int ii = offset; ii < n + offset; ii++) {
+    if (sampling_due(in, ii, prod, npt)) {
+      host_sweeps(r, pending, npt);
+      pending = 0;
+    }
+    if (!npt && ii == offset) printf("Sweep number\n");
+    if (npt && ii == 0) printf("Sweep number  Density\n");
+    if (ii % in->output_int == 0) {
+      if (npt) printf("%d  %.8f\n", ii, r->in.rho);
+      else printf("%d\n", ii);
+      fflush(stdout);
+    }
+    if (every(ii, in->restart_write)) host_write_restart(r, ii);
+    if (prod) {
+      if (every(ii, in->config_write)) host_write_config(r, ii);
+      if (!npt && every(ii, in->pressv_sample_int)) host_compute_pressv(r, &obs);
+      if (every(ii, in->presst_sample_int)) host_compute_presst(r, &obs);
+      if (every(ii, in->ql_sample_int)) host_compute_op(r, &obs);
+      if (!npt && every(ii, in->mu_sample_int)) host_compute_mu(r, &obs);
+      if (!npt && every(ii, in->rdf_sample_int)) host_compute_rdf(r, &obs, ii);
+    }
+    pending++;
+  }
+  host_sweeps(r, pending, npt);
+}
+
+/* get_sample_nvt / get_sample_npt (src/optimizer.c:66-78, 150-166). */
+static void sample_acceptance(host_run *r, int sweeps, bool npt, double *acc_part, double *acc_vol) {
+  host_reset_counters(r);
+  host_sweeps(r, sweeps, npt);
+  *acc_part = (double)r->counters[HSMC_CNT_ACCEPTED] / ((double)r->counters[HSMC_CNT_MOVES]);
+  if (acc_vol) *acc_vol = (double)r->counters[HSMC_CNT_VOL_ACCEPTED] / ((double)r->counters[HSMC_CNT_VOL_MOVES]);
+}
+
+/* opt_nvt (src/optimizer.c:23-64): secant search of dr_max. */
+static void opt_nvt(host_run *r) {
+  host_input *in = &r->in;
+  int per = in->opt_sweeps / in->opt_samples;
+  double a1, a2, d1, d2;
+  printf("---------------------------------------------------\n");
+  printf("Maximum displacement optimization started ...\n");
+  printf("Sweeps for optimization: %d\n", in->opt_sweeps);
+  printf("Number of samples: %d\n", in->opt_samples);
+  sample_acceptance(r, per, false, &a1, NULL);
+  d1 = in->dr_max;
+  if (a1 > in->opt_part_target) in->dr_max *= 2;
+  else in->dr_max /= 2;
+  sample_acceptance(r, per, false, &a2, NULL);
+  d2 = in->dr_max;
+  for (int k = 0; k < in->opt_samples; k++) {
+    in->dr_max = d2 - (a2 - in->opt_part_target) * (d2 - d1) / (a2 - a1);
+    if (in->dr_max > 1.0) {
+      in->dr_max = 1.0;
+    } else if (in->dr_max <= 0.0) {
+      in->dr_max = -in->dr_max;
+      if (in->dr_max > 1.0) in->dr_max = d2 / 2;
+    }
+    d1 = d2;
+    a1 = a2;
+    sample_acceptance(r, per, false, &a2, NULL);
+    d2 = in->dr_max;
+  }
+  printf("Optimal maximum displacement: %.8f\n", in->dr_max);
+  printf("Acceptance ratio: %.8f\n", a2);
+  printf("Maximum displacement optimization completed\n");
+}
+
+/* opt_npt (src/optimizer.c:83-148): secant search of dr_max and dv_max. */
+static void opt_npt(host_run *r) {
+  host_input *in = &r->in;
+  int per = in->opt_sweeps / in->opt_samples;
+  double ap1, ap2, av1, av2, d1, d2, v1, v2;
+  printf("---------------------------------------------------\n");
+  printf("Maximum displacement optimization started ...\n");
+  printf("Sweeps for optimization: %d\n", in->opt_sweeps);
+  printf("Number of samples: %d\n", in->opt_samples);
+  sample_acceptance(r, per, true, &ap1, &av1);
+  d1 = in->dr_max;
+  v1 = in->dv_max;
+  if (ap1 > in->opt_part_target) in->dr_max *= 2;
+  else in->dr_max /= 2;
+  if (av1 > in->opt_vol_target) in->dv_max *= 2;
+  else in->dv_max /= 2;
+  sample_acceptance(r, per, true, &ap2, &av2);
+  d2 = in->dr_max;
+  v2 = in->dv_max;
+  for (int k = 0; k < in->opt_samples; k++) {
+    in->dr_max = d2 - (ap2 - in->opt_part_target) * (d2 - d1) / (ap2 - ap1);
+    in->dv_max = v2 - (av2 - in->opt_vol_target) * (v2 - v1) / (av2 - av1);
+    if (in->dr_max > 1.0) in->dr_max = 1.0;
+    if (in->dr_max <= 0.0) {
+      in->dr_max = -in->dr_max;
+      if (in->dr_max > 1.0) in->dr_max = d2 / 2;
+    }
+    if (in->dv_max <= 0.0) {
+      in->dv_max = -in->dv_max;
+      if (in->dv_max > 0.1) in->dv_max = v2 / 2;
+    }
+    d1 = d2;
+    v1 = v2;
+    ap1 = ap2;
+    av1 = av2;
+    sample_acceptance(r, per, true, &ap2, &av2);
+    d2 = in->dr_max;
+    v2 = in->dv_max;
+  }
+  printf("Optimal maximum particle displacement: %.8f\n", in->dr_max);
+  printf("Acceptance ratio: %.8f \n", ap2);
+  printf("Optimal maximum volume deformation: %.8f\n", in->dv_max);
+  printf("Acceptance ratio: %.8f \n", av2);
+  printf("Maximum displacement optimization completed\n");
+}
+
+static void print_summary(const host_run *r, double seconds, bool npt) {
+  const uint64_t *c = r->counters;
+  printf("---------------------------------------------------\n");
+  printf("-- Particle moves: %.8e\n", (double)c[HSMC_CNT_MOVES]);
+  printf("   Acceptance percentage: %f\n", (double)c[HSMC_CNT_ACCEPTED] / ((double)c[HSMC_CNT_MOVES]));
+  printf("   Rejection percentage: %f\n", (double)c[HSMC_CNT_REJECTED] / ((double)c[HSMC_CNT_MOVES]));
+  if (npt) {
+    printf("-- Volume moves: %.8e\n", (double)c[HSMC_CNT_VOL_MOVES]);
+    printf("   Acceptance percentage: %f\n", (double)c[HSMC_CNT_VOL_ACCEPTED] / ((double)c[HSMC_CNT_VOL_MOVES]));
+    printf("   Rejection percentage: %f\n", (double)c[HSMC_CNT_VOL_REJECTED] / ((double)c[HSMC_CNT_VOL_MOVES]));
+  }
+  printf("Elapsed time: %f seconds\n", seconds);
+}
+
+static void start_system(host_run *r) {
+  if (r->in.restart_read == 0) {
+    host_box_init(r, r->in.type, r->in.nx, r->in.ny, r->in.nz, r->in.rho);
+    host_part_alloc(r);
+    host_part_init(r);
+  } else {
+    host_read_restart(r, r->in.restart_name);
+  }
+  host_print_sim_info(r);
+  host_cells_init(r, true);
+  host_gpu_open(r);
+  host_gpu_upload(r);
+}
+
+static void simulate(host_run *r, bool npt) {
+  double t0 = wall_seconds();
+  host_reset_counters(r);
+  printf("---------------------------------------------------\n");
+  printf("Equilibration...\n");
+  run_block(r, false, 0, npt);
+  printf("Equilibration completed.\n");
+  printf("---------------------------------------------------\n");
+  printf("Production...\n");
+  run_block(r, true, r->in.sweep_eq, npt);
+  printf("Production completed.\n");
+  print_summary(r, wall_seconds() - t0, npt);
+  hsmc_gpu_destroy(r->gpu);
+  r->gpu = NULL;
+  free(r->conf);
+  r->conf = NULL;
+}
+
+void host_nvt(host_run *r) {
+  start_system(r);
+  if (r->in.opt_flag == 1) {
+    opt_nvt(r);
+    host_part_init(r);
+    host_cells_init(r, false);
+    host_gpu_upload(r);
+  }
+  simulate(r, false);
+}
+
+void host_npt(host_run *r) {
+  start_system(r);
+  if (r->in.opt_flag == 1) {
+    double rho_start = r->in.rho;
+    opt_npt(r);
+    r->in.rho = rho_start;
+    host_box_init(r, r->in.type, r->in.nx, r->in.ny, r->in.nz, rho_start);
+    host_part_init(r);
+    host_cells_init(r, false);
+    /* the box changed back: a fresh device context for the lattice start */
+    uint64_t st[4];
+    host_gpu_check(hsmc_gpu_rng_state(r->gpu, st), "rng_state");
+    memcpy(r->rng_host, st, sizeof(st));
+    r->have_rng = true;
+    host_gpu_open(r);
+    host_gpu_upload(r);
+  }
+  simulate(r, true);
+}

@@ -48,7 +48,7 @@ int gsl_rng_fwrite(FILE *stream, const gsl_rng *r);
 int gsl_rng_fread(FILE *stream, gsl_rng *r);
 
 /* Replay support (not part of GSL). */
-void hsmc_shim_script_raw(const unsigned int *vals, size_t n);
+void hsmc_shim_script_raw(const unsigned long *vals, size_t n);
 void hsmc_shim_script_int(const int *vals, size_t n);
 void hsmc_shim_script_off(void);
 size_t hsmc_shim_script_left_raw(void);

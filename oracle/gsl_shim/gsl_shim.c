@@ -62,12 +62,12 @@ const gsl_rng_type *gsl_rng_mt19937 = &mt_type;
 
 /* ---------------------------------------------------------------- script */
 
-static const unsigned int *script_raw = NULL;
+static const unsigned long *script_raw = NULL;
 static size_t script_raw_n = 0, script_raw_pos = 0;
 static const int *script_int = NULL;
 static size_t script_int_n = 0, script_int_pos = 0;
 
-void hsmc_shim_script_raw(const unsigned int *vals, size_t n) {
+void hsmc_shim_script_raw(const unsigned long *vals, size_t n) {
   script_raw = vals;
   script_raw_n = n;
   script_raw_pos = 0;
@@ -115,7 +115,7 @@ unsigned long int gsl_rng_get(const gsl_rng *r) {
       fprintf(stderr, "gsl shim: scripted raw draws exhausted\n");
       exit(EXIT_FAILURE);
     }
-    return (unsigned long)script_raw[script_raw_pos++];
+    return script_raw[script_raw_pos++];
   }
   return mt_next((mt_state *)r->state);
 }

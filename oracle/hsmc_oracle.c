@@ -519,6 +519,41 @@ int hso_sweeps_npt(hso_sim *s, int n) {
   return s->err;
 }
 
+/* part_move (src/moves.c:27-80) with u - 0.5 = (2r - 2^32 + 1) * 2^-33 per
+ * axis, the step factor the GPU draws; the reference's own code forms the
+ * same value from the draw 2r + 1 with maximum 2^33. */
+int hso_replay_moves_offsets(hso_sim *s, int n, const int *ids, const uint32_t *raw, int *accepted) {
+  for (int k = 0; k < n; k++) {
+    int id = ids[k];
+    if (id < 0 || id >= s->n) return HSO_ERR_ARG;
+    double *p = s->conf[id];
+    double ox = p[1], oy = p[2], oz = p[3];
+    int c_old = cell_of_particle(s, id);
+    for (int d = 0; d < 3; d++) {
+      double t = (double)(2 * (long long)raw[3 * k + d] - 4294967295LL) * 0x1p-33;
+      p[1 + d] += t * s->dr_max;
+    }
+    wrap_into_box(s, p);
+    accepted[k] = 0;
+    if (overlap_of(s, id, 1.0)) {
+      p[1] = ox;
+      p[2] = oy;
+      p[3] = oz;
+      s->rej++;
+    } else {
+      int c_new = cell_of_particle(s, id);
+      if (c_new != c_old) {
+        int e = cell_move(s, c_old, c_new, id);
+        if (e) return e;
+      }
+      s->acc++;
+      accepted[k] = 1;
+    }
+    s->moves++;
+  }
+  return s->err;
+}
+
 int hso_replay_moves(hso_sim *s, int n, const int *ids, const uint32_t *raw, int *accepted) {
   script_set(s, raw, 3 * (size_t)n, ids, (size_t)n);
   for (int k = 0; k < n; k++) accepted[k] = particle_move(s);
@@ -661,6 +696,17 @@ int hso_widom_decisions(hso_sim *s, int n, const uint32_t *raw, uint8_t *overlap
 }
 
 int hso_widom_rng(hso_sim *s, int n) { return hso_widom_decisions(s, n, NULL, NULL); }
+
+int hso_widom_points(hso_sim *s, int n, const double *pts, uint8_t *overlap) {
+  int ok = 0;
+  for (int k = 0; k < n; k++) {
+    int ov = insertion_overlaps(s, pts[3 * k], pts[3 * k + 1], pts[3 * k + 2]);
+    if (ov < 0) return -1;
+    if (overlap) overlap[k] = (uint8_t)ov;
+    if (!ov) ok++;
+  }
+  return ok;
+}
 
 /* src/compute_order_parameter.c:25-229 */
 double hso_ql(hso_sim *s, int l, double rc, double *per_particle, double *rc_used) {
@@ -832,13 +878,13 @@ int hso_replay_checkerboard(hso_sim *s, int n, const int *ids, const uint32_t *r
       decision[k] = 3;
       continue;
     }
-    double ux = (double)raw[3 * k] / (double)4294967295u;
-    double uy = (double)raw[3 * k + 1] / (double)4294967295u;
-    double uz = (double)raw[3 * k + 2] / (double)4294967295u;
+    /* u - 0.5 for the draw r: (2r - 2^32 + 1) * 2^-33 (exact), the value the
+     * reference's own part_move forms from the draw 2r + 1 with maximum 2^33 */
     double q[4] = {p[0], p[1], p[2], p[3]};
-    q[1] += (ux - 0.5) * s->dr_max;
-    q[2] += (uy - 0.5) * s->dr_max;
-    q[3] += (uz - 0.5) * s->dr_max;
+    for (int d = 0; d < 3; d++) {
+      double t = (double)(2 * (long long)raw[3 * k + d] - 4294967295LL) * 0x1p-33;
+      q[1 + d] += t * s->dr_max;
+    }
     wrap_into_box(s, q);
     if (flat_cell32(q, sh, nc, len32, inv_w32) != cells[k]) {
       decision[k] = 2;

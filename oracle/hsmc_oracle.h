@@ -50,6 +50,7 @@ void hso_counters(const hso_sim *s, unsigned long long *out6);
 void hso_reset_counters(hso_sim *s);
 
 int hso_replay_moves(hso_sim *s, int n, const int *ids, const uint32_t *raw, int *accepted);
+int hso_replay_moves_offsets(hso_sim *s, int n, const int *ids, const uint32_t *raw, int *accepted);
 int hso_check_overlap_at(hso_sim *s, int i, double x, double y, double z);
 int hso_scan_overlap(hso_sim *s, double sf);
 int hso_vol_move_replay(hso_sim *s, const uint32_t *raw, int n_raw);
@@ -61,6 +62,7 @@ int hso_presst_counts_sf(hso_sim *s, const double *sf, int n, double *out);
 int hso_widom(hso_sim *s, int n, const uint32_t *raw);
 int hso_widom_decisions(hso_sim *s, int n, const uint32_t *raw, uint8_t *overlap);
 int hso_widom_rng(hso_sim *s, int n);
+int hso_widom_points(hso_sim *s, int n, const double *pts, uint8_t *overlap);
 double hso_ql(hso_sim *s, int l, double rc, double *per_particle, double *rc_used);
 int hso_opt_nvt(hso_sim *s, int opt_sweeps, int opt_samples, double target, double *dr_out, double *acc_out);
 
@@ -74,7 +76,9 @@ int hso_brute_pair_hist(const double *conf, int n, double lx, double ly, double 
                         int nbins, unsigned long long *counts);
 
 /* Replay of trial moves made by a checkerboard sweep.  Move k moves particle
- * ids[k] with displacement draws raw[3k..3k+2]; the move must stay in the
+ * ids[k] by (2r - 2^32 + 1) * 2^-33 * dr_max per axis for the draws
+ * r = raw[3k..3k+2] (the reference's part_move arithmetic with u - 0.5 given
+ * exactly); the move must stay in the
  * cell cells[k] of the shifted grid described by shift32[3k..3k+2] and the
  * per-axis (nc, length_f32, inv_width_f32).  decision[k] receives
  * 0 = accepted, 1 = rejected for overlap, 2 = rejected for leaving the cell,

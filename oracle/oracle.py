@@ -100,6 +100,15 @@ class _SimBase:
         self._lib_replay(ids.size, ids, raw, acc)
         return acc
 
+    def replay_moves_offsets(self, ids, raw) -> np.ndarray:
+        """part_move with the device's exact step factor (2r - 2^32 + 1) * 2^-33."""
+        ids = np.ascontiguousarray(ids, dtype=np.int32)
+        raw = np.ascontiguousarray(raw, dtype=np.uint32).reshape(-1)
+        assert raw.size == 3 * ids.size
+        acc = np.zeros(ids.size, dtype=np.int32)
+        self._lib_replay_offsets(ids.size, ids, raw, acc)
+        return acc
+
     def rdf_counts(self, dr: float, rmax: float, max_bins: int = 100000):
         out = np.zeros(max_bins, dtype=np.float64)
         used = C.c_double()
@@ -161,6 +170,8 @@ class OracleSim(_SimBase):
             L.hso_counters.argtypes = [C.c_void_p, _u64p]
             L.hso_reset_counters.argtypes = [C.c_void_p]
             L.hso_replay_moves.argtypes = [C.c_void_p, C.c_int, _i32p, _u32p, _i32p]
+            L.hso_replay_moves_offsets.argtypes = [C.c_void_p, C.c_int, _i32p, _u32p, _i32p]
+            L.hso_widom_points.argtypes = [C.c_void_p, C.c_int, _dp, _u8p]
             L.hso_check_overlap_at.argtypes = [C.c_void_p, C.c_int, C.c_double, C.c_double, C.c_double]
             L.hso_scan_overlap.argtypes = [C.c_void_p, C.c_double]
             L.hso_vol_move_replay.argtypes = [C.c_void_p, _u32p, C.c_int]
@@ -243,6 +254,16 @@ class OracleSim(_SimBase):
 
     def _lib_replay(self, n, ids, raw, acc):
         self._lib.hso_replay_moves(self._h, n, ids, raw, acc)
+
+    def _lib_replay_offsets(self, n, ids, raw, acc):
+        self._lib.hso_replay_moves_offsets(self._h, n, ids, raw, acc)
+
+    def widom_points(self, pts):
+        pts = np.ascontiguousarray(pts, dtype=np.float64).reshape(-1, 3)
+        ov = np.zeros(pts.shape[0], dtype=np.uint8)
+        if self._lib.hso_widom_points(self._h, pts.shape[0], pts, ov) < 0:
+            raise ValueError("insertion point outside the cell table")
+        return ov
 
     def check_overlap_at(self, i, x, y, z) -> int:
         return self._lib.hso_check_overlap_at(self._h, i, x, y, z)
@@ -360,6 +381,7 @@ class RefSim(_SimBase):
             L.ref_sweeps_npt.argtypes = [C.c_int]
             L.ref_counters.argtypes = [_u64p]
             L.ref_replay_moves.argtypes = [C.c_int, _i32p, _u32p, _i32p]
+            L.ref_replay_moves_offsets.argtypes = [C.c_int, _i32p, _u32p, _i32p]
             L.ref_check_overlap_at.argtypes = [C.c_int, C.c_double, C.c_double, C.c_double]
             L.ref_scan_overlap.argtypes = [C.c_double]
             L.ref_vol_move_replay.argtypes = [_u32p, C.c_int]
@@ -420,6 +442,9 @@ class RefSim(_SimBase):
 
     def _lib_replay(self, n, ids, raw, acc):
         self._lib.ref_replay_moves(n, ids, raw, acc)
+
+    def _lib_replay_offsets(self, n, ids, raw, acc):
+        self._lib.ref_replay_moves_offsets(n, ids, raw, acc)
 
     def check_overlap_at(self, i, x, y, z) -> int:
         return self._lib.ref_check_overlap_at(i, x, y, z)

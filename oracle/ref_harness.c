@@ -47,6 +47,7 @@ extern double *presst_hist;
 extern int wtest;
 extern double ql_ave;
 extern double *ql;
+extern unsigned long r_num_max;
 
 void global_ql_compute();
 void ql_alloc();
@@ -132,15 +133,44 @@ void ref_reset_counters(void) { reset_moves_counters(); }
 /* Run part_move() once per entry with scripted draws: ids[k] is returned by
  * rng_get_int and raw[3k..3k+2] by the three rng_get_double calls.
  * accepted[k] receives 1 when the reference accepted the move. */
+static unsigned long *widen(const unsigned int *raw, size_t n, int offset_form) {
+  unsigned long *w = malloc(sizeof(unsigned long) * (n ? n : 1));
+  for (size_t k = 0; k < n; k++) w[k] = offset_form ? 2ul * raw[k] + 1ul : raw[k];
+  return w;
+}
+
 int ref_replay_moves(int n, const int *ids, const unsigned int *raw, int *accepted) {
+  unsigned long *w = widen(raw, 3 * (size_t)n, 0);
   hsmc_shim_script_int(ids, (size_t)n);
-  hsmc_shim_script_raw(raw, 3 * (size_t)n);
+  hsmc_shim_script_raw(w, 3 * (size_t)n);
   for (int k = 0; k < n; k++) {
     unsigned long before = acc_part_moves;
     part_move();
     accepted[k] = acc_part_moves != before;
   }
   hsmc_shim_script_off();
+  free(w);
+  return 0;
+}
+
+/* part_move() driven by the device's draws: with the generator maximum set to
+ * 2^33 and the draw 2r + 1, rng_get_double returns (2r + 1) / 2^33, so the
+ * reference forms u - 0.5 = (2r - 2^32 + 1) * 2^-33 exactly as the device
+ * does.  The maximum is restored afterwards. */
+int ref_replay_moves_offsets(int n, const int *ids, const unsigned int *raw, int *accepted) {
+  unsigned long *w = widen(raw, 3 * (size_t)n, 1);
+  unsigned long saved = r_num_max;
+  r_num_max = 8589934592ul;
+  hsmc_shim_script_int(ids, (size_t)n);
+  hsmc_shim_script_raw(w, 3 * (size_t)n);
+  for (int k = 0; k < n; k++) {
+    unsigned long before = acc_part_moves;
+    part_move();
+    accepted[k] = acc_part_moves != before;
+  }
+  hsmc_shim_script_off();
+  r_num_max = saved;
+  free(w);
   return 0;
 }
 
@@ -170,10 +200,12 @@ int ref_scan_overlap(double sf) {
 /* One vol_move() with scripted uniforms (raw[0] for the volume, raw[1] for the
  * acceptance test when it is drawn).  Returns 1 when accepted. */
 int ref_vol_move_replay(const unsigned int *raw, int n_raw) {
-  hsmc_shim_script_raw(raw, (size_t)n_raw);
+  unsigned long *w = widen(raw, (size_t)n_raw, 0);
+  hsmc_shim_script_raw(w, (size_t)n_raw);
   unsigned long before = acc_vol_moves;
   vol_move();
   hsmc_shim_script_off();
+  free(w);
   return acc_vol_moves != before;
 }
 
@@ -229,10 +261,12 @@ int ref_presst_counts(double dxi, double xi_max, double *out, int max_n) {
 /* Widom insertions with scripted uniforms (3 per insertion); returns the
  * number of insertions without overlap. */
 int ref_widom(int n, const unsigned int *raw) {
+  unsigned long *w = widen(raw, 3 * (size_t)n, 0);
   G_IN.mu_insertions = n;
-  hsmc_shim_script_raw(raw, 3 * (size_t)n);
+  hsmc_shim_script_raw(w, 3 * (size_t)n);
   widom_insertion();
   hsmc_shim_script_off();
+  free(w);
   return wtest;
 }
 

@@ -63,6 +63,10 @@ def main() -> None:
         out[f"{name}/replay_raw"] = mraw
         out[f"{name}/replay_acc"] = r.replay_moves(ids, mraw)
         out[f"{name}/replay_config"] = r.get_config()
+        oraw = rng.integers(0, 2**32, size=3 * 300, dtype=np.uint64).astype(np.uint32)
+        out[f"{name}/offset_raw"] = oraw
+        out[f"{name}/offset_acc"] = r.replay_moves_offsets(ids, oraw)
+        out[f"{name}/offset_config"] = r.get_config()
     out["mt/seed4357_first16"] = RefSim.rng_raw(4357, 16)
     out["mt/seed0_first16"] = RefSim.rng_raw(0, 16)
     out["mt/seed5489_10000"] = RefSim.rng_raw(5489, 10000)[-16:]

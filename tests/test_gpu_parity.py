@@ -15,7 +15,8 @@ pytestmark = pytest.mark.gpu
 def fluid(oracle_mod, gpu, rho, n, seed, dr, sweeps=30, neigh_dr=1.05):
     """An oracle system run from the lattice (the reference's own chain) and a
     GPU system started from the same configuration."""
-    o = oracle_mod.OracleSim(rho=rho, n_cells=n, seed=seed, dr_max=dr, neigh_dr=neigh_dr)
+    o = oracle_mod.OracleSim(rho=rho, n_cells=n, seed=seed, dr_max=dr, neigh_dr=neigh_dr,
+                             neigh_max_part=10 if neigh_dr < 1.2 else 40)
     if sweeps:
         o.sweeps_nvt(sweeps)
     conf = o.get_config()
@@ -112,6 +113,13 @@ def test_widom_decisions_bit_exact(oracle_mod, gpu_lib, rho, n, seed, dr):
     raw = np.random.default_rng(seed).integers(0, 2**32 - 1, size=3 * 20000, dtype=np.uint32)
     pos = (raw.astype(np.float64) / 4294967295.0 * L).reshape(-1, 3)
     assert np.array_equal(g.widom_replay(pos), o.widom_decisions(raw))
+    # the device's own insertion points: (2r + 1) * 2^-33 * L
+    pos2 = ((2.0 * raw.astype(np.float64) + 1.0) * 2.0**-33 * L).reshape(-1, 3)
+    ov = g.widom_replay(pos2)
+    assert np.array_equal(ov, o.widom_points(pos2))
+    # the device's random insertions count the same decisions on average
+    ok = g.widom_insertion(20000)
+    assert abs(ok / 20000 - (1 - ov.mean())) < 5 * np.sqrt(max(ov.mean() * (1 - ov.mean()), 1e-4) / 20000) + 1e-3
 
 
 @pytest.mark.parametrize("rho,n,seed,dr", CASES)

@@ -146,6 +146,10 @@ def test_oracle_matches_reference_fixtures(oracle_mod, golden, name):
     acc = o.replay_moves(golden[f"{name}/replay_ids"], golden[f"{name}/replay_raw"])
     assert np.array_equal(acc, golden[f"{name}/replay_acc"])
     assert np.array_equal(o.get_config(), golden[f"{name}/replay_config"])
+    # the GPU's step factor, through the reference's own part_move
+    acc = o.replay_moves_offsets(golden[f"{name}/replay_ids"], golden[f"{name}/offset_raw"])
+    assert np.array_equal(acc, golden[f"{name}/offset_acc"])
+    assert np.array_equal(o.get_config(), golden[f"{name}/offset_config"])
 
 
 def test_mt_fixtures(oracle_mod, golden):
@@ -181,3 +185,7 @@ def test_oracle_matches_reference_side_by_side(oracle_mod, ref_available):
             assert o.check_overlap_at(i, *p) == r.check_overlap_at(i, *p)
         for sf in (0.9999, 0.999, 0.99):
             assert o.scan_overlap(sf) == r.scan_overlap(sf)
+        ids = rng.integers(0, o.n, size=4000).astype(np.int32)
+        raw = rng.integers(0, 2**32, size=12000, dtype=np.uint64).astype(np.uint32)
+        assert np.array_equal(o.replay_moves_offsets(ids, raw), r.replay_moves_offsets(ids, raw))
+        assert np.array_equal(o.get_config(), r.get_config())
