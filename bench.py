@@ -213,6 +213,7 @@ def run_gpu_arm(args):
 
     sysm = hsmc_gb300.HardSphereSystem(rho=RHO, cells=CELLS, dr_max=0.12, seed=2026 + rank)
     dr, acc = tune_dr(sysm)
+    lanes = sysm.autotune(5)
     # The reference restarts from the lattice after optimising (src/nvt.c:58-62).
     sysm.upload(hsmc_gb300.lattice_config(RHO, (CELLS,) * 3))
     sysm.set_step(dr)
@@ -290,6 +291,7 @@ def run_gpu_arm(args):
         "config": {"workload": "NVT fluid N=256000 (40^3 FCC) rho=0.85 cubic periodic, FP64 positions, "
                                "checkerboard sweeps", "n_particles": N, "rho": RHO,
                    "sweeps_per_step": SWEEPS_PER_STEP, "dr_max": dr, "acceptance": acc_moves / max(moves, 1),
+                   "lanes_per_cell": lanes,
                    "l2": "flushed between steps (256 MB write)", "parallelism": f"replicas x{world}"},
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                      "frac": achieved / peak, "traffic": float(traffic) if traffic else None,

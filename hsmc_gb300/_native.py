@@ -42,7 +42,8 @@ class HsmcParams(C.Structure):
         ("pressure", C.c_double),
         ("seed", C.c_uint64),
         ("cell_capacity", C.c_int),
-        ("reserved", C.c_int * 7),
+        ("lanes_per_cell", C.c_int),
+        ("reserved", C.c_int * 6),
     ]
 
 
@@ -91,6 +92,7 @@ def load() -> C.CDLL:
     L.hsmc_gpu_sweeps_traced.argtypes = [_vp, C.c_int, _vp, C.c_int64, _P(C.c_int64), _vp]
     L.hsmc_gpu_grid_info.argtypes = [_vp, _vp, _vp, _vp, _P(C.c_int)]
     L.hsmc_gpu_set_profiling.argtypes = [_vp, C.c_int]
+    L.hsmc_gpu_autotune.argtypes = [_vp, C.c_int, _P(C.c_int)]
     L.hsmc_gpu_last_timing.argtypes = [_vp, _P(C.c_double), _P(C.c_double), _P(C.c_int)]
     _lib = L
     return L

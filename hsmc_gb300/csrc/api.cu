@@ -23,6 +23,7 @@ using namespace hsmc;
 namespace {
 
 constexpr int kGraphSweeps = 8;
+constexpr int kDefaultLanes = 2;  // lanes per active cell in a move pass
 
 struct Scratch {
   void *ptr = nullptr;
@@ -58,7 +59,9 @@ struct hsmc_ctx {
   unsigned long long widom_seq = 0;
   bool uploaded = false;
   bool profiling = false;
-  cudaGraphExec_t graph = nullptr;
+  cudaGraphExec_t graph = nullptr;      // NVT: kGraphSweeps x (build + 8 passes) + advance
+  cudaGraphExec_t graph_npt = nullptr;  // NpT: the same plus one volume move per sweep
+  double margin = 0.0;                  // grid margin over 1 of the cell edge
   cudaEvent_t ev_start = nullptr, ev_stop = nullptr;
   std::vector<cudaEvent_t> ev_pass;
   double last_total_ms = 0.0, last_move_ms = 0.0;
@@ -191,6 +194,14 @@ int hsmc_gpu_create(const hsmc_params *prm, hsmc_ctx **out) {
   const double rho = prm->n_particles / (prm->box[0] * prm->box[1] * prm->box[2]);
   int e = make_box(prm->box, prm->rho > 0 ? prm->rho : rho, b, cap);
   if (e) return e;
+  // NpT boxes change: cells are allocated for a box 25% longer per side, and
+  // the grid margin is fixed for that largest box.
+  Box balloc = b;
+  int cap_alloc = cap;
+  if (prm->pressure > 0) {
+    const double grown[3] = {prm->box[0] * 1.25, prm->box[1] * 1.25, prm->box[2] * 1.25};
+    if ((e = make_box(grown, b.rho, balloc, cap_alloc))) return e;
+  }
   if (prm->cell_capacity > 0) {
     if (prm->cell_capacity > 32) return HSMC_ERR_INVALID_ARG;
     cap = prm->cell_capacity <= 8 ? 8 : (prm->cell_capacity <= 16 ? 16 : 32);
@@ -201,11 +212,20 @@ int hsmc_gpu_create(const hsmc_params *prm, hsmc_ctx **out) {
   ctx->n = prm->n_particles;
   ctx->num_sms = p.multiProcessorCount;
   ctx->hbox = b;
-  ctx->group = cap;
+  switch (prm->lanes_per_cell) {
+    case 0: ctx->group = kDefaultLanes; break;
+    case 1: case 2: case 4: case 8: ctx->group = prm->lanes_per_cell; break;
+    default: delete ctx; return HSMC_ERR_INVALID_ARG;
+  }
   SysPtrs &sp = ctx->sp;
   sp.n = ctx->n;
   sp.cap = cap;
-  sp.ncell_alloc = b.ncell;
+  sp.ncell_alloc = balloc.ncell;
+  {
+    double lmax = balloc.len[0];
+    for (int d = 1; d < 3; d++) lmax = balloc.len[d] > lmax ? balloc.len[d] : lmax;
+    ctx->margin = 5.9604644775390625e-08 * (64.0 * lmax + 64.0);
+  }
   auto fail = [&](cudaError_t err) {
     hsmc_gpu_destroy(ctx);
     return cuda_status(err);
@@ -227,6 +247,11 @@ int hsmc_gpu_create(const hsmc_params *prm, hsmc_ctx **out) {
   s0.dv_max = prm->dv_max;
   s0.pressure = prm->pressure;
   s0.seed = prm->seed;
+  s0.per_cell = prm->lattice_type == 1 ? 1 : 4;
+  for (int d = 0; d < 3; d++) {
+    s0.cells[d] = prm->cells[d];
+    s0.nc_alloc[d] = balloc.nc[d];
+  }
   if ((ce = cudaMemcpy(sp.st, &s0, sizeof(DevState), cudaMemcpyHostToDevice)) != cudaSuccess) return fail(ce);
   if ((ce = cudaEventCreate(&ctx->ev_start)) != cudaSuccess) return fail(ce);
   if ((ce = cudaEventCreate(&ctx->ev_stop)) != cudaSuccess) return fail(ce);
@@ -239,6 +264,7 @@ void hsmc_gpu_destroy(hsmc_ctx *ctx) {
   if (!ctx) return;
   if (ctx->stream) cudaStreamSynchronize(ctx->stream);
   if (ctx->graph) cudaGraphExecDestroy(ctx->graph);
+  if (ctx->graph_npt) cudaGraphExecDestroy(ctx->graph_npt);
   SysPtrs &sp = ctx->sp;
   cudaFree(sp.pos);
   for (int l = 0; l < 2; l++) {
@@ -320,29 +346,39 @@ int hsmc_gpu_last_timing(hsmc_ctx *ctx, double *total_ms, double *move_kernel_ms
   return HSMC_OK;
 }
 
-static void enqueue_sweep(hsmc_ctx *ctx, long long offset, bool trace) {
+static void enqueue_sweep(hsmc_ctx *ctx, long long offset, bool trace, bool npt) {
   launch_build(ctx->sp, offset, ctx->num_sms, ctx->stream);
   for (int k = 0; k < 8; k++) launch_move_pass(ctx->sp, k, ctx->group, trace, ctx->pass_grid, ctx->stream);
+  if (npt) launch_volume_move(ctx->sp, offset, ctx->margin, ctx->stream);
 }
 
-static int ensure_graph(hsmc_ctx *ctx) {
-  if (ctx->graph) return HSMC_OK;
+static int ensure_graph(hsmc_ctx *ctx, bool npt) {
+  cudaGraphExec_t &exec = npt ? ctx->graph_npt : ctx->graph;
+  if (exec) return HSMC_OK;
   cudaGraph_t g = nullptr;
   HSMC_CUDA(cudaStreamBeginCapture(ctx->stream, cudaStreamCaptureModeThreadLocal));
-  for (int s = 0; s < kGraphSweeps; s++) enqueue_sweep(ctx, s, false);
+  for (int s = 0; s < kGraphSweeps; s++) enqueue_sweep(ctx, s, false, npt);
   launch_advance(ctx->sp, kGraphSweeps, ctx->stream);
   cudaError_t e = cudaStreamEndCapture(ctx->stream, &g);
   if (e != cudaSuccess) return cuda_status(e);
-  e = cudaGraphInstantiate(&ctx->graph, g, 0);
+  e = cudaGraphInstantiate(&exec, g, 0);
   cudaGraphDestroy(g);
   if (e != cudaSuccess) {
-    ctx->graph = nullptr;
+    exec = nullptr;
     return cuda_status(e);
   }
   return HSMC_OK;
 }
 
-static int run_sweeps(hsmc_ctx *ctx, int n_sweeps, bool trace, uint64_t counters[6]) {
+// Rebuilds the layout of the last sweep in place (after volume moves the
+// positions no longer match it), so observables see a consistent layout.
+static void rebuild_current_layout(hsmc_ctx *ctx) {
+  const int layout = (int)((ctx->sweep_base - 1) & 1ull);
+  cudaMemsetAsync(ctx->sp.cnt[layout], 0, sizeof(int) * (size_t)ctx->sp.ncell_alloc, ctx->stream);
+  launch_build(ctx->sp, -1, ctx->num_sms, ctx->stream);
+}
+
+static int run_sweeps(hsmc_ctx *ctx, int n_sweeps, bool trace, bool npt, uint64_t counters[6]) {
   if (!ctx || n_sweeps < 0) return HSMC_ERR_INVALID_ARG;
   if (!ctx->uploaded) return HSMC_ERR_INVALID_ARG;
   clear_counters_async(ctx);
@@ -351,10 +387,11 @@ static int run_sweeps(hsmc_ctx *ctx, int n_sweeps, bool trace, uint64_t counters
   ctx->last_move_launches = 0;
   const bool direct = trace || ctx->profiling;
   if (!direct) {
-    int e = ensure_graph(ctx);
+    int e = ensure_graph(ctx, npt);
     if (e) return e;
   }
-  if (ctx->profiling && !trace) {
+  const bool timing = ctx->profiling && !trace;
+  if (timing) {
     const size_t need = 16 * (size_t)n_sweeps;
     while (ctx->ev_pass.size() < need) {
       cudaEvent_t ev;
@@ -366,7 +403,7 @@ static int run_sweeps(hsmc_ctx *ctx, int n_sweeps, bool trace, uint64_t counters
   int done = 0;
   if (!direct) {
     while (n_sweeps - done >= kGraphSweeps) {
-      HSMC_CUDA(cudaGraphLaunch(ctx->graph, ctx->stream));
+      HSMC_CUDA(cudaGraphLaunch(npt ? ctx->graph_npt : ctx->graph, ctx->stream));
       done += kGraphSweeps;
     }
   }
@@ -374,20 +411,22 @@ static int run_sweeps(hsmc_ctx *ctx, int n_sweeps, bool trace, uint64_t counters
   for (int s = 0; s < rest; s++) {
     launch_build(ctx->sp, s, ctx->num_sms, ctx->stream);
     for (int k = 0; k < 8; k++) {
-      if (ctx->profiling && !trace) HSMC_CUDA(cudaEventRecord(ctx->ev_pass[16 * s + 2 * k], ctx->stream));
+      if (timing) HSMC_CUDA(cudaEventRecord(ctx->ev_pass[16 * s + 2 * k], ctx->stream));
       launch_move_pass(ctx->sp, k, ctx->group, trace, ctx->pass_grid, ctx->stream);
-      if (ctx->profiling && !trace) HSMC_CUDA(cudaEventRecord(ctx->ev_pass[16 * s + 2 * k + 1], ctx->stream));
+      if (timing) HSMC_CUDA(cudaEventRecord(ctx->ev_pass[16 * s + 2 * k + 1], ctx->stream));
     }
+    if (npt) launch_volume_move(ctx->sp, s, ctx->margin, ctx->stream);
   }
   if (rest > 0) launch_advance(ctx->sp, rest, ctx->stream);
   HSMC_CUDA(cudaEventRecord(ctx->ev_stop, ctx->stream));
+  ctx->sweep_base += (unsigned long long)n_sweeps;
+  if (npt && n_sweeps > 0) rebuild_current_layout(ctx);
   int e = check_kernels(ctx);
   if (e) return e;
-  ctx->sweep_base += (unsigned long long)n_sweeps;
   float ms = 0.f;
   HSMC_CUDA(cudaEventElapsedTime(&ms, ctx->ev_start, ctx->ev_stop));
   ctx->last_total_ms = ms;
-  if (ctx->profiling && !trace) {
+  if (timing) {
     double sum = 0.0;
     for (int s = 0; s < rest; s++)
       for (int k = 0; k < 8; k++) {
@@ -400,6 +439,9 @@ static int run_sweeps(hsmc_ctx *ctx, int n_sweeps, bool trace, uint64_t counters
   }
   DevState s;
   if ((e = read_state(ctx, s))) return e;
+  if (npt) {
+    HSMC_CUDA(cudaMemcpy(&ctx->hbox, ctx->sp.box, sizeof(Box), cudaMemcpyDeviceToHost));
+  }
   if (counters) {
     const uint64_t moves = (uint64_t)ctx->n * (uint64_t)n_sweeps;
     counters[HSMC_CNT_MOVES] = moves;
@@ -413,16 +455,45 @@ static int run_sweeps(hsmc_ctx *ctx, int n_sweeps, bool trace, uint64_t counters
   return HSMC_OK;
 }
 
+int hsmc_gpu_autotune(hsmc_ctx *ctx, int sweeps_per_variant, int *lanes_out) {
+  if (!ctx || sweeps_per_variant <= 0 || !ctx->uploaded) return HSMC_ERR_INVALID_ARG;
+  const int options[4] = {1, 2, 4, 8};
+  const bool was_profiling = ctx->profiling;
+  const bool npt = ctx->prm.pressure > 0;
+  ctx->profiling = true;
+  int best = ctx->group;
+  double best_ms = 1e300;
+  for (int v = 0; v < 4; v++) {
+    ctx->group = options[v];
+    ctx->pass_grid = move_pass_grid(ctx->group, ctx->sp.cap, ctx->sp.ncell_alloc, ctx->num_sms);
+    int e = run_sweeps(ctx, sweeps_per_variant, false, npt, nullptr);
+    if (e) {
+      ctx->profiling = was_profiling;
+      return e;
+    }
+    if (ctx->last_move_ms < best_ms) {
+      best_ms = ctx->last_move_ms;
+      best = options[v];
+    }
+  }
+  ctx->profiling = was_profiling;
+  ctx->group = best;
+  ctx->pass_grid = move_pass_grid(ctx->group, ctx->sp.cap, ctx->sp.ncell_alloc, ctx->num_sms);
+  if (ctx->graph) cudaGraphExecDestroy(ctx->graph);
+  if (ctx->graph_npt) cudaGraphExecDestroy(ctx->graph_npt);
+  ctx->graph = ctx->graph_npt = nullptr;
+  if (lanes_out) *lanes_out = best;
+  return HSMC_OK;
+}
+
 int hsmc_gpu_sweeps(hsmc_ctx *ctx, int n_sweeps, uint64_t counters[6]) {
   if (!ctx || ctx->prm.pressure > 0) return HSMC_ERR_INVALID_ARG;
-  return run_sweeps(ctx, n_sweeps, false, counters);
+  return run_sweeps(ctx, n_sweeps, false, false, counters);
 }
 
 int hsmc_gpu_npt_sweeps(hsmc_ctx *ctx, int n_sweeps, uint64_t counters[6]) {
-  (void)ctx;
-  (void)n_sweeps;
-  (void)counters;
-  return HSMC_ERR_INVALID_ARG;  // provided by the NpT driver
+  if (!ctx || !(ctx->prm.pressure > 0)) return HSMC_ERR_INVALID_ARG;
+  return run_sweeps(ctx, n_sweeps, false, true, counters);
 }
 
 int hsmc_gpu_sweeps_traced(hsmc_ctx *ctx, int n_sweeps, uint32_t *rec, int64_t capacity, int64_t *n_rec,
@@ -431,7 +502,7 @@ int hsmc_gpu_sweeps_traced(hsmc_ctx *ctx, int n_sweeps, uint32_t *rec, int64_t c
   HSMC_CUDA(ctx->trace.ensure(sizeof(uint32_t) * 12 * (size_t)capacity));
   ctx->sp.trace = (uint32_t *)ctx->trace.ptr;
   ctx->sp.trace_cap = (unsigned long long)capacity;
-  int e = run_sweeps(ctx, n_sweeps, true, counters);
+  int e = run_sweeps(ctx, n_sweeps, true, ctx->prm.pressure > 0, counters);
   ctx->sp.trace = nullptr;
   ctx->sp.trace_cap = 0;
   DevState s;
@@ -522,15 +593,17 @@ int hsmc_gpu_presst(hsmc_ctx *ctx, const double *sf, int n_sf, uint64_t *nonover
 }
 
 int hsmc_gpu_scan_overlap(hsmc_ctx *ctx, double sf, int *overlap) {
-  if (!overlap) return HSMC_ERR_INVALID_ARG;
-  if (sf >= 1.0) {  // expansion: scaled distances never shrink
-    *overlap = 0;
-    return HSMC_OK;
-  }
-  unsigned long long m[4];
-  int e = scaled_scan(ctx, &sf, 1, m);
+  if (!ctx || !overlap || !ctx->uploaded || !(sf > 0.5 && sf <= 2.0)) return HSMC_ERR_INVALID_ARG;
+  // The kernel the NpT volume move runs, on a caller-given scale factor.
+  const int zero = 0;
+  HSMC_CUDA(cudaMemcpyAsync(&ctx->sp.st->vol_sf, &sf, sizeof(double), cudaMemcpyHostToDevice, ctx->stream));
+  HSMC_CUDA(cudaMemcpyAsync(&ctx->sp.st->vol_overlap, &zero, sizeof(int), cudaMemcpyHostToDevice, ctx->stream));
+  launch_volume_scan(ctx->sp, ctx->stream);
+  int e = check_kernels(ctx);
   if (e) return e;
-  *overlap = (int)(m[0] & 1ull);
+  int ov = 0;
+  HSMC_CUDA(cudaMemcpy(&ov, &ctx->sp.st->vol_overlap, sizeof(int), cudaMemcpyDeviceToHost));
+  *overlap = ov ? 1 : 0;
   return HSMC_OK;
 }
 

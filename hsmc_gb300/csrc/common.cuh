@@ -195,6 +195,13 @@ struct DevState {
   int status;
   int pad;
   SweepParams params;
+  // NpT: the trial volume move of the current sweep and the lattice the box
+  // is rebuilt from (sim_box_init, src/sim_info.c:32-71)
+  double vol_sf, vol_new, vol_ratio, vol_u_acc;
+  int vol_overlap, vol_accept;
+  int cells[3], per_cell;
+  int nc_alloc[3];
+  int pad2;
 };
 
 struct alignas(16) Slot {  // one particle in a cell: single-precision copy + id

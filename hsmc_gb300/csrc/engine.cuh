@@ -27,6 +27,8 @@ struct SysPtrs {
 void launch_build(const SysPtrs &p, long long sweep_offset, int num_sms, cudaStream_t s);
 void launch_move_pass(const SysPtrs &p, int pass, int group, bool trace, int grid, cudaStream_t s);
 void launch_advance(const SysPtrs &p, int n_sweeps, cudaStream_t s);
+void launch_volume_move(const SysPtrs &p, long long sweep_offset, double margin, cudaStream_t s);
+void launch_volume_scan(const SysPtrs &p, cudaStream_t s);
 int move_pass_grid(int group, int cap, int ncell_alloc, int num_sms);
 
 // observables.cu

@@ -72,19 +72,6 @@ __global__ void __launch_bounds__(256) k_build(SysPtrs p, long long offset) {
 
 // ------------------------------------------------------------- move pass
 
-// One pair of the single-precision screen: d = t_mover - t_other.  Returns
-// the overlap decision, re-evaluating in FP64 (reference arithmetic, mover
-// first as in check_overlap) when r^2 is within the band of 1.
-__device__ __forceinline__ bool pair_overlaps(float dx, float dy, float dz, float band, double mx, double my,
-                                              double mz, double ox, double oy, double oz, const double *len,
-                                              const double *half, unsigned long long &rechecks) {
-  const float r2 = dx * dx + dy * dy + dz * dz;
-  if (r2 < 1.0f - band) return true;
-  if (r2 > 1.0f + band) return false;
-  rechecks++;
-  return ref_r2(mx, my, mz, ox, oy, oz, len, half) < 1.0;
-}
-
 __device__ __forceinline__ void load_xyz(const double *pos, int id, double &x, double &y, double &z) {
   const double2 a = *reinterpret_cast<const double2 *>(pos + 4 * (size_t)id);
   const double2 b = *reinterpret_cast<const double2 *>(pos + 4 * (size_t)id + 2);
@@ -93,32 +80,56 @@ __device__ __forceinline__ void load_xyz(const double *pos, int id, double &x, d
   z = b.y;
 }
 
-template <int G, int CAP, int NCAND, bool TRACE>
-__global__ void __launch_bounds__(256) k_move_pass(SysPtrs p, int pass) {
-  static_assert(CAP <= G, "each lane holds at most one particle of its cell");
-  static_assert(G == 8 || G == 16 || G == 32, "group size");
-  constexpr int GPB = 256 / G;               // groups per block
-  constexpr int NB = (26 + G - 1) / G;        // neighbour cells per lane
-  __shared__ float4 cand[GPB][NCAND];
+// Minimum-image difference of two single-precision coordinates in [0, L].
+__device__ __forceinline__ float wrap_diff(float d, float len, float half) {
+  if (d > half) d -= len;
+  else if (d < -half) d += len;
+  return d;
+}
+
+// Single-precision screen of one pair, with the FP64 re-evaluation (the
+// reference's compute_dist arithmetic, mover first as in check_overlap) for
+// pairs whose r^2 lies within the guard band of 1.
+__device__ __forceinline__ bool screen_pair(float dx, float dy, float dz, float band, double mx, double my,
+                                            double mz, const double *pos, int other, const double *len,
+                                            const double *half, unsigned &rechecks) {
+  const float r2 = dx * dx + dy * dy + dz * dz;
+  if (r2 < 1.0f - band) return true;
+  if (r2 > 1.0f + band) return false;
+  rechecks++;
+  double ox, oy, oz;
+  load_xyz(pos, other, ox, oy, oz);
+  return ref_r2(mx, my, mz, ox, oy, oz, len, half) < 1.0;
+}
+
+// One colour pass.  A group of G lanes owns one active cell at a time; every
+// lane keeps its own copy of the cell's particles (so the trial sequence
+// needs no broadcasts), the 26 neighbour cells are split across the lanes,
+// and the lanes agree on each decision with one ballot.
+template <int G, int CAP, bool TRACE>
+__global__ void __launch_bounds__(128) k_move_pass(SysPtrs p, int pass) {
+  static_assert(G == 1 || G == 2 || G == 4 || G == 8, "group size");
+  constexpr int NB = (26 + G - 1) / G;  // neighbour cells per lane
 
   const DevState *st = p.st;
   const Box *bx = p.box;
   const unsigned long long sweep = st->params.sweep;
   const int layout = (int)(sweep & 1ull);
   const int colour = st->params.perm[pass];
-  const float sh0 = st->params.shift32[0], sh1 = st->params.shift32[1], sh2 = st->params.shift32[2];
+  const float sh[3] = {st->params.shift32[0], st->params.shift32[1], st->params.shift32[2]};
   const double dr = st->dr_max;
   const unsigned long long seed = st->seed;
   const unsigned long long seq = sweep * 8ull + (unsigned long long)pass;
   const double len[3] = {bx->len[0], bx->len[1], bx->len[2]};
   const double half[3] = {bx->half[0], bx->half[1], bx->half[2]};
   const float L32[3] = {bx->len32[0], bx->len32[1], bx->len32[2]};
+  const float H32[3] = {0.5f * bx->len32[0], 0.5f * bx->len32[1], 0.5f * bx->len32[2]};
   const float iw[3] = {bx->inv_w32[0], bx->inv_w32[1], bx->inv_w32[2]};
   const int nc[3] = {bx->nc[0], bx->nc[1], bx->nc[2]};
   const float band = bx->band;
   const int *__restrict__ cnt = p.cnt[layout];
   Slot *__restrict__ slot = p.slot[layout];
-  const double *__restrict__ pos = p.pos;
+  double *__restrict__ pos = p.pos;
 
   // The first pass of a sweep clears the other layout for the next build.
   if (pass == 0) {
@@ -126,17 +137,18 @@ __global__ void __launch_bounds__(256) k_move_pass(SysPtrs p, int pass) {
     for (int c = blockIdx.x * blockDim.x + threadIdx.x; c < p.ncell_alloc; c += gridDim.x * blockDim.x) other[c] = 0;
   }
 
-  const int lane = threadIdx.x % G;
-  const int gib = threadIdx.x / G;
-  const int gbase = (threadIdx.x & 31) & ~(G - 1);
+  const int lane = (int)(threadIdx.x % G);
+  const int group = (int)((blockIdx.x * blockDim.x + threadIdx.x) / G);
+  const int groups = (int)((gridDim.x * blockDim.x) / G);
+  const int gbase = (int)((threadIdx.x & 31) & ~(G - 1));
   const unsigned gmask = (G == 32) ? 0xffffffffu : (((1u << G) - 1u) << gbase);
   const int hx = nc[0] >> 1, hy = nc[1] >> 1, hz = nc[2] >> 1;
   const int n_active = hx * hy * hz;
   const int cx = colour & 1, cy = (colour >> 1) & 1, cz = (colour >> 2) & 1;
 
-  unsigned long long acc = 0, rej_o = 0, rej_b = 0, rechecks = 0;
+  unsigned acc = 0, rej_o = 0, rej_b = 0, rechecks = 0;
 
-  for (int ac = blockIdx.x * GPB + gib; ac < n_active; ac += gridDim.x * GPB) {
+  for (int ac = group; ac < n_active; ac += groups) {
     const int ax = ac % hx, ayz = ac / hx, ay = ayz % hy, az = ayz / hy;
     const int ix = 2 * ax + cx, iy = 2 * ay + cy, iz = 2 * az + cz;
     const int c = ix + nc[0] * (iy + nc[1] * iz);
@@ -147,165 +159,104 @@ __global__ void __launch_bounds__(256) k_move_pass(SysPtrs p, int pass) {
       continue;
     }
 
-    // Own particles: lane l < n holds particle l of the cell.
-    double px = 0.0, py = 0.0, pz = 0.0;
-    float tx = 0.f, ty = 0.f, tz = 0.f;
-    int pid = 0x7fffffff;
-    if (lane < n) {
-      const Slot sv = slot[(size_t)c * CAP + lane];
-      pid = sv.id;
-      load_xyz(pos, pid, px, py, pz);
-      int ci;
-      axis_cell(sv.x, sh0, L32[0], iw[0], nc[0], ci, tx);
-      axis_cell(sv.y, sh1, L32[1], iw[1], nc[1], ci, ty);
-      axis_cell(sv.z, sh2, L32[2], iw[2], nc[2], ci, tz);
+    // The cell's particles, in id order so the chain does not depend on the
+    // order in which the build's atomics filled the slots.
+    double qx[CAP], qy[CAP], qz[CAP];
+    float fx[CAP], fy[CAP], fz[CAP];
+    int qid[CAP], qslot[CAP];
+    for (int j = 0; j < n; j++) {
+      const Slot sv = slot[(size_t)c * CAP + j];
+      int at = j;
+      while (at > 0 && qid[at - 1] > sv.id) {
+        qid[at] = qid[at - 1];
+        qslot[at] = qslot[at - 1];
+        at--;
+      }
+      qid[at] = sv.id;
+      qslot[at] = j;
     }
-    // Moves visit the cell's particles by rank of id, so the chain does not
-    // depend on the order atomics filled the slots.
-    int rank = 0;
-#pragma unroll
-    for (int j = 0; j < G; j++) {
-      const int o = __shfl_sync(gmask, pid, j, G);
-      rank += (o < pid) ? 1 : 0;
+    for (int j = 0; j < n; j++) {
+      load_xyz(pos, qid[j], qx[j], qy[j], qz[j]);
+      fx[j] = __double2float_rn(qx[j]);
+      fy[j] = __double2float_rn(qy[j]);
+      fz[j] = __double2float_rn(qz[j]);
     }
 
-    // Stage the 26 neighbour cells' particles in shared memory, as grid
-    // coordinates t with the periodic image already applied.
-    int nb_c[NB];
-    float nb_img[NB][3];
-    int nb_n[NB];
-    int mine = 0;
+    // This lane's neighbour cells (the centre cell excluded).
+    const int xm = ix == 0 ? nc[0] - 1 : ix - 1, xp = ix == nc[0] - 1 ? 0 : ix + 1;
+    const int ym = iy == 0 ? nc[1] - 1 : iy - 1, yp = iy == nc[1] - 1 ? 0 : iy + 1;
+    const int zm = iz == 0 ? nc[2] - 1 : iz - 1, zp = iz == nc[2] - 1 ? 0 : iz + 1;
+    int nb_c[NB], nb_n[NB];
 #pragma unroll
     for (int q = 0; q < NB; q++) {
       const int o26 = lane + q * G;
       nb_n[q] = 0;
       nb_c[q] = 0;
       if (o26 < 26) {
-        const int o = o26 < 13 ? o26 : o26 + 1;  // skip the centre (13)
-        const int off[3] = {o / 9 - 1, (o / 3) % 3 - 1, o % 3 - 1};
-        const int base[3] = {ix, iy, iz};
-        int idx[3];
-#pragma unroll
-        for (int d = 0; d < 3; d++) {
-          int v = base[d] + off[d];
-          float img = 0.f;
-          if (v < 0) {
-            v += nc[d];
-            img = -L32[d];
-          } else if (v >= nc[d]) {
-            v -= nc[d];
-            img = L32[d];
-          }
-          idx[d] = v;
-          nb_img[q][d] = img;
-        }
-        nb_c[q] = idx[0] + nc[0] * (idx[1] + nc[1] * idx[2]);
+        const int o = o26 < 13 ? o26 : o26 + 1;
+        const int a = o / 9, b = (o / 3) % 3, e = o % 3;
+        const int x = a == 0 ? xm : (a == 1 ? ix : xp);
+        const int y = b == 0 ? ym : (b == 1 ? iy : yp);
+        const int z = e == 0 ? zm : (e == 1 ? iz : zp);
+        nb_c[q] = x + nc[0] * (y + nc[1] * z);
         const int m = cnt[nb_c[q]];
         nb_n[q] = m < CAP ? m : CAP;  // an overfull cell was flagged by the build
-        mine += nb_n[q];
       }
     }
-    int incl = mine;
-#pragma unroll
-    for (int d = 1; d < G; d <<= 1) {
-      const int v = __shfl_up_sync(gmask, incl, d, G);
-      if (lane >= d) incl += v;
-    }
-    const int total = __shfl_sync(gmask, incl, G - 1, G);
-    const bool staged = total <= NCAND;
-    if (staged) {
-      int w = incl - mine;
-#pragma unroll
-      for (int q = 0; q < NB; q++) {
-        for (int k = 0; k < nb_n[q]; k++) {
-          const Slot sv = slot[(size_t)nb_c[q] * CAP + k];
-          int ci;
-          float a0, a1, a2;
-          axis_cell(sv.x, sh0, L32[0], iw[0], nc[0], ci, a0);
-          axis_cell(sv.y, sh1, L32[1], iw[1], nc[1], ci, a1);
-          axis_cell(sv.z, sh2, L32[2], iw[2], nc[2], ci, a2);
-          cand[gib][w++] = make_float4(__fadd_rn(a0, nb_img[q][0]), __fadd_rn(a1, nb_img[q][1]),
-                                       __fadd_rn(a2, nb_img[q][2]), __int_as_float(sv.id));
-        }
-      }
-    }
-    __syncwarp(gmask);
 
-    bool moved = false;
+    unsigned moved = 0;
     for (int trial = 0; trial < n; trial++) {
       const U32x4 r = draw4(seed, (uint32_t)trial, (uint32_t)c, seq, TAG_MOVE);
-      const int pick = (int)__umulhi(r.x, (unsigned)n);
-      const unsigned sel = __ballot_sync(gmask, lane < n && rank == pick);
-      const int ml = __ffs(sel >> gbase) - 1;
-      const double mx = __shfl_sync(gmask, px, ml, G);
-      const double my = __shfl_sync(gmask, py, ml, G);
-      const double mz = __shfl_sync(gmask, pz, ml, G);
-      const double qx = propose_axis(mx, centred_offset(r.y), dr, len[0]);
-      const double qy = propose_axis(my, centred_offset(r.z), dr, len[1]);
-      const double qz = propose_axis(mz, centred_offset(r.w), dr, len[2]);
+      const int s = (int)__umulhi(r.x, (unsigned)n);  // rank of the moving particle
+      const double nx = propose_axis(qx[s], centred_offset(r.y), dr, len[0]);
+      const double ny = propose_axis(qy[s], centred_offset(r.z), dr, len[1]);
+      const double nz = propose_axis(qz[s], centred_offset(r.w), dr, len[2]);
+      const float gx = __double2float_rn(nx), gy = __double2float_rn(ny), gz = __double2float_rn(nz);
       int c0, c1, c2;
-      float ux, uy, uz;
-      axis_cell(__double2float_rn(qx), sh0, L32[0], iw[0], nc[0], c0, ux);
-      axis_cell(__double2float_rn(qy), sh1, L32[1], iw[1], nc[1], c1, uy);
-      axis_cell(__double2float_rn(qz), sh2, L32[2], iw[2], nc[2], c2, uz);
+      float t;
+      axis_cell(gx, sh[0], L32[0], iw[0], nc[0], c0, t);
+      axis_cell(gy, sh[1], L32[1], iw[1], nc[1], c1, t);
+      axis_cell(gz, sh[2], L32[2], iw[2], nc[2], c2, t);
+      const unsigned rc_before = rechecks;
       int decision;
-      unsigned rc_before = (unsigned)rechecks;
       if (c0 != ix || c1 != iy || c2 != iz) {
-        decision = 2;
+        decision = 2;  // the move would leave the active cell
       } else {
         bool ov = false;
-        if (lane < n && lane != ml)
-          ov = pair_overlaps(ux - tx, uy - ty, uz - tz, band, qx, qy, qz, px, py, pz, len, half, rechecks);
-        if (staged) {
-          for (int j = lane; j < total && !ov; j += G) {
-            const float4 cd = cand[gib][j];
-            const float dx = ux - cd.x, dy = uy - cd.y, dz = uz - cd.z;
-            const float r2 = dx * dx + dy * dy + dz * dz;
-            if (r2 < 1.0f - band) {
-              ov = true;
-            } else if (r2 <= 1.0f + band) {
-              double ox, oy, oz;
-              load_xyz(pos, __float_as_int(cd.w), ox, oy, oz);
-              rechecks++;
-              ov = ref_r2(qx, qy, qz, ox, oy, oz, len, half) < 1.0;
-            }
-          }
-        } else {
-          // Too many neighbours to stage: read them straight from the slots.
-#pragma unroll
-          for (int q = 0; q < NB; q++) {
-            for (int k = 0; k < nb_n[q] && !ov; k++) {
-              const Slot sv = slot[(size_t)nb_c[q] * CAP + k];
-              int ci;
-              float a0, a1, a2;
-              axis_cell(sv.x, sh0, L32[0], iw[0], nc[0], ci, a0);
-              axis_cell(sv.y, sh1, L32[1], iw[1], nc[1], ci, a1);
-              axis_cell(sv.z, sh2, L32[2], iw[2], nc[2], ci, a2);
-              const float dx = ux - __fadd_rn(a0, nb_img[q][0]);
-              const float dy = uy - __fadd_rn(a1, nb_img[q][1]);
-              const float dz = uz - __fadd_rn(a2, nb_img[q][2]);
-              const float r2 = dx * dx + dy * dy + dz * dz;
-              if (r2 < 1.0f - band) {
-                ov = true;
-              } else if (r2 <= 1.0f + band) {
-                double ox, oy, oz;
-                load_xyz(pos, sv.id, ox, oy, oz);
-                rechecks++;
-                ov = ref_r2(qx, qy, qz, ox, oy, oz, len, half) < 1.0;
-              }
-            }
+        for (int j = lane; j < n && !ov; j += G) {
+          if (j == s) continue;
+          const float dx = wrap_diff(gx - fx[j], L32[0], H32[0]);
+          const float dy = wrap_diff(gy - fy[j], L32[1], H32[1]);
+          const float dz = wrap_diff(gz - fz[j], L32[2], H32[2]);
+          const float r2 = dx * dx + dy * dy + dz * dz;
+          if (r2 < 1.0f - band) {
+            ov = true;
+          } else if (r2 <= 1.0f + band) {
+            rechecks++;
+            ov = ref_r2(nx, ny, nz, qx[j], qy[j], qz[j], len, half) < 1.0;
           }
         }
-        decision = __ballot_sync(gmask, ov) ? 1 : 0;
+#pragma unroll
+        for (int q = 0; q < NB; q++) {
+          for (int k = 0; k < nb_n[q] && !ov; k++) {
+            const Slot o = slot[(size_t)nb_c[q] * CAP + k];
+            const float dx = wrap_diff(gx - o.x, L32[0], H32[0]);
+            const float dy = wrap_diff(gy - o.y, L32[1], H32[1]);
+            const float dz = wrap_diff(gz - o.z, L32[2], H32[2]);
+            ov = screen_pair(dx, dy, dz, band, nx, ny, nz, pos, o.id, len, half, rechecks);
+          }
+        }
+        if (G > 1) ov = __ballot_sync(gmask, ov) != 0u;
+        decision = ov ? 1 : 0;
       }
-      if (decision == 0 && lane == ml) {
-        px = qx;
-        py = qy;
-        pz = qz;
-        tx = ux;
-        ty = uy;
-        tz = uz;
-        moved = true;
+      if (decision == 0) {
+        qx[s] = nx;
+        qy[s] = ny;
+        qz[s] = nz;
+        fx[s] = gx;
+        fy[s] = gy;
+        fz[s] = gz;
+        moved |= 1u << s;
       }
       if (lane == 0) {
         acc += decision == 0;
@@ -313,8 +264,8 @@ __global__ void __launch_bounds__(256) k_move_pass(SysPtrs p, int pass) {
         rej_b += decision == 2;
       }
       if (TRACE) {
-        const unsigned any_rc = __ballot_sync(gmask, (unsigned)rechecks != rc_before);
-        const int mid = __shfl_sync(gmask, pid, ml, G);
+        bool any_rc = rechecks != rc_before;
+        if (G > 1) any_rc = __ballot_sync(gmask, any_rc) != 0u;
         if (lane == 0) {
           const unsigned long long at = atomicAdd(&p.st->trace_count, 1ull);
           if (at < p.trace_cap) {
@@ -322,14 +273,14 @@ __global__ void __launch_bounds__(256) k_move_pass(SysPtrs p, int pass) {
             rec[0] = (uint32_t)seq;
             rec[1] = (uint32_t)c;
             rec[2] = (uint32_t)trial;
-            rec[3] = (uint32_t)mid;
+            rec[3] = (uint32_t)qid[s];
             rec[4] = r.y;
             rec[5] = r.z;
             rec[6] = r.w;
             rec[7] = (uint32_t)decision;
-            rec[8] = __float_as_uint(sh0);
-            rec[9] = __float_as_uint(sh1);
-            rec[10] = __float_as_uint(sh2);
+            rec[8] = __float_as_uint(sh[0]);
+            rec[9] = __float_as_uint(sh[1]);
+            rec[10] = __float_as_uint(sh[2]);
             rec[11] = any_rc ? 1u : 0u;
           } else {
             atomicOr(&p.st->status, ST_TRACE_FULL);
@@ -337,31 +288,178 @@ __global__ void __launch_bounds__(256) k_move_pass(SysPtrs p, int pass) {
         }
       }
     }
-    __syncwarp(gmask);
-
-    if (moved) {
-      double *pp = p.pos + 4 * (size_t)pid;
-      pp[1] = px;
-      pp[2] = py;
-      pp[3] = pz;
-      slot[(size_t)c * CAP + lane] = Slot{__double2float_rn(px), __double2float_rn(py), __double2float_rn(pz), pid};
+    if (G > 1) __syncwarp(gmask);
+    for (int j = lane; j < n; j += G) {
+      if (!((moved >> j) & 1u)) continue;
+      double *pp = pos + 4 * (size_t)qid[j];
+      pp[1] = qx[j];
+      pp[2] = qy[j];
+      pp[3] = qz[j];
+      slot[(size_t)c * CAP + qslot[j]] = Slot{fx[j], fy[j], fz[j], qid[j]};
     }
   }
 
-  acc = warp_sum_u64(acc);
-  rej_o = warp_sum_u64(rej_o);
-  rej_b = warp_sum_u64(rej_b);
-  rechecks = warp_sum_u64(rechecks);
+  unsigned long long a64 = warp_sum_u64(acc), o64 = warp_sum_u64(rej_o), b64 = warp_sum_u64(rej_b),
+                     r64 = warp_sum_u64(rechecks);
   if ((threadIdx.x & 31) == 0) {
     DevState *ws = p.st;
-    if (acc) atomicAdd(&ws->acc, acc);
-    if (rej_o) atomicAdd(&ws->rej_overlap, rej_o);
-    if (rej_b) atomicAdd(&ws->rej_boundary, rej_b);
-    if (rechecks) atomicAdd(&ws->rechecks, rechecks);
+    if (a64) atomicAdd(&ws->acc, a64);
+    if (o64) atomicAdd(&ws->rej_overlap, o64);
+    if (b64) atomicAdd(&ws->rej_boundary, b64);
+    if (r64) atomicAdd(&ws->rechecks, r64);
   }
 }
 
 __global__ void k_advance(DevState *st, int n) { st->sweep_base += (unsigned long long)n; }
+
+// ------------------------------------------------------------ volume move
+// vol_move (src/moves.c:83-153) as four launches so it stays on the device:
+// propose (1 thread), scaled overlap scan (N threads, early exit once an
+// overlap is seen), decide and rebuild the box (1 thread), rescale (N threads).
+
+// ln V' = ln V + (u - 1/2) dv_max; sf = (V'/V)^(1/3).
+__global__ void k_vol_propose(SysPtrs p, long long offset) {
+  DevState *st = p.st;
+  const Box *bx = p.box;
+  const unsigned long long s = st->sweep_base + (unsigned long long)offset;
+  const U32x4 r = draw4(st->seed, 0u, 0u, s, TAG_VOLUME);
+  const double vol = bx->vol;
+  const double log_new = log(vol) + centred_offset(r.x) * st->dv_max;
+  const double vol_new = exp(log_new);
+  const double ratio = vol_new / vol;
+  st->vol_sf = pow(ratio, 1. / 3.);
+  st->vol_new = vol_new;
+  st->vol_ratio = ratio;
+  st->vol_u_acc = open_unit(r.y);
+  st->vol_overlap = 0;
+  st->vol_accept = 0;
+  st->vol_moves += 1;
+}
+
+// check_overlap(i, sf, sf, sf) for every i (src/moves.c:104-112).  A scale
+// factor >= 1 cannot bring a pair closer than it is, so nothing runs then.
+__global__ void __launch_bounds__(256) k_vol_scan(SysPtrs p) {
+  const DevState *st = p.st;
+  const double sf = st->vol_sf;
+  if (!(sf < 1.0)) return;
+  if (*(volatile const int *)&st->vol_overlap) return;
+  const Box *bx = p.box;
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= p.n) return;
+  const int layout = (int)(st->params.sweep & 1ull);
+  const int *cnt = p.cnt[layout];
+  const Slot *slot = p.slot[layout];
+  const double len[3] = {bx->len[0], bx->len[1], bx->len[2]};
+  const float L32[3] = {bx->len32[0], bx->len32[1], bx->len32[2]};
+  const float iw[3] = {bx->inv_w32[0], bx->inv_w32[1], bx->inv_w32[2]};
+  const float sh[3] = {st->params.shift32[0], st->params.shift32[1], st->params.shift32[2]};
+  const int nc[3] = {bx->nc[0], bx->nc[1], bx->nc[2]};
+  const float reach = (float)(1.0 / sf) + 1e-3f;
+  double x, y, z;
+  load_xyz(p.pos, i, x, y, z);
+  const float xs[3] = {__double2float_rn(x), __double2float_rn(y), __double2float_rn(z)};
+  int ci[3], k[3];
+  for (int d = 0; d < 3; d++) {
+    float t;
+    axis_cell(xs[d], sh[d], L32[d], iw[d], nc[d], ci[d], t);
+    k[d] = (int)ceilf(reach * iw[d] * 1.0001f);
+    if (2 * k[d] + 1 > nc[d]) k[d] = -1;
+  }
+  bool ov = false;
+  for (int a = (k[2] < 0 ? 0 : -k[2]); !ov && a <= (k[2] < 0 ? nc[2] - 1 : k[2]); a++) {
+    const int cz = k[2] < 0 ? a : (ci[2] + a + nc[2]) % nc[2];
+    for (int b = (k[1] < 0 ? 0 : -k[1]); !ov && b <= (k[1] < 0 ? nc[1] - 1 : k[1]); b++) {
+      const int cy = k[1] < 0 ? b : (ci[1] + b + nc[1]) % nc[1];
+      for (int e = (k[0] < 0 ? 0 : -k[0]); !ov && e <= (k[0] < 0 ? nc[0] - 1 : k[0]); e++) {
+        const int cx = k[0] < 0 ? e : (ci[0] + e + nc[0]) % nc[0];
+        const int c = cx + nc[0] * (cy + nc[1] * cz);
+        const int m = cnt[c];
+        const int n = m < p.cap ? m : p.cap;
+        for (int q = 0; q < n && !ov; q++) {
+          const Slot o = slot[(size_t)c * p.cap + q];
+          if (o.id == i) continue;
+          float dx = xs[0] - o.x, dy = xs[1] - o.y, dz = xs[2] - o.z;
+          dx -= L32[0] * rintf(dx / L32[0]);
+          dy -= L32[1] * rintf(dy / L32[1]);
+          dz -= L32[2] * rintf(dz / L32[2]);
+          if (dx * dx + dy * dy + dz * dz > reach * reach) continue;
+          double ox, oy, oz;
+          load_xyz(p.pos, o.id, ox, oy, oz);
+          if (ref_r2_scaled(x, y, z, ox, oy, oz, len, sf) < 1.0) ov = true;
+        }
+      }
+    }
+  }
+  if (ov) atomicOr(&p.st->vol_overlap, 1);
+}
+
+// Acceptance exp(beta P (V - V') + (N + 1) ln(V'/V)) against a fresh uniform
+// (src/moves.c:114-127); on acceptance the box is rebuilt from the lattice
+// counts and the new density (src/moves.c:128-132) and the device grid is
+// re-derived for it.
+__global__ void k_vol_decide(SysPtrs p, double margin) {
+  DevState *st = p.st;
+  Box *bx = p.box;
+  if (st->vol_overlap) return;
+  const double boltz = exp(st->pressure * (bx->vol - st->vol_new) + (p.n + 1) * log(st->vol_ratio));
+  if (st->vol_u_acc >= boltz) return;
+  const double rho = p.n / st->vol_new;
+  const double cell_vol = st->per_cell / rho;
+  const double cell_size = pow(cell_vol, 1. / 3.);
+  double lmax = 0.0;
+  for (int d = 0; d < 3; d++) {
+    const double len = st->cells[d] * cell_size;
+    int nc = 2 * (int)floor(len / (2.0 * (1.0 + margin)));
+    if (nc > st->nc_alloc[d]) nc = st->nc_alloc[d];
+    if (nc < 4) {
+      atomicOr(&st->status, ST_BAD_CELL);
+      return;
+    }
+    bx->len[d] = len;
+    bx->half[d] = len / 2.0;
+    bx->len32[d] = (float)len;
+    bx->inv_w32[d] = (float)(nc / len);
+    bx->w32[d] = (float)(len / nc);
+    bx->nc[d] = nc;
+    lmax = len > lmax ? len : lmax;
+  }
+  bx->ncell = bx->nc[0] * bx->nc[1] * bx->nc[2];
+  bx->vol = st->cells[0] * st->cells[1] * st->cells[2] * cell_vol;
+  bx->rho = rho;
+  bx->band = (float)(5.9604644775390625e-08 * (48.0 * lmax + 16.0) + 1e-6);
+  st->vol_accept = 1;
+  st->vol_acc += 1;
+}
+
+// Positions scaled by sf and wrapped into the new box (src/moves.c:133-140).
+__global__ void __launch_bounds__(256) k_vol_apply(SysPtrs p) {
+  const DevState *st = p.st;
+  if (!st->vol_accept) return;
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= p.n) return;
+  const double sf = st->vol_sf;
+  const Box *bx = p.box;
+  double *q = p.pos + 4 * (size_t)i;
+  for (int d = 0; d < 3; d++) {
+    double v = __dmul_rn(q[1 + d], sf);
+    if (gt_pos(v, bx->len[d])) v = __dsub_rn(v, bx->len[d]);
+    else if (lt_zero(v)) v = __dadd_rn(v, bx->len[d]);
+    q[1 + d] = v;
+  }
+}
+
+void launch_volume_scan(const SysPtrs &p, cudaStream_t s) {
+  const int blocks = (p.n + 255) / 256;
+  k_vol_scan<<<blocks, 256, 0, s>>>(p);
+}
+
+void launch_volume_move(const SysPtrs &p, long long sweep_offset, double margin, cudaStream_t s) {
+  const int blocks = (p.n + 255) / 256;
+  k_vol_propose<<<1, 1, 0, s>>>(p, sweep_offset);
+  k_vol_scan<<<blocks, 256, 0, s>>>(p);
+  k_vol_decide<<<1, 1, 0, s>>>(p, margin);
+  k_vol_apply<<<blocks, 256, 0, s>>>(p);
+}
 
 // ------------------------------------------------------------------ launch
 
@@ -371,36 +469,58 @@ void launch_build(const SysPtrs &p, long long sweep_offset, int num_sms, cudaStr
   k_build<<<blocks > 0 ? blocks : 1, 256, 0, s>>>(p, sweep_offset);
 }
 
-template <int G, int CAP, int NCAND, bool TRACE>
+// Groups per pass = active cells (an eighth of the grid); one wave when the
+// occupancy allows it, grid-stride otherwise.
+template <int G, int CAP>
 static int pass_blocks_for(int ncell_alloc, int num_sms) {
   int per_sm = 0;
-  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_move_pass<G, CAP, NCAND, TRACE>, 256, 0);
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_move_pass<G, CAP, false>, 128, 0);
   if (per_sm < 1) per_sm = 1;
-  const int groups = ncell_alloc / 8;
-  const int need = (groups + (256 / G) - 1) / (256 / G);
+  const long long threads = (long long)(ncell_alloc / 8) * G;
+  const int need = (int)((threads + 127) / 128);
   const int cap = per_sm * num_sms;
   return need < cap ? (need > 0 ? need : 1) : cap;
 }
 
+template <int G>
+static int pass_blocks_g(int cap, int ncell_alloc, int num_sms) {
+  switch (cap) {
+    case 8: return pass_blocks_for<G, 8>(ncell_alloc, num_sms);
+    case 16: return pass_blocks_for<G, 16>(ncell_alloc, num_sms);
+    default: return pass_blocks_for<G, 32>(ncell_alloc, num_sms);
+  }
+}
+
 int move_pass_grid(int group, int cap, int ncell_alloc, int num_sms) {
-  (void)cap;
   switch (group) {
-    case 8: return pass_blocks_for<8, 8, 48, false>(ncell_alloc, num_sms);
-    case 16: return pass_blocks_for<16, 16, 96, false>(ncell_alloc, num_sms);
-    default: return pass_blocks_for<32, 32, 192, false>(ncell_alloc, num_sms);
+    case 1: return pass_blocks_g<1>(cap, ncell_alloc, num_sms);
+    case 2: return pass_blocks_g<2>(cap, ncell_alloc, num_sms);
+    case 4: return pass_blocks_g<4>(cap, ncell_alloc, num_sms);
+    default: return pass_blocks_g<8>(cap, ncell_alloc, num_sms);
+  }
+}
+
+template <int G, int CAP>
+static void launch_gc(const SysPtrs &p, int pass, bool trace, int grid, cudaStream_t s) {
+  if (trace) k_move_pass<G, CAP, true><<<grid, 128, 0, s>>>(p, pass);
+  else k_move_pass<G, CAP, false><<<grid, 128, 0, s>>>(p, pass);
+}
+
+template <int G>
+static void launch_g(const SysPtrs &p, int pass, bool trace, int grid, cudaStream_t s) {
+  switch (p.cap) {
+    case 8: launch_gc<G, 8>(p, pass, trace, grid, s); break;
+    case 16: launch_gc<G, 16>(p, pass, trace, grid, s); break;
+    default: launch_gc<G, 32>(p, pass, trace, grid, s); break;
   }
 }
 
 void launch_move_pass(const SysPtrs &p, int pass, int group, bool trace, int grid, cudaStream_t s) {
-  if (group == 8) {
-    if (trace) k_move_pass<8, 8, 48, true><<<grid, 256, 0, s>>>(p, pass);
-    else k_move_pass<8, 8, 48, false><<<grid, 256, 0, s>>>(p, pass);
-  } else if (group == 16) {
-    if (trace) k_move_pass<16, 16, 96, true><<<grid, 256, 0, s>>>(p, pass);
-    else k_move_pass<16, 16, 96, false><<<grid, 256, 0, s>>>(p, pass);
-  } else {
-    if (trace) k_move_pass<32, 32, 192, true><<<grid, 256, 0, s>>>(p, pass);
-    else k_move_pass<32, 32, 192, false><<<grid, 256, 0, s>>>(p, pass);
+  switch (group) {
+    case 1: launch_g<1>(p, pass, trace, grid, s); break;
+    case 2: launch_g<2>(p, pass, trace, grid, s); break;
+    case 4: launch_g<4>(p, pass, trace, grid, s); break;
+    default: launch_g<8>(p, pass, trace, grid, s); break;
   }
 }
 

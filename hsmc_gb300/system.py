@@ -81,7 +81,7 @@ class HardSphereSystem:
 
     def __init__(self, rho: float, cells, lattice_type: int = 2, dr_max: float = 0.05, dv_max: float = 0.001,
                  pressure: float = 0.0, seed: int = 0, conf: np.ndarray | None = None, cell_capacity: int = 0,
-                 box=None):
+                 box=None, lanes_per_cell: int = 0):
         lib = _native.load()
         self._lib = lib
         if np.isscalar(cells):
@@ -111,6 +111,7 @@ class HardSphereSystem:
         p.pressure = pressure
         p.seed = seed
         p.cell_capacity = cell_capacity
+        p.lanes_per_cell = lanes_per_cell
         h = C.c_void_p()
         _check(lib.hsmc_gpu_create(C.byref(p), C.byref(h)), "hsmc_gpu_create")
         self._h = h
@@ -262,6 +263,11 @@ class HardSphereSystem:
     def rng_set_state(self, st) -> None:
         st = np.ascontiguousarray(st, dtype=np.uint64)
         _check(self._lib.hsmc_gpu_rng_set_state(self._h, st.ctypes.data), "hsmc_gpu_rng_set_state")
+
+    def autotune(self, sweeps_per_variant: int = 5) -> int:
+        lanes = C.c_int()
+        _check(self._lib.hsmc_gpu_autotune(self._h, sweeps_per_variant, C.byref(lanes)), "hsmc_gpu_autotune")
+        return lanes.value
 
     def set_profiling(self, on: bool) -> None:
         _check(self._lib.hsmc_gpu_set_profiling(self._h, 1 if on else 0), "hsmc_gpu_set_profiling")

@@ -59,7 +59,9 @@ typedef struct {
   double pressure;      /* beta*P for NpT, 0 for NVT (keyword "npt", 1st value) */
   uint64_t seed;        /* random stream key (keyword "seed") */
   int cell_capacity;    /* particles per device cell; 0 chooses from the cell size */
-  int reserved[7];
+  int lanes_per_cell;   /* GPU lanes sharing one active cell in a move pass: 1, 2, 4 or 8;
+                           0 picks the default */
+  int reserved[6];
 } hsmc_params;
 
 /* Replaces the set-up in hs_nvt / hs_npt (src/nvt.c:30-62, src/npt.c:25-70):
@@ -175,6 +177,13 @@ int hsmc_gpu_sweeps_traced(hsmc_ctx *ctx, int n_sweeps, uint32_t *rec, int64_t c
 /* Geometry of the device cell grid used by the sweeps: nc[3], len32[3] and
  * inv_w32[3] (float), capacity; for checking traced moves. */
 int hsmc_gpu_grid_info(hsmc_ctx *ctx, int nc[3], float len32[3], float inv_w32[3], int *capacity);
+
+/* Times the move pass for each lanes-per-cell mapping (1, 2, 4, 8) over
+ * sweeps_per_variant sweeps each and keeps the fastest; *lanes_out receives
+ * it.  The chain does not depend on the mapping (same random counters, exact
+ * decisions), so these are ordinary sweeps of the run: the configuration
+ * advances by 4 * sweeps_per_variant sweeps. */
+int hsmc_gpu_autotune(hsmc_ctx *ctx, int sweeps_per_variant, int *lanes_out);
 
 /* Timing of the last sweep call, from CUDA events on the context's stream:
  * total device time, and (only with profiling on) the summed time and count

@@ -12,7 +12,7 @@ import pytest
 pytestmark = pytest.mark.gpu
 
 
-def fluid(oracle_mod, gpu, rho, n, seed, dr, sweeps=30, neigh_dr=1.05):
+def fluid(oracle_mod, gpu, rho, n, seed, dr, sweeps=30, neigh_dr=1.05, lanes=0):
     """An oracle system run from the lattice (the reference's own chain) and a
     GPU system started from the same configuration."""
     o = oracle_mod.OracleSim(rho=rho, n_cells=n, seed=seed, dr_max=dr, neigh_dr=neigh_dr,
@@ -20,7 +20,7 @@ def fluid(oracle_mod, gpu, rho, n, seed, dr, sweeps=30, neigh_dr=1.05):
     if sweeps:
         o.sweeps_nvt(sweeps)
     conf = o.get_config()
-    g = gpu.HardSphereSystem(rho=rho, cells=n, dr_max=dr, seed=seed + 1000, conf=conf)
+    g = gpu.HardSphereSystem(rho=rho, cells=n, dr_max=dr, seed=seed + 1000, conf=conf, lanes_per_cell=lanes)
     return o, g, conf
 
 
@@ -59,11 +59,12 @@ def test_overlap_decisions_bit_exact(oracle_mod, gpu_lib, rho, n, seed, dr):
     assert 0 < want.sum() < len(want)
 
 
+@pytest.mark.parametrize("lanes", [1, 2, 4, 8])
 @pytest.mark.parametrize("rho,n,seed,dr", CASES + [(0.70, 10, 5, 0.2)])
-def test_traced_sweeps_replay_bit_exact(oracle_mod, gpu_lib, rho, n, seed, dr):
+def test_traced_sweeps_replay_bit_exact(oracle_mod, gpu_lib, rho, n, seed, dr, lanes):
     from oracle.philox import TAG_MOVE, draw4
 
-    o, g, conf = fluid(oracle_mod, gpu_lib, rho, n, seed, dr, sweeps=10)
+    o, g, conf = fluid(oracle_mod, gpu_lib, rho, n, seed, dr, sweeps=10, lanes=lanes)
     sweeps = 4
     rec, cnt = g.sweeps_traced(sweeps)
     assert len(rec) == o.n * sweeps
@@ -81,6 +82,17 @@ def test_traced_sweeps_replay_bit_exact(oracle_mod, gpu_lib, rho, n, seed, dr):
     assert np.array_equal(dec, rec[:, 7].astype(np.int32))
     assert np.array_equal(o.get_config(), g.download())
     assert cnt[1] == np.sum(dec == 0)
+
+
+def test_chain_independent_of_lane_mapping(gpu_lib):
+    """Same seed, same trajectory whatever the number of lanes per cell."""
+    finals = []
+    for lanes in (1, 2, 4, 8):
+        g = gpu_lib.HardSphereSystem(rho=0.8, cells=8, dr_max=0.15, seed=123, lanes_per_cell=lanes)
+        c = g.sweep_nvt(37)
+        finals.append((g.download(), c.copy()))
+    for conf, c in finals[1:]:
+        assert np.array_equal(conf, finals[0][0]) and np.array_equal(c, finals[0][1])
 
 
 @pytest.mark.parametrize("rho,n,seed,dr", CASES)
