@@ -110,6 +110,10 @@ template <int G, int CAP, bool TRACE>
 __global__ void __launch_bounds__(128) k_move_pass(SysPtrs p, int pass) {
   static_assert(G == 1 || G == 2 || G == 4 || G == 8, "group size");
   constexpr int NB = (26 + G - 1) / G;  // neighbour cells per lane
+  // Staged neighbour particles per thread: about 27 rho w^3 / G on average;
+  // a lane with more than NCL screens from the slots directly.
+  constexpr int NCL = G == 1 ? 32 : (G == 2 ? 20 : (G == 4 ? 12 : 8));
+  __shared__ Slot stage_mem[NCL][128];
 
   const DevState *st = p.st;
   const Box *bx = p.box;
@@ -148,15 +152,55 @@ __global__ void __launch_bounds__(128) k_move_pass(SysPtrs p, int pass) {
 
   unsigned acc = 0, rej_o = 0, rej_b = 0, rechecks = 0;
 
+  Slot(*stage)[128] = stage_mem;  // [NCL][threads]: column per thread, conflict-free
+
   for (int ac = group; ac < n_active; ac += groups) {
     const int ax = ac % hx, ayz = ac / hx, ay = ayz % hy, az = ayz / hy;
     const int ix = 2 * ax + cx, iy = 2 * ay + cy, iz = 2 * az + cz;
     const int c = ix + nc[0] * (iy + nc[1] * iz);
+
+    // Load phase, so one trial never waits on a chain of memory round trips:
+    // (1) the counts of the cell and of this lane's neighbour cells, issued
+    // together; (2) every slot of those cells, the neighbours' staged in this
+    // thread's column of shared memory; (3) the cell's FP64 positions.
+    const int xm = ix == 0 ? nc[0] - 1 : ix - 1, xp = ix == nc[0] - 1 ? 0 : ix + 1;
+    const int ym = iy == 0 ? nc[1] - 1 : iy - 1, yp = iy == nc[1] - 1 ? 0 : iy + 1;
+    const int zm = iz == 0 ? nc[2] - 1 : iz - 1, zp = iz == nc[2] - 1 ? 0 : iz + 1;
+    int nb_c[NB], nb_n[NB];
+#pragma unroll
+    for (int q = 0; q < NB; q++) {
+      const int o26 = lane + q * G;
+      nb_c[q] = c;
+      if (o26 < 26) {
+        const int o = o26 < 13 ? o26 : o26 + 1;  // the centre (13) is the cell itself
+        const int a = o / 9, b = (o / 3) % 3, e = o % 3;
+        const int x = a == 0 ? xm : (a == 1 ? ix : xp);
+        const int y = b == 0 ? ym : (b == 1 ? iy : yp);
+        const int z = e == 0 ? zm : (e == 1 ? iz : zp);
+        nb_c[q] = x + nc[0] * (y + nc[1] * z);
+      }
+    }
     const int n = cnt[c];
+#pragma unroll
+    for (int q = 0; q < NB; q++) {
+      const int m = (lane + q * G < 26) ? cnt[nb_c[q]] : 0;
+      nb_n[q] = m < CAP ? m : CAP;  // an overfull cell was flagged by the build
+    }
     if (n == 0) continue;
     if (n > CAP) {
       if (lane == 0) atomicOr(&p.st->status, ST_CELL_OVERFLOW);
       continue;
+    }
+
+    int staged = 0;
+#pragma unroll
+    for (int q = 0; q < NB; q++) staged += nb_n[q];
+    const bool direct = staged > NCL;  // rare: screen straight from the slots
+    if (!direct) {
+      int w = 0;
+#pragma unroll
+      for (int q = 0; q < NB; q++)
+        for (int k = 0; k < nb_n[q]; k++) stage[w++][threadIdx.x] = slot[(size_t)nb_c[q] * CAP + k];
     }
 
     // The cell's particles, in id order so the chain does not depend on the
@@ -180,28 +224,6 @@ __global__ void __launch_bounds__(128) k_move_pass(SysPtrs p, int pass) {
       fx[j] = __double2float_rn(qx[j]);
       fy[j] = __double2float_rn(qy[j]);
       fz[j] = __double2float_rn(qz[j]);
-    }
-
-    // This lane's neighbour cells (the centre cell excluded).
-    const int xm = ix == 0 ? nc[0] - 1 : ix - 1, xp = ix == nc[0] - 1 ? 0 : ix + 1;
-    const int ym = iy == 0 ? nc[1] - 1 : iy - 1, yp = iy == nc[1] - 1 ? 0 : iy + 1;
-    const int zm = iz == 0 ? nc[2] - 1 : iz - 1, zp = iz == nc[2] - 1 ? 0 : iz + 1;
-    int nb_c[NB], nb_n[NB];
-#pragma unroll
-    for (int q = 0; q < NB; q++) {
-      const int o26 = lane + q * G;
-      nb_n[q] = 0;
-      nb_c[q] = 0;
-      if (o26 < 26) {
-        const int o = o26 < 13 ? o26 : o26 + 1;
-        const int a = o / 9, b = (o / 3) % 3, e = o % 3;
-        const int x = a == 0 ? xm : (a == 1 ? ix : xp);
-        const int y = b == 0 ? ym : (b == 1 ? iy : yp);
-        const int z = e == 0 ? zm : (e == 1 ? iz : zp);
-        nb_c[q] = x + nc[0] * (y + nc[1] * z);
-        const int m = cnt[nb_c[q]];
-        nb_n[q] = m < CAP ? m : CAP;  // an overfull cell was flagged by the build
-      }
     }
 
     unsigned moved = 0;
@@ -236,14 +258,24 @@ __global__ void __launch_bounds__(128) k_move_pass(SysPtrs p, int pass) {
             ov = ref_r2(nx, ny, nz, qx[j], qy[j], qz[j], len, half) < 1.0;
           }
         }
-#pragma unroll
-        for (int q = 0; q < NB; q++) {
-          for (int k = 0; k < nb_n[q] && !ov; k++) {
-            const Slot o = slot[(size_t)nb_c[q] * CAP + k];
+        if (!direct) {
+          for (int j = 0; j < staged && !ov; j++) {
+            const Slot o = stage[j][threadIdx.x];
             const float dx = wrap_diff(gx - o.x, L32[0], H32[0]);
             const float dy = wrap_diff(gy - o.y, L32[1], H32[1]);
             const float dz = wrap_diff(gz - o.z, L32[2], H32[2]);
             ov = screen_pair(dx, dy, dz, band, nx, ny, nz, pos, o.id, len, half, rechecks);
+          }
+        } else {
+#pragma unroll
+          for (int q = 0; q < NB; q++) {
+            for (int k = 0; k < nb_n[q] && !ov; k++) {
+              const Slot o = slot[(size_t)nb_c[q] * CAP + k];
+              const float dx = wrap_diff(gx - o.x, L32[0], H32[0]);
+              const float dy = wrap_diff(gy - o.y, L32[1], H32[1]);
+              const float dz = wrap_diff(gz - o.z, L32[2], H32[2]);
+              ov = screen_pair(dx, dy, dz, band, nx, ny, nz, pos, o.id, len, half, rechecks);
+            }
           }
         }
         if (G > 1) ov = __ballot_sync(gmask, ov) != 0u;
