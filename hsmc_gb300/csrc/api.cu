@@ -564,6 +564,82 @@ int hsmc_gpu_pressv(hsmc_ctx *ctx, double dr, double rmax, int nbins, uint64_t *
   return pair_counts(ctx, dr, rmax, nbins, counts);
 }
 
+// --------------------------------------------------- allocation-free g(r)
+// hsmc_gpu_rdf grows a device histogram with cudaMalloc whenever a caller
+// asks for more bins than before.  Some callers cannot let a library
+// allocate: a host program that hands all device memory to its own memory
+// manager up front, or that runs under a fixed per-process memory budget on
+// a GPU shared with other jobs, has nothing left to give; and a sampling loop
+// with a hard time budget cannot absorb a first-call cudaMalloc, which may
+// synchronise the device.  For them the counts go into the fixed array
+// below, compiled into the library and resident on every GPU that loads it
+// until the process exits.  In host code the symbol is only a stand-in for
+// the device array: its device address is looked up once per device with
+// cudaGetSymbolAddress and that address is what the kernel receives.
+// Every call shares this array and clears it before counting, so two calls
+// that run at the same time on one GPU (different contexts or streams)
+// race on it.
+static __device__ __align__(256) unsigned long long g_rdf_noalloc_bins[HSMC_RDF_NOALLOC_MAX_BINS];
+
+static unsigned long long *noalloc_bins_on(int device, int *status) {
+  static unsigned long long *addr[256] = {nullptr};
+  static bool ready[256] = {false};
+  *status = HSMC_OK;
+  if (device < 0 || device >= 256) {
+    *status = HSMC_ERR_NO_DEVICE;
+    return nullptr;
+  }
+  if (!ready[device]) {
+    void *p = nullptr;
+    cudaError_t e = cudaGetSymbolAddress(&p, g_rdf_noalloc_bins);
+    if (e != cudaSuccess) {
+      *status = cuda_status(e);
+      return nullptr;
+    }
+    addr[device] = (unsigned long long *)p;
+    ready[device] = true;
+  }
+  return addr[device];
+}
+
+int hsmc_gpu_rdf_noalloc(hsmc_ctx *ctx, double dr, double rmax, int nbins, uint64_t *counts) {
+  if (!ctx || !counts || nbins <= 0 || !(dr > 0) || !(rmax > 1.0) || !ctx->uploaded) return HSMC_ERR_INVALID_ARG;
+  if (nbins > HSMC_RDF_NOALLOC_MAX_BINS) {
+    fprintf(stderr, "hsmc_gpu_rdf_noalloc: %d bins requested, at most %d are available\n", nbins,
+            HSMC_RDF_NOALLOC_MAX_BINS);
+    return HSMC_ERR_INVALID_ARG;
+  }
+  // The array's address is looked up with the context's device current.
+  cudaPointerAttributes attr{};
+  HSMC_CUDA(cudaPointerGetAttributes(&attr, ctx->sp.pos));
+  int current = 0;
+  HSMC_CUDA(cudaGetDevice(&current));
+  if (current != attr.device) HSMC_CUDA(cudaSetDevice(attr.device));
+  int st = HSMC_OK;
+  unsigned long long *d = noalloc_bins_on(attr.device, &st);
+  int e = st;
+  if (!e) {
+    cudaError_t ce = cudaMemsetAsync(d, 0, sizeof(unsigned long long) * (size_t)nbins, ctx->stream);
+    if (ce == cudaSuccess) ce = cudaMemsetAsync(&ctx->sp.st->status, 0, sizeof(int), ctx->stream);
+    if (ce != cudaSuccess) e = cuda_status(ce);
+  }
+  if (!e) {
+    int k[3];
+    stencil_for(ctx->hbox, rmax, k);
+    launch_pair_hist(ctx->sp, dr, rmax, nbins, d, k, ctx->stream);
+    e = check_kernels(ctx);
+  }
+  if (!e) {
+    cudaError_t ce = cudaMemcpyAsync(counts, d, sizeof(uint64_t) * (size_t)nbins, cudaMemcpyDeviceToHost, ctx->stream);
+    if (ce != cudaSuccess) e = cuda_status(ce);
+  }
+  DevState s;
+  if (!e) e = read_state(ctx, s);
+  if (!e && s.status) e = status_to_code(s.status);
+  if (current != attr.device) cudaSetDevice(current);
+  return e;
+}
+
 static int scaled_scan(hsmc_ctx *ctx, const double *sf, int n_sf, unsigned long long mask[4]) {
   if (!ctx || !sf || n_sf <= 0 || n_sf > 256 || !ctx->uploaded) return HSMC_ERR_INVALID_ARG;
   double smallest = 1.0;

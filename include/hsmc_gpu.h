@@ -115,6 +115,20 @@ int hsmc_gpu_get_box(hsmc_ctx *ctx, double out[5]);
  * cutoff dr*nbins + 1 (src/compute_rdf.c:104) and at most half the box. */
 int hsmc_gpu_rdf(hsmc_ctx *ctx, double dr, double rmax, int nbins, uint64_t *counts);
 
+/* hsmc_gpu_rdf without any allocation, for callers that cannot let the
+ * library allocate device memory: a program that gives all device memory to
+ * its own memory manager up front or runs under a fixed memory budget on a
+ * shared GPU, or a sampling loop that cannot absorb a first-call cudaMalloc.
+ * No counterpart in the reference.  The counts use a fixed device array of
+ * HSMC_RDF_NOALLOC_MAX_BINS 64-bit bins compiled into the library (resident
+ * on every GPU that loads it until the process exits); more bins are refused
+ * with HSMC_ERR_INVALID_ARG.  The first call on a device looks up that
+ * array's device address, so make the first call before any stream capture.
+ * All calls share the array and clear it before counting: calls that run at
+ * the same time on one GPU race on it.  Results equal hsmc_gpu_rdf's. */
+#define HSMC_RDF_NOALLOC_MAX_BINS 16384
+int hsmc_gpu_rdf_noalloc(hsmc_ctx *ctx, double dr, double rmax, int nbins, uint64_t *counts);
+
 /* Virial-route contact histogram, the same counting on [1, rmax)
  * (pressv_compute_hist, src/compute_press.c:123-165). */
 int hsmc_gpu_pressv(hsmc_ctx *ctx, double dr, double rmax, int nbins, uint64_t *counts);
