@@ -209,6 +209,16 @@ struct alignas(16) Slot {  // one particle in a cell: single-precision copy + id
   int id;
 };
 
+// FP64 coordinates of particle id from the double[N][4] (id, x, y, z) array:
+// two aligned 16-byte loads.
+__device__ __forceinline__ void load_xyz(const double *pos, int id, double &x, double &y, double &z) {
+  const double2 a = *reinterpret_cast<const double2 *>(pos + 4 * (size_t)id);
+  const double2 b = *reinterpret_cast<const double2 *>(pos + 4 * (size_t)id + 2);
+  x = a.y;
+  y = b.x;
+  z = b.y;
+}
+
 // Counters of one launch reduced per warp, then added once per warp.
 __device__ __forceinline__ unsigned long long warp_sum_u64(unsigned long long v) {
 #pragma unroll

@@ -89,14 +89,6 @@ __device__ __forceinline__ void for_each_near(const CellView &v, const Stencil &
   }
 }
 
-__device__ __forceinline__ void load_pos(const double *pos, int id, double &x, double &y, double &z) {
-  const double2 a = *reinterpret_cast<const double2 *>(pos + 4 * (size_t)id);
-  const double2 b = *reinterpret_cast<const double2 *>(pos + 4 * (size_t)id + 2);
-  x = a.y;
-  y = b.x;
-  z = b.y;
-}
-
 // Single-precision squared minimum-image distance, for discarding far pairs.
 __device__ __forceinline__ float approx_r2(float ax, float ay, float az, const Slot &o, const float *L32) {
   float dx = ax - o.x, dy = ay - o.y, dz = az - o.z;
@@ -124,13 +116,13 @@ __global__ void __launch_bounds__(256) k_pair_hist(SysPtrs p, Stencil s, double 
   bool bad = false;
   if (i < p.n) {
     double x, y, z;
-    load_pos(p.pos, i, x, y, z);
+    load_xyz(p.pos, i, x, y, z);
     const float x32 = __double2float_rn(x), y32 = __double2float_rn(y), z32 = __double2float_rn(z);
     for_each_near(v, s, x, y, z, [&](const Slot &o) {
       if (o.id == i) return;
       if (approx_r2(x32, y32, z32, o, v.L32) > cut2) return;
       double ox, oy, oz;
-      load_pos(p.pos, o.id, ox, oy, oz);
+      load_xyz(p.pos, o.id, ox, oy, oz);
       const double r = __dsqrt_rn(ref_r2(x, y, z, ox, oy, oz, len, half));
       if (r < rmax) {
         const int b = (int)__ddiv_rn(__dsub_rn(r, 1.0), bin);
@@ -176,13 +168,13 @@ __global__ void __launch_bounds__(256) k_scaled_scan(SysPtrs p, Stencil s, int n
   unsigned long long m[4] = {0ull, 0ull, 0ull, 0ull};
   if (i < p.n) {
     double x, y, z;
-    load_pos(p.pos, i, x, y, z);
+    load_xyz(p.pos, i, x, y, z);
     const float x32 = __double2float_rn(x), y32 = __double2float_rn(y), z32 = __double2float_rn(z);
     for_each_near(v, s, x, y, z, [&](const Slot &o) {
       if (o.id == i) return;
       if (approx_r2(x32, y32, z32, o, v.L32) > cut2) return;
       double ox, oy, oz;
-      load_pos(p.pos, o.id, ox, oy, oz);
+      load_xyz(p.pos, o.id, ox, oy, oz);
       for (int k = 0; k < n_sf; k++) {
         const unsigned long long bit = 1ull << (k & 63);
         if (m[k >> 6] & bit) continue;
@@ -221,7 +213,7 @@ __device__ __forceinline__ bool point_overlaps(const CellView &v, const SysPtrs 
     const float r2 = approx_r2(x32, y32, z32, o, v.L32);
     if (r2 > 1.01f) return;
     double ox, oy, oz;
-    load_pos(p.pos, o.id, ox, oy, oz);
+    load_xyz(p.pos, o.id, ox, oy, oz);
     if (ref_r2(x, y, z, ox, oy, oz, len, half) < 1.0) ov = true;
   });
   return ov;
@@ -304,7 +296,7 @@ __global__ void __launch_bounds__(128) k_ql(SysPtrs p, Stencil s, int l, double 
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= p.n) return;
   double x, y, z;
-  load_pos(p.pos, i, x, y, z);
+  load_xyz(p.pos, i, x, y, z);
   const float x32 = __double2float_rn(x), y32 = __double2float_rn(y), z32 = __double2float_rn(z);
   double re[QL_LMAX + 1], im[QL_LMAX + 1];
   for (int m = 0; m <= QL_LMAX; m++) re[m] = im[m] = 0.0;
@@ -314,7 +306,7 @@ __global__ void __launch_bounds__(128) k_ql(SysPtrs p, Stencil s, int l, double 
     if (o.id == i) return;
     if (approx_r2(x32, y32, z32, o, v.L32) > cut2) return;
     double ox, oy, oz;
-    load_pos(p.pos, o.id, ox, oy, oz);
+    load_xyz(p.pos, o.id, ox, oy, oz);
     const double dx = min_image(__dsub_rn(x, ox), len[0], half[0]);
     const double dy = min_image(__dsub_rn(y, oy), len[1], half[1]);
     const double dz = min_image(__dsub_rn(z, oz), len[2], half[2]);
