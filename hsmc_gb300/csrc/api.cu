@@ -95,7 +95,7 @@ static int status_to_code(int st) {
 // Cell grid for a box: an even number of cells per axis, each edge at least
 // 1 + margin, the margin covering single-precision rounding of coordinates
 // up to the box length.
-static int make_box(const double len[3], double rho, Box &b, int &cap) {
+int hsmc::make_box(const double len[3], double rho, Box &b, int &cap) {
   double lmax = len[0];
   for (int d = 1; d < 3; d++) lmax = len[d] > lmax ? len[d] : lmax;
   const double u = 5.9604644775390625e-08;  // 2^-24
@@ -237,6 +237,7 @@ int hsmc_gpu_create(const hsmc_params *prm, hsmc_ctx **out) {
     if ((ce = cudaMalloc(&sp.cnt[l], sizeof(int) * (size_t)sp.ncell_alloc)) != cudaSuccess) return fail(ce);
     if ((ce = cudaMalloc(&sp.slot[l], sizeof(Slot) * (size_t)sp.ncell_alloc * cap)) != cudaSuccess) return fail(ce);
     if ((ce = cudaMemset(sp.cnt[l], 0, sizeof(int) * (size_t)sp.ncell_alloc)) != cudaSuccess) return fail(ce);
+    if ((ce = cudaMalloc(&sp.list[l], sizeof(int) * (size_t)sp.ncell_alloc * NBUCKET)) != cudaSuccess) return fail(ce);
   }
   if ((ce = cudaMalloc(&sp.box, sizeof(Box))) != cudaSuccess) return fail(ce);
   if ((ce = cudaMalloc(&sp.st, sizeof(DevState))) != cudaSuccess) return fail(ce);
@@ -270,6 +271,7 @@ void hsmc_gpu_destroy(hsmc_ctx *ctx) {
   for (int l = 0; l < 2; l++) {
     cudaFree(sp.cnt[l]);
     cudaFree(sp.slot[l]);
+    cudaFree(sp.list[l]);
   }
   cudaFree(sp.box);
   cudaFree(sp.st);
@@ -301,6 +303,7 @@ int hsmc_gpu_upload_config(hsmc_ctx *ctx, const double (*conf)[4], int n) {
   for (int l = 0; l < 2; l++)
     HSMC_CUDA(cudaMemsetAsync(sp.cnt[l], 0, sizeof(int) * (size_t)sp.ncell_alloc, ctx->stream));
   HSMC_CUDA(cudaMemsetAsync(&sp.st->status, 0, sizeof(int), ctx->stream));
+  HSMC_CUDA(cudaMemsetAsync(&sp.st->list_len, 0, sizeof(sp.st->list_len), ctx->stream));
   launch_build(sp, -1, ctx->num_sms, ctx->stream);
   int e = check_kernels(ctx);
   if (e) return e;
@@ -375,6 +378,7 @@ static int ensure_graph(hsmc_ctx *ctx, bool npt) {
 static void rebuild_current_layout(hsmc_ctx *ctx) {
   const int layout = (int)((ctx->sweep_base - 1) & 1ull);
   cudaMemsetAsync(ctx->sp.cnt[layout], 0, sizeof(int) * (size_t)ctx->sp.ncell_alloc, ctx->stream);
+  cudaMemsetAsync(&ctx->sp.st->list_len[layout], 0, sizeof(ctx->sp.st->list_len[layout]), ctx->stream);
   launch_build(ctx->sp, -1, ctx->num_sms, ctx->stream);
 }
 
@@ -760,6 +764,17 @@ int hsmc_gpu_rng_set_state(hsmc_ctx *ctx, const uint64_t st[4]) {
   ctx->widom_seq = st[2];
   HSMC_CUDA(cudaMemcpyAsync(&ctx->sp.st->seed, &st[0], sizeof(uint64_t), cudaMemcpyHostToDevice, ctx->stream));
   HSMC_CUDA(cudaMemcpyAsync(&ctx->sp.st->sweep_base, &st[1], sizeof(uint64_t), cudaMemcpyHostToDevice, ctx->stream));
+  if (ctx->uploaded) {
+    // The layout a sweep writes follows the parity of its index: rebuild the
+    // current one for the new position in the stream.
+    SysPtrs &sp = ctx->sp;
+    for (int l = 0; l < 2; l++)
+      HSMC_CUDA(cudaMemsetAsync(sp.cnt[l], 0, sizeof(int) * (size_t)sp.ncell_alloc, ctx->stream));
+    HSMC_CUDA(cudaMemsetAsync(&sp.st->list_len, 0, sizeof(sp.st->list_len), ctx->stream));
+    launch_build(sp, -1, ctx->num_sms, ctx->stream);
+    int e = check_kernels(ctx);
+    if (e) return e;
+  }
   HSMC_CUDA(cudaStreamSynchronize(ctx->stream));
   return HSMC_OK;
 }

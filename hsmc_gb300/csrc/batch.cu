@@ -1,0 +1,332 @@
+// Batched replicas (include/hsmc_gpu.h, hsmc_batch_*): many independent NVT
+// systems of different size and density advanced together.  All replicas
+// live in pooled device buffers; a device table holds one SysPtrs per
+// replica, and every kernel of a sweep covers all of them in one launch
+// (blockIdx.y = replica).  Sweeps run as CUDA graphs.
+#include <cuda_runtime.h>
+
+#include <cstddef>
+#include <cstdio>
+#include <vector>
+
+#include "../../include/hsmc_gpu.h"
+#include "engine.cuh"
+
+using namespace hsmc;
+
+namespace {
+
+constexpr int kBatchGraphSweeps = 8;
+constexpr int kBatchLanes = 2;
+
+int cuda_fail(cudaError_t e) {
+  fprintf(stderr, "hsmc_gpu: CUDA error %s\n", cudaGetErrorString(e));
+  return HSMC_ERR_CUDA;
+}
+
+#define BATCH_CUDA(call)                    \
+  do {                                      \
+    cudaError_t e_ = (call);                \
+    if (e_ != cudaSuccess) return cuda_fail(e_); \
+  } while (0)
+
+int code_of(int st) {
+  if (st & (ST_CELL_OVERFLOW | ST_BAD_CELL)) return HSMC_ERR_CELL_OVERFLOW;
+  if (st & ST_BAD_BIN) return HSMC_ERR_BAD_BIN;
+  if (st & ST_OUT_OF_BOX) return HSMC_ERR_OUT_OF_BOX;
+  return HSMC_OK;
+}
+
+}  // namespace
+
+struct hsmc_batch {
+  int reps = 0;
+  int cap = 8;
+  int group = kBatchLanes;
+  int max_n = 0, max_ncell = 0;
+  cudaStream_t stream = nullptr;
+  std::vector<hsmc_params> prm;
+  std::vector<SysPtrs> sp;  // host copies of the device table
+  std::vector<Box> hbox;
+  std::vector<char> uploaded;
+  SysPtrs *d_reps = nullptr;
+  double *pos = nullptr;
+  int *cnt[2] = {nullptr, nullptr}, *list[2] = {nullptr, nullptr};
+  Slot *slot[2] = {nullptr, nullptr};
+  Box *box = nullptr;
+  DevState *st = nullptr;
+  unsigned long long *hist = nullptr;
+  size_t hist_bins = 0;
+  cudaGraphExec_t graph = nullptr;
+  cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+  double last_ms = 0.0;
+};
+
+static int batch_check(hsmc_batch *b) {
+  BATCH_CUDA(cudaGetLastError());
+  BATCH_CUDA(cudaStreamSynchronize(b->stream));
+  return HSMC_OK;
+}
+
+static int batch_status(hsmc_batch *b, std::vector<DevState> &out) {
+  out.resize(b->reps);
+  BATCH_CUDA(cudaMemcpyAsync(out.data(), b->st, sizeof(DevState) * b->reps, cudaMemcpyDeviceToHost, b->stream));
+  BATCH_CUDA(cudaStreamSynchronize(b->stream));
+  for (const DevState &s : out)
+    if (s.status) return code_of(s.status);
+  return HSMC_OK;
+}
+
+extern "C" {
+
+void hsmc_batch_destroy(hsmc_batch *b) {
+  if (!b) return;
+  if (b->stream) cudaStreamSynchronize(b->stream);
+  if (b->graph) cudaGraphExecDestroy(b->graph);
+  cudaFree(b->d_reps);
+  cudaFree(b->pos);
+  for (int l = 0; l < 2; l++) {
+    cudaFree(b->cnt[l]);
+    cudaFree(b->list[l]);
+    cudaFree(b->slot[l]);
+  }
+  cudaFree(b->box);
+  cudaFree(b->st);
+  cudaFree(b->hist);
+  if (b->ev0) cudaEventDestroy(b->ev0);
+  if (b->ev1) cudaEventDestroy(b->ev1);
+  if (b->stream) cudaStreamDestroy(b->stream);
+  delete b;
+}
+
+int hsmc_batch_create(const hsmc_params *params, int n_systems, hsmc_batch **out) {
+  if (!params || !out || n_systems <= 0 || n_systems > 65535) return HSMC_ERR_INVALID_ARG;
+  *out = nullptr;
+  int dev = 0;
+  cudaDeviceProp dp{};
+  if (cudaGetDevice(&dev) != cudaSuccess || cudaGetDeviceProperties(&dp, dev) != cudaSuccess)
+    return HSMC_ERR_NO_DEVICE;
+  if (!(dp.major == 10 && dp.minor == 3)) return HSMC_ERR_NO_DEVICE;
+  hsmc_batch *b = new hsmc_batch();
+  b->reps = n_systems;
+  b->prm.assign(params, params + n_systems);
+  b->hbox.resize(n_systems);
+  b->sp.resize(n_systems);
+  b->uploaded.assign(n_systems, 0);
+  size_t tot_n = 0, tot_cell = 0;
+  int cap = 8;
+  for (int k = 0; k < n_systems; k++) {
+    const hsmc_params &p = params[k];
+    if (p.n_particles <= 0 || p.pressure > 0 || !(p.dr_max >= 0)) {
+      delete b;
+      return HSMC_ERR_INVALID_ARG;
+    }
+    for (int d = 0; d < 3; d++)
+      if (!(p.box[d] > 0) || !(p.dr_max < p.box[d])) {
+        delete b;
+        return HSMC_ERR_INVALID_ARG;
+      }
+    int ck = 8;
+    const double rho = p.rho > 0 ? p.rho : p.n_particles / (p.box[0] * p.box[1] * p.box[2]);
+    int e = make_box(p.box, rho, b->hbox[k], ck);
+    if (e) {
+      delete b;
+      return e;
+    }
+    cap = ck > cap ? ck : cap;
+    tot_n += (size_t)p.n_particles;
+    tot_cell += (size_t)b->hbox[k].ncell;
+    b->max_n = p.n_particles > b->max_n ? p.n_particles : b->max_n;
+    b->max_ncell = b->hbox[k].ncell > b->max_ncell ? b->hbox[k].ncell : b->max_ncell;
+  }
+  b->cap = cap;
+  auto fail = [&](cudaError_t e) {
+    hsmc_batch_destroy(b);
+    return cuda_fail(e);
+  };
+  cudaError_t ce;
+  if ((ce = cudaStreamCreateWithFlags(&b->stream, cudaStreamNonBlocking)) != cudaSuccess) return fail(ce);
+  if ((ce = cudaMalloc(&b->pos, sizeof(double) * 4 * tot_n)) != cudaSuccess) return fail(ce);
+  for (int l = 0; l < 2; l++) {
+    if ((ce = cudaMalloc(&b->cnt[l], sizeof(int) * tot_cell)) != cudaSuccess) return fail(ce);
+    if ((ce = cudaMemset(b->cnt[l], 0, sizeof(int) * tot_cell)) != cudaSuccess) return fail(ce);
+    if ((ce = cudaMalloc(&b->list[l], sizeof(int) * tot_cell * NBUCKET)) != cudaSuccess) return fail(ce);
+    if ((ce = cudaMalloc(&b->slot[l], sizeof(Slot) * tot_cell * cap)) != cudaSuccess) return fail(ce);
+  }
+  if ((ce = cudaMalloc(&b->box, sizeof(Box) * n_systems)) != cudaSuccess) return fail(ce);
+  if ((ce = cudaMalloc(&b->st, sizeof(DevState) * n_systems)) != cudaSuccess) return fail(ce);
+  if ((ce = cudaMalloc(&b->d_reps, sizeof(SysPtrs) * n_systems)) != cudaSuccess) return fail(ce);
+  std::vector<DevState> st0(n_systems);
+  size_t on = 0, oc = 0;
+  for (int k = 0; k < n_systems; k++) {
+    SysPtrs &s = b->sp[k];
+    s.pos = b->pos + 4 * on;
+    for (int l = 0; l < 2; l++) {
+      s.cnt[l] = b->cnt[l] + oc;
+      s.list[l] = b->list[l] + oc * NBUCKET;
+      s.slot[l] = b->slot[l] + oc * cap;
+    }
+    s.box = b->box + k;
+    s.st = b->st + k;
+    s.trace = nullptr;
+    s.trace_cap = 0;
+    s.n = params[k].n_particles;
+    s.cap = cap;
+    s.ncell_alloc = b->hbox[k].ncell;
+    DevState &d = st0[k];
+    d = DevState{};
+    d.sweep_base = 1;
+    d.dr_max = params[k].dr_max;
+    d.dv_max = params[k].dv_max;
+    d.seed = params[k].seed;
+    d.per_cell = params[k].lattice_type == 1 ? 1 : 4;
+    for (int q = 0; q < 3; q++) {
+      d.cells[q] = params[k].cells[q];
+      d.nc_alloc[q] = b->hbox[k].nc[q];
+    }
+    on += (size_t)params[k].n_particles;
+    oc += (size_t)b->hbox[k].ncell;
+  }
+  if ((ce = cudaMemcpy(b->box, b->hbox.data(), sizeof(Box) * n_systems, cudaMemcpyHostToDevice)) != cudaSuccess)
+    return fail(ce);
+  if ((ce = cudaMemcpy(b->st, st0.data(), sizeof(DevState) * n_systems, cudaMemcpyHostToDevice)) != cudaSuccess)
+    return fail(ce);
+  if ((ce = cudaMemcpy(b->d_reps, b->sp.data(), sizeof(SysPtrs) * n_systems, cudaMemcpyHostToDevice)) !=
+      cudaSuccess)
+    return fail(ce);
+  if ((ce = cudaEventCreate(&b->ev0)) != cudaSuccess) return fail(ce);
+  if ((ce = cudaEventCreate(&b->ev1)) != cudaSuccess) return fail(ce);
+  *out = b;
+  return HSMC_OK;
+}
+
+int hsmc_batch_upload_config(hsmc_batch *b, int k, const double (*conf)[4], int n) {
+  if (!b || k < 0 || k >= b->reps || !conf || n != b->sp[k].n) return HSMC_ERR_INVALID_ARG;
+  const Box &bx = b->hbox[k];
+  for (int i = 0; i < n; i++) {
+    if (conf[i][0] != (double)i) return HSMC_ERR_INVALID_ARG;
+    for (int d = 0; d < 3; d++)
+      if (!(conf[i][1 + d] >= 0.0 && conf[i][1 + d] <= bx.len[d])) return HSMC_ERR_OUT_OF_BOX;
+  }
+  const SysPtrs &s = b->sp[k];
+  BATCH_CUDA(cudaMemcpyAsync(s.pos, conf, sizeof(double) * 4 * (size_t)n, cudaMemcpyHostToDevice, b->stream));
+  for (int l = 0; l < 2; l++)
+    BATCH_CUDA(cudaMemsetAsync(s.cnt[l], 0, sizeof(int) * (size_t)s.ncell_alloc, b->stream));
+  BATCH_CUDA(cudaMemsetAsync(&s.st->list_len, 0, sizeof(s.st->list_len), b->stream));
+  BATCH_CUDA(cudaMemsetAsync(&s.st->status, 0, sizeof(int), b->stream));
+  launch_build(s, -1, 0, b->stream);
+  int e = batch_check(b);
+  if (e) return e;
+  DevState d;
+  BATCH_CUDA(cudaMemcpy(&d, s.st, sizeof(DevState), cudaMemcpyDeviceToHost));
+  if (d.status) return code_of(d.status);
+  b->uploaded[k] = 1;
+  return HSMC_OK;
+}
+
+int hsmc_batch_download_config(hsmc_batch *b, int k, double (*conf)[4], int n) {
+  if (!b || k < 0 || k >= b->reps || !conf || n != b->sp[k].n) return HSMC_ERR_INVALID_ARG;
+  BATCH_CUDA(cudaMemcpyAsync(conf, b->sp[k].pos, sizeof(double) * 4 * (size_t)n, cudaMemcpyDeviceToHost, b->stream));
+  BATCH_CUDA(cudaStreamSynchronize(b->stream));
+  return HSMC_OK;
+}
+
+int hsmc_batch_set_steps(hsmc_batch *b, const double *dr_max) {
+  if (!b || !dr_max) return HSMC_ERR_INVALID_ARG;
+  for (int k = 0; k < b->reps; k++)
+    for (int d = 0; d < 3; d++)
+      if (!(dr_max[k] >= 0 && dr_max[k] < b->hbox[k].len[d])) return HSMC_ERR_INVALID_ARG;
+  BATCH_CUDA(cudaMemcpy2DAsync(&b->st[0].dr_max, sizeof(DevState), dr_max, sizeof(double), sizeof(double),
+                               (size_t)b->reps, cudaMemcpyHostToDevice, b->stream));
+  BATCH_CUDA(cudaStreamSynchronize(b->stream));
+  for (int k = 0; k < b->reps; k++) b->prm[k].dr_max = dr_max[k];
+  return HSMC_OK;
+}
+
+static void enqueue_batch_sweep(hsmc_batch *b, long long offset, int grid_x) {
+  launch_build_batch(b->d_reps, b->reps, b->max_n, b->max_ncell, offset, b->stream);
+  for (int k = 0; k < 8; k++) launch_move_pass_batch(b->d_reps, b->reps, b->cap, k, b->group, grid_x, b->stream);
+}
+
+int hsmc_batch_sweeps(hsmc_batch *b, int n_sweeps, uint64_t *counters) {
+  if (!b || n_sweeps < 0) return HSMC_ERR_INVALID_ARG;
+  for (int k = 0; k < b->reps; k++)
+    if (!b->uploaded[k]) return HSMC_ERR_INVALID_ARG;
+  const int grid_x = move_pass_grid_batch(b->group, b->max_ncell);
+  if (!b->graph) {
+    cudaGraph_t g = nullptr;
+    BATCH_CUDA(cudaStreamBeginCapture(b->stream, cudaStreamCaptureModeThreadLocal));
+    for (int s = 0; s < kBatchGraphSweeps; s++) enqueue_batch_sweep(b, s, grid_x);
+    launch_advance_batch(b->d_reps, b->reps, kBatchGraphSweeps, b->stream);
+    cudaError_t e = cudaStreamEndCapture(b->stream, &g);
+    if (e != cudaSuccess) return cuda_fail(e);
+    e = cudaGraphInstantiate(&b->graph, g, 0);
+    cudaGraphDestroy(g);
+    if (e != cudaSuccess) {
+      b->graph = nullptr;
+      return cuda_fail(e);
+    }
+  }
+  // counters (acc .. scan_mask) and status of every replica
+  BATCH_CUDA(cudaMemset2DAsync(&b->st[0].acc, sizeof(DevState), 0, offsetof(DevState, dr_max) - offsetof(DevState, acc),
+                               (size_t)b->reps, b->stream));
+  BATCH_CUDA(cudaMemset2DAsync(&b->st[0].status, sizeof(DevState), 0, sizeof(int), (size_t)b->reps, b->stream));
+  BATCH_CUDA(cudaEventRecord(b->ev0, b->stream));
+  int done = 0;
+  while (n_sweeps - done >= kBatchGraphSweeps) {
+    BATCH_CUDA(cudaGraphLaunch(b->graph, b->stream));
+    done += kBatchGraphSweeps;
+  }
+  const int rest = n_sweeps - done;
+  for (int s = 0; s < rest; s++) enqueue_batch_sweep(b, s, grid_x);
+  if (rest > 0) launch_advance_batch(b->d_reps, b->reps, rest, b->stream);
+  BATCH_CUDA(cudaEventRecord(b->ev1, b->stream));
+  int e = batch_check(b);
+  if (e) return e;
+  float ms = 0.f;
+  BATCH_CUDA(cudaEventElapsedTime(&ms, b->ev0, b->ev1));
+  b->last_ms = ms;
+  std::vector<DevState> st;
+  const int status = batch_status(b, st);
+  if (counters) {
+    for (int k = 0; k < b->reps; k++) {
+      const uint64_t moves = (uint64_t)b->sp[k].n * (uint64_t)n_sweeps;
+      uint64_t *c = counters + 6 * (size_t)k;
+      c[HSMC_CNT_MOVES] = moves;
+      c[HSMC_CNT_ACCEPTED] = st[k].acc;
+      c[HSMC_CNT_REJECTED] = moves - st[k].acc;
+      c[HSMC_CNT_VOL_MOVES] = c[HSMC_CNT_VOL_ACCEPTED] = c[HSMC_CNT_VOL_REJECTED] = 0;
+    }
+  }
+  return status;
+}
+
+int hsmc_batch_pressv(hsmc_batch *b, double dr, double rmax, int nbins, uint64_t *counts) {
+  if (!b || !counts || nbins <= 0 || !(dr > 0) || !(rmax > 1.0)) return HSMC_ERR_INVALID_ARG;
+  for (int k = 0; k < b->reps; k++)
+    if (!b->uploaded[k]) return HSMC_ERR_INVALID_ARG;
+  const size_t need = (size_t)nbins * b->reps;
+  if (need > b->hist_bins) {
+    cudaFree(b->hist);
+    b->hist = nullptr;
+    b->hist_bins = 0;
+    BATCH_CUDA(cudaMalloc(&b->hist, sizeof(unsigned long long) * need));
+    b->hist_bins = need;
+  }
+  BATCH_CUDA(cudaMemsetAsync(b->hist, 0, sizeof(unsigned long long) * need, b->stream));
+  BATCH_CUDA(cudaMemset2DAsync(&b->st[0].status, sizeof(DevState), 0, sizeof(int), (size_t)b->reps, b->stream));
+  launch_pair_hist_batch(b->d_reps, b->reps, b->max_n, dr, rmax, nbins, b->hist, b->stream);
+  int e = batch_check(b);
+  if (e) return e;
+  BATCH_CUDA(cudaMemcpy(counts, b->hist, sizeof(uint64_t) * need, cudaMemcpyDeviceToHost));
+  std::vector<DevState> st;
+  return batch_status(b, st);
+}
+
+int hsmc_batch_last_timing(hsmc_batch *b, double *total_ms) {
+  if (!b || !total_ms) return HSMC_ERR_INVALID_ARG;
+  *total_ms = b->last_ms;
+  return HSMC_OK;
+}
+
+}  // extern "C"

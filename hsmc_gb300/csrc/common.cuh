@@ -202,12 +202,26 @@ struct DevState {
   int cells[3], per_cell;
   int nc_alloc[3];
   int pad2;
+  // non-empty cells per layout, colour and occupancy bucket (bucket b holds
+  // cells with min(n, NBUCKET - 1) = b particles), filled after each build
+  int list_len[2][8][9];
 };
 
-struct alignas(16) Slot {  // one particle in a cell: single-precision copy + id
+// One particle in a cell: its grid coordinates t (single precision, from
+// axis_cell of the rounded position, so t lies in the cell's own slab of
+// [0, L)) and its id.
+struct alignas(16) Slot {
   float x, y, z;
   int id;
 };
+
+// Occupancy buckets of the per-colour cell lists (n = 1..7, and 8 or more).
+constexpr int NBUCKET = 9;
+
+// Colour (0..7) of a cell of the 2x2x2 checkerboard.
+__host__ __device__ __forceinline__ int cell_colour(int ix, int iy, int iz) {
+  return (ix & 1) | ((iy & 1) << 1) | ((iz & 1) << 2);
+}
 
 // FP64 coordinates of particle id from the double[N][4] (id, x, y, z) array:
 // two aligned 16-byte loads.

@@ -14,6 +14,8 @@ struct SysPtrs {
   double *pos;         // N x 4 doubles: (id, x, y, z), the reference's layout
   int *cnt[2];         // per-cell particle counts, one array per layout
   Slot *slot[2];       // per-cell slots, capacity `cap`, one array per layout
+  int *list[2];        // per layout: the non-empty cells by colour and occupancy,
+                       // 8 x NBUCKET segments of ncell_alloc / 8 entries
   Box *box;            // box and cell grid
   DevState *st;        // counters, parameters, status
   uint32_t *trace;     // trace records (12 words each) or nullptr
@@ -23,6 +25,9 @@ struct SysPtrs {
   int ncell_alloc;     // cells allocated per layout
 };
 
+// api.cu: device cell grid for a box (even count per axis, edge >= 1 + margin)
+int make_box(const double len[3], double rho, Box &b, int &cap);
+
 // sweep.cu
 void launch_build(const SysPtrs &p, long long sweep_offset, int num_sms, cudaStream_t s);
 void launch_move_pass(const SysPtrs &p, int pass, int group, bool trace, int grid, cudaStream_t s);
@@ -30,6 +35,16 @@ void launch_advance(const SysPtrs &p, int n_sweeps, cudaStream_t s);
 void launch_volume_move(const SysPtrs &p, long long sweep_offset, double margin, cudaStream_t s);
 void launch_volume_scan(const SysPtrs &p, cudaStream_t s);
 int move_pass_grid(int group, int cap, int ncell_alloc, int num_sms);
+
+// batched replicas: reps is a device array of n_reps SysPtrs
+void launch_build_batch(const SysPtrs *reps, int n_reps, int max_n, int max_ncell, long long sweep_offset,
+                        cudaStream_t s);
+void launch_move_pass_batch(const SysPtrs *reps, int n_reps, int cap, int pass, int group, int grid_x,
+                            cudaStream_t s);
+void launch_advance_batch(const SysPtrs *reps, int n_reps, int n_sweeps, cudaStream_t s);
+int move_pass_grid_batch(int group, int max_ncell);
+void launch_pair_hist_batch(const SysPtrs *reps, int n_reps, int max_n, double bin, double rmax, int nbins,
+                            unsigned long long *counts, cudaStream_t s);
 
 // observables.cu
 void launch_pair_hist(const SysPtrs &p, double bin, double rmax, int nbins, unsigned long long *counts,

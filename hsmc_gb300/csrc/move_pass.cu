@@ -18,16 +18,16 @@
 
 namespace hsmc {
 
-// Grid coordinate of a candidate relative to the active cell: its own t plus
-// the periodic image of the neighbour cell it sits in.
-__device__ __forceinline__ float4 staged_coord(const Slot &o, const float *sh, const float *L32, const float *iw,
-                                               const int *nc, float ix, float iy, float iz) {
-  int ci;
-  float tx, ty, tz;
-  axis_cell(o.x, sh[0], L32[0], iw[0], nc[0], ci, tx);
-  axis_cell(o.y, sh[1], L32[1], iw[1], nc[1], ci, ty);
-  axis_cell(o.z, sh[2], L32[2], iw[2], nc[2], ci, tz);
-  return make_float4(__fadd_rn(tx, ix), __fadd_rn(ty, iy), __fadd_rn(tz, iz), __int_as_float(o.id));
+// Neighbour offsets of the 26 cells around a cell, packed (dx+1) | (dy+1)<<2
+// | (dz+1)<<4, in the order x-major, the cell itself left out.
+__constant__ unsigned char c_nbr[26] = {
+    0x00, 0x10, 0x20, 0x04, 0x14, 0x24, 0x08, 0x18, 0x28, 0x01, 0x11, 0x21, 0x05,
+    0x25, 0x09, 0x19, 0x29, 0x02, 0x12, 0x22, 0x06, 0x16, 0x26, 0x0a, 0x1a, 0x2a};
+
+// Grid coordinate of a candidate relative to the active cell: the slot's t
+// plus the periodic image of the neighbour cell it sits in.
+__device__ __forceinline__ float4 staged_coord(const Slot &o, float ix, float iy, float iz) {
+  return make_float4(__fadd_rn(o.x, ix), __fadd_rn(o.y, iy), __fadd_rn(o.z, iz), __int_as_float(o.id));
 }
 
 __device__ __forceinline__ float dist2(float ux, float uy, float uz, const float4 &q) {
@@ -35,8 +35,11 @@ __device__ __forceinline__ float dist2(float ux, float uy, float uz, const float
   return dx * dx + dy * dy + dz * dz;
 }
 
-template <int G, int CAP, bool TRACE>
-__global__ void __launch_bounds__(128, 4) k_move_pass(SysPtrs p, int pass) {
+template <int G, int CAP, bool TRACE, bool BATCH>
+__global__ void __launch_bounds__(128, 4) k_move_pass(SysPtrs p1, const SysPtrs *reps, int pass) {
+  // In a batch, blockIdx.y is the replica (see k_build).
+  const SysPtrs p = BATCH ? reps[blockIdx.y] : p1;
+  const uint32_t rep = BATCH ? blockIdx.y : 0u;
   static_assert(G == 1 || G == 2 || G == 4 || G == 8, "group size");
   constexpr int NB = (26 + G - 1) / G;  // neighbour cells per lane
   // Staged neighbour particles per thread: about 27 rho w^3 / G on average;
@@ -68,6 +71,7 @@ __global__ void __launch_bounds__(128, 4) k_move_pass(SysPtrs p, int pass) {
   if (pass == 0) {
     int *other = p.cnt[layout ^ 1];
     for (int c = blockIdx.x * blockDim.x + threadIdx.x; c < p.ncell_alloc; c += gridDim.x * blockDim.x) other[c] = 0;
+    if (blockIdx.x == 0 && threadIdx.x < 8 * NBUCKET) (&p.st->list_len[layout ^ 1][0][0])[threadIdx.x] = 0;
   }
 
   const int tid = (int)threadIdx.x;
@@ -76,26 +80,42 @@ __global__ void __launch_bounds__(128, 4) k_move_pass(SysPtrs p, int pass) {
   const int groups = (int)((gridDim.x * blockDim.x) / G);
   const int gbase = (tid & 31) & ~(G - 1);
   const unsigned gmask = (G == 32) ? 0xffffffffu : (((1u << G) - 1u) << gbase);
-  const int hx = nc[0] >> 1, hy = nc[1] >> 1, hz = nc[2] >> 1;
-  const int n_active = hx * hy * hz;
-  const int cx = colour & 1, cy = (colour >> 1) & 1, cz = (colour >> 2) & 1;
 
   unsigned acc = 0, rej_o = 0, rej_b = 0, rechecks = 0;
 
-  for (int ac = group; ac < n_active; ac += groups) {
-    const int ax = ac % hx, ayz = ac / hx, ay = ayz % hy, az = ayz / hy;
-    const int ix = 2 * ax + cx, iy = 2 * ay + cy, iz = 2 * az + cz;
-    const int c = ix + nc[0] * (iy + nc[1] * iz);
+  // The non-empty cells of this colour, fullest first: consecutive groups
+  // (the lanes of one warp) get cells with the same number of trials.
+  int blen[NBUCKET];
+  int n_list = 0;
+#pragma unroll
+  for (int b = 0; b < NBUCKET; b++) {
+    blen[b] = st->list_len[layout][colour][b];
+    n_list += blen[b];
+  }
+  const size_t seg = (size_t)(p.ncell_alloc / 8);
+  const int *__restrict__ lists = p.list[layout] + (size_t)colour * NBUCKET * seg;
 
-    // (1) counts, all issued together
+  for (int li = group; li < n_list; li += groups) {
+    int b = NBUCKET - 1, off = li;
+    while (off >= blen[b]) {
+      off -= blen[b];
+      b--;
+    }
+    const int c = lists[(size_t)b * seg + off];
+    const int ix = c % nc[0], iyz = c / nc[0], iy = iyz % nc[1], iz = iyz / nc[1];
+
+    // (1) counts of the cell and of this lane's neighbour cells, issued together
     int nb_c[NB], nb_n[NB];
+    unsigned nb_code[NB];
 #pragma unroll
     for (int q = 0; q < NB; q++) {
       const int o26 = lane + q * G;
       nb_c[q] = c;
+      nb_code[q] = 0x15u;  // offset (0,0,0)
       if (o26 < 26) {
-        const int o = o26 < 13 ? o26 : o26 + 1;  // 13 is the cell itself
-        int x = ix + o / 9 - 1, y = iy + (o / 3) % 3 - 1, z = iz + o % 3 - 1;
+        const unsigned code = c_nbr[o26];
+        nb_code[q] = code;
+        int x = ix + (int)(code & 3u) - 1, y = iy + (int)((code >> 2) & 3u) - 1, z = iz + (int)(code >> 4) - 1;
         x += x < 0 ? nc[0] : (x >= nc[0] ? -nc[0] : 0);
         y += y < 0 ? nc[1] : (y >= nc[1] ? -nc[1] : 0);
         z += z < 0 ? nc[2] : (z >= nc[2] ? -nc[2] : 0);
@@ -108,7 +128,6 @@ __global__ void __launch_bounds__(128, 4) k_move_pass(SysPtrs p, int pass) {
       const int m = (lane + q * G < 26) ? cnt[nb_c[q]] : 0;
       nb_n[q] = m < CAP ? m : CAP;  // an overfull cell was flagged by the build
     }
-    if (n == 0) continue;
     if (n > CAP) {
       if (lane == 0) atomicOr(&p.st->status, ST_CELL_OVERFLOW);
       continue;
@@ -124,14 +143,13 @@ __global__ void __launch_bounds__(128, 4) k_move_pass(SysPtrs p, int pass) {
 #pragma unroll
       for (int q = 0; q < NB; q++) {
         if (nb_n[q] == 0) continue;
-        const int o26 = lane + q * G;
-        const int o = o26 < 13 ? o26 : o26 + 1;
-        const int ox = o / 9 - 1, oy = (o / 3) % 3 - 1, oz = o % 3 - 1;
+        const unsigned code = nb_code[q];
+        const int ox = (int)(code & 3u) - 1, oy = (int)((code >> 2) & 3u) - 1, oz = (int)(code >> 4) - 1;
         const float imx = (ix + ox < 0) ? -L32[0] : (ix + ox >= nc[0] ? L32[0] : 0.f);
         const float imy = (iy + oy < 0) ? -L32[1] : (iy + oy >= nc[1] ? L32[1] : 0.f);
         const float imz = (iz + oz < 0) ? -L32[2] : (iz + oz >= nc[2] ? L32[2] : 0.f);
         for (int k = 0; k < nb_n[q]; k++)
-          stage[w++][tid] = staged_coord(slot[(size_t)nb_c[q] * CAP + k], sh, L32, iw, nc, imx, imy, imz);
+          stage[w++][tid] = staged_coord(slot[(size_t)nb_c[q] * CAP + k], imx, imy, imz);
       }
     }
 
@@ -146,22 +164,22 @@ __global__ void __launch_bounds__(128, 4) k_move_pass(SysPtrs p, int pass) {
       while (at > 0 && qid[at - 1] > sv.id) {
         qid[at] = qid[at - 1];
         qslot[at] = qslot[at - 1];
+        tx[at] = tx[at - 1];
+        ty[at] = ty[at - 1];
+        tz[at] = tz[at - 1];
         at--;
       }
       qid[at] = sv.id;
       qslot[at] = j;
+      tx[at] = sv.x;
+      ty[at] = sv.y;
+      tz[at] = sv.z;
     }
-    for (int j = 0; j < n; j++) {
-      load_xyz(pos, qid[j], qx[j], qy[j], qz[j]);
-      int ci;
-      axis_cell(__double2float_rn(qx[j]), sh[0], L32[0], iw[0], nc[0], ci, tx[j]);
-      axis_cell(__double2float_rn(qy[j]), sh[1], L32[1], iw[1], nc[1], ci, ty[j]);
-      axis_cell(__double2float_rn(qz[j]), sh[2], L32[2], iw[2], nc[2], ci, tz[j]);
-    }
+    for (int j = 0; j < n; j++) load_xyz(pos, qid[j], qx[j], qy[j], qz[j]);
 
     unsigned moved = 0;
     for (int trial = 0; trial < n; trial++) {
-      const U32x4 r = draw4(seed, (uint32_t)trial, (uint32_t)c, seq, TAG_MOVE);
+      const U32x4 r = draw4(seed, (rep << 8) | (uint32_t)trial, (uint32_t)c, seq, TAG_MOVE);
       const int s = (int)__umulhi(r.x, (unsigned)n);  // rank of the moving particle
       const double nx = propose_axis(qx[s], centred_offset(r.y), dr, len[0]);
       const double ny = propose_axis(qy[s], centred_offset(r.z), dr, len[1]);
@@ -226,14 +244,13 @@ __global__ void __launch_bounds__(128, 4) k_move_pass(SysPtrs p, int pass) {
 #pragma unroll
           for (int q = 0; q < NB; q++) {
             if (nb_n[q] == 0) continue;
-            const int o26 = lane + q * G;
-            const int o = o26 < 13 ? o26 : o26 + 1;
-            const int ox = o / 9 - 1, oy = (o / 3) % 3 - 1, oz = o % 3 - 1;
+            const unsigned code = nb_code[q];
+            const int ox = (int)(code & 3u) - 1, oy = (int)((code >> 2) & 3u) - 1, oz = (int)(code >> 4) - 1;
             const float imx = (ix + ox < 0) ? -L32[0] : (ix + ox >= nc[0] ? L32[0] : 0.f);
             const float imy = (iy + oy < 0) ? -L32[1] : (iy + oy >= nc[1] ? L32[1] : 0.f);
             const float imz = (iz + oz < 0) ? -L32[2] : (iz + oz >= nc[2] ? L32[2] : 0.f);
             for (int k = 0; k < nb_n[q] && !ov; k++) {
-              const float4 a = staged_coord(slot[(size_t)nb_c[q] * CAP + k], sh, L32, iw, nc, imx, imy, imz);
+              const float4 a = staged_coord(slot[(size_t)nb_c[q] * CAP + k], imx, imy, imz);
               const float r2 = dist2(ux, uy, uz, a);
               if (r2 < lo) {
                 ov = true;
@@ -295,8 +312,7 @@ __global__ void __launch_bounds__(128, 4) k_move_pass(SysPtrs p, int pass) {
       pp[1] = qx[j];
       pp[2] = qy[j];
       pp[3] = qz[j];
-      slot[(size_t)c * CAP + qslot[j]] =
-          Slot{__double2float_rn(qx[j]), __double2float_rn(qy[j]), __double2float_rn(qz[j]), qid[j]};
+      slot[(size_t)c * CAP + qslot[j]] = Slot{tx[j], ty[j], tz[j], qid[j]};
     }
   }
 
@@ -317,7 +333,7 @@ __global__ void __launch_bounds__(128, 4) k_move_pass(SysPtrs p, int pass) {
 template <int G, int CAP>
 static int pass_blocks_for(int ncell_alloc, int num_sms) {
   int per_sm = 0;
-  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_move_pass<G, CAP, false>, 128, 0);
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_move_pass<G, CAP, false, false>, 128, 0);
   if (per_sm < 1) per_sm = 1;
   const long long threads = (long long)(ncell_alloc / 8) * G;
   const int need = (int)((threads + 127) / 128);
@@ -345,8 +361,38 @@ int move_pass_grid(int group, int cap, int ncell_alloc, int num_sms) {
 
 template <int G, int CAP>
 static void launch_gc(const SysPtrs &p, int pass, bool trace, int grid, cudaStream_t s) {
-  if (trace) k_move_pass<G, CAP, true><<<grid, 128, 0, s>>>(p, pass);
-  else k_move_pass<G, CAP, false><<<grid, 128, 0, s>>>(p, pass);
+  if (trace) k_move_pass<G, CAP, true, false><<<grid, 128, 0, s>>>(p, nullptr, pass);
+  else k_move_pass<G, CAP, false, false><<<grid, 128, 0, s>>>(p, nullptr, pass);
+}
+
+template <int G, int CAP>
+static void launch_batch_gc(const SysPtrs *reps, int n_reps, int pass, int grid_x, cudaStream_t s) {
+  k_move_pass<G, CAP, false, true><<<dim3((unsigned)grid_x, (unsigned)n_reps), 128, 0, s>>>(SysPtrs{}, reps, pass);
+}
+
+// Blocks per replica for the batched pass: enough groups for the largest
+// replica's colour list; blocks past a smaller replica's list exit at once.
+int move_pass_grid_batch(int group, int max_ncell) {
+  const long long threads = (long long)(max_ncell / 8) * group;
+  const int x = (int)((threads + 127) / 128);
+  return x > 0 ? x : 1;
+}
+
+void launch_move_pass_batch(const SysPtrs *reps, int n_reps, int cap, int pass, int group, int grid_x,
+                            cudaStream_t s) {
+#define HSMC_BATCH_CAP(G)                                                      \
+  switch (cap) {                                                               \
+    case 8: launch_batch_gc<G, 8>(reps, n_reps, pass, grid_x, s); break;       \
+    case 16: launch_batch_gc<G, 16>(reps, n_reps, pass, grid_x, s); break;     \
+    default: launch_batch_gc<G, 32>(reps, n_reps, pass, grid_x, s); break;     \
+  }
+  switch (group) {
+    case 1: HSMC_BATCH_CAP(1) break;
+    case 2: HSMC_BATCH_CAP(2) break;
+    case 4: HSMC_BATCH_CAP(4) break;
+    default: HSMC_BATCH_CAP(8) break;
+  }
+#undef HSMC_BATCH_CAP
 }
 
 template <int G>

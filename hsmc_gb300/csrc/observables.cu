@@ -89,6 +89,15 @@ __device__ __forceinline__ void for_each_near(const CellView &v, const Stencil &
   }
 }
 
+// Grid coordinates of a point (the slots hold particles this way).
+__device__ __forceinline__ void grid_coords(const CellView &v, double x, double y, double z, float &tx, float &ty,
+                                            float &tz) {
+  int ci;
+  axis_cell(__double2float_rn(x), v.sh[0], v.L32[0], v.iw[0], v.nc[0], ci, tx);
+  axis_cell(__double2float_rn(y), v.sh[1], v.L32[1], v.iw[1], v.nc[1], ci, ty);
+  axis_cell(__double2float_rn(z), v.sh[2], v.L32[2], v.iw[2], v.nc[2], ci, tz);
+}
+
 // Single-precision squared minimum-image distance, for discarding far pairs.
 __device__ __forceinline__ float approx_r2(float ax, float ay, float az, const Slot &o, const float *L32) {
   float dx = ax - o.x, dy = ay - o.y, dz = az - o.z;
@@ -101,8 +110,22 @@ __device__ __forceinline__ float approx_r2(float ax, float ay, float az, const S
 // ------------------------------------------------------------ pair counts
 constexpr int HIST_SMEM_BINS = 4096;
 
-__global__ void __launch_bounds__(256) k_pair_hist(SysPtrs p, Stencil s, double bin, double rmax, int nbins,
-                                                   unsigned long long *counts, float cut2) {
+// In a batch (BATCH), blockIdx.y is the replica: its pointers come from reps,
+// its counts go to counts + replica * nbins, and its stencil follows its grid.
+template <bool BATCH>
+__global__ void __launch_bounds__(256) k_pair_hist(SysPtrs p1, const SysPtrs *reps, Stencil s1, double bin,
+                                                   double rmax, int nbins, unsigned long long *counts1, float cut2) {
+  const SysPtrs p = BATCH ? reps[blockIdx.y] : p1;
+  unsigned long long *counts = BATCH ? counts1 + (size_t)blockIdx.y * nbins : counts1;
+  Stencil s = s1;
+  if (BATCH) {
+    for (int d = 0; d < 3; d++) {
+      const int nc = p.box->nc[d];
+      int kk = (int)ceil((rmax + 1e-3) * nc / p.box->len[d]);
+      kk = kk < 1 ? 1 : kk;
+      s.k[d] = (2 * kk + 1 >= nc) ? -1 : kk;
+    }
+  }
   __shared__ unsigned int sh[HIST_SMEM_BINS];
   const bool use_sh = nbins <= HIST_SMEM_BINS;
   if (use_sh)
@@ -117,7 +140,8 @@ __global__ void __launch_bounds__(256) k_pair_hist(SysPtrs p, Stencil s, double 
   if (i < p.n) {
     double x, y, z;
     load_xyz(p.pos, i, x, y, z);
-    const float x32 = __double2float_rn(x), y32 = __double2float_rn(y), z32 = __double2float_rn(z);
+    float x32, y32, z32;  // grid coordinates, as the slots hold them
+    grid_coords(v, x, y, z, x32, y32, z32);
     for_each_near(v, s, x, y, z, [&](const Slot &o) {
       if (o.id == i) return;
       if (approx_r2(x32, y32, z32, o, v.L32) > cut2) return;
@@ -153,7 +177,14 @@ void launch_pair_hist(const SysPtrs &p, double bin, double rmax, int nbins, unsi
   Stencil s{{stencil[0], stencil[1], stencil[2]}};
   const float cut = (float)rmax + 1e-3f;
   const int blocks = (p.n + 255) / 256;
-  k_pair_hist<<<blocks > 0 ? blocks : 1, 256, 0, st>>>(p, s, bin, rmax, nbins, counts, cut * cut);
+  k_pair_hist<false><<<blocks > 0 ? blocks : 1, 256, 0, st>>>(p, nullptr, s, bin, rmax, nbins, counts, cut * cut);
+}
+
+void launch_pair_hist_batch(const SysPtrs *reps, int n_reps, int max_n, double bin, double rmax, int nbins,
+                            unsigned long long *counts, cudaStream_t st) {
+  const float cut = (float)rmax + 1e-3f;
+  const dim3 grid((unsigned)((max_n + 255) / 256), (unsigned)n_reps);
+  k_pair_hist<true><<<grid, 256, 0, st>>>(SysPtrs{}, reps, Stencil{{0, 0, 0}}, bin, rmax, nbins, counts, cut * cut);
 }
 
 // ------------------------------------------------------- scaled overlap
@@ -169,7 +200,8 @@ __global__ void __launch_bounds__(256) k_scaled_scan(SysPtrs p, Stencil s, int n
   if (i < p.n) {
     double x, y, z;
     load_xyz(p.pos, i, x, y, z);
-    const float x32 = __double2float_rn(x), y32 = __double2float_rn(y), z32 = __double2float_rn(z);
+    float x32, y32, z32;  // grid coordinates, as the slots hold them
+    grid_coords(v, x, y, z, x32, y32, z32);
     for_each_near(v, s, x, y, z, [&](const Slot &o) {
       if (o.id == i) return;
       if (approx_r2(x32, y32, z32, o, v.L32) > cut2) return;
@@ -206,7 +238,8 @@ void launch_scaled_scan(const SysPtrs &p, const double *sf, int n_sf, int stenci
 __device__ __forceinline__ bool point_overlaps(const CellView &v, const SysPtrs &p, const Stencil &s, double x,
                                                double y, double z, int skip, const double *len,
                                                const double *half) {
-  const float x32 = __double2float_rn(x), y32 = __double2float_rn(y), z32 = __double2float_rn(z);
+  float x32, y32, z32;  // grid coordinates, as the slots hold them
+  grid_coords(v, x, y, z, x32, y32, z32);
   bool ov = false;
   for_each_near(v, s, x, y, z, [&](const Slot &o) {
     if (ov || o.id == skip) return;
@@ -297,7 +330,8 @@ __global__ void __launch_bounds__(128) k_ql(SysPtrs p, Stencil s, int l, double 
   if (i >= p.n) return;
   double x, y, z;
   load_xyz(p.pos, i, x, y, z);
-  const float x32 = __double2float_rn(x), y32 = __double2float_rn(y), z32 = __double2float_rn(z);
+  float x32, y32, z32;  // grid coordinates, as the slots hold them
+  grid_coords(v, x, y, z, x32, y32, z32);
   double re[QL_LMAX + 1], im[QL_LMAX + 1];
   for (int m = 0; m <= QL_LMAX; m++) re[m] = im[m] = 0.0;
   int bonds = 0;

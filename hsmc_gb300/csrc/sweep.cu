@@ -23,12 +23,18 @@ namespace hsmc {
 // ------------------------------------------------------------------ build
 // Bins every particle into the layout of sweep s = sweep_base + offset.
 // Thread 0 also publishes that sweep's shift and colour order.
-__global__ void __launch_bounds__(256) k_build(SysPtrs p, long long offset) {
+// In a batch (BATCH), blockIdx.y is the replica and its pointers come from
+// reps; the replica index enters every random counter, so replica 0 draws
+// what a single system draws.
+template <bool BATCH>
+__global__ void __launch_bounds__(256) k_build(SysPtrs p1, const SysPtrs *reps, long long offset) {
+  const SysPtrs p = BATCH ? reps[blockIdx.y] : p1;
+  const uint32_t rep = BATCH ? blockIdx.y : 0u;
   const DevState *st = p.st;
   const Box *bx = p.box;
   const unsigned long long s = st->sweep_base + (unsigned long long)offset;
   const unsigned long long seed = st->seed;
-  const U32x4 rs = draw4(seed, 0u, 0u, s, TAG_SHIFT);
+  const U32x4 rs = draw4(seed, rep << 8, 0u, s, TAG_SHIFT);
   const float w0 = bx->w32[0], w1 = bx->w32[1], w2 = bx->w32[2];
   const float sh0 = __fmul_rn(__uint2float_rn(rs.x >> 8) * 5.9604644775390625e-08f, w0);
   const float sh1 = __fmul_rn(__uint2float_rn(rs.y >> 8) * 5.9604644775390625e-08f, w1);
@@ -42,7 +48,7 @@ __global__ void __launch_bounds__(256) k_build(SysPtrs p, long long offset) {
     ws->params.shift32[1] = sh1;
     ws->params.shift32[2] = sh2;
     int perm[8] = {0, 1, 2, 3, 4, 5, 6, 7};
-    const U32x4 ra = draw4(seed, 0u, 0u, s, TAG_PERM), rb = draw4(seed, 1u, 0u, s, TAG_PERM);
+    const U32x4 ra = draw4(seed, rep << 8, 0u, s, TAG_PERM), rb = draw4(seed, (rep << 8) | 1u, 0u, s, TAG_PERM);
     const uint32_t r[7] = {ra.x, ra.y, ra.z, ra.w, rb.x, rb.y, rb.z};
     for (int k = 7; k >= 1; k--) {  // Fisher-Yates
       int j = (int)__umulhi(r[7 - k], (unsigned)(k + 1));
@@ -57,20 +63,53 @@ __global__ void __launch_bounds__(256) k_build(SysPtrs p, long long offset) {
   const double2 b = *reinterpret_cast<const double2 *>(p.pos + 4 * (size_t)i + 2);
   const float x32 = __double2float_rn(a.y), y32 = __double2float_rn(b.x), z32 = __double2float_rn(b.y);
   int cx, cy, cz;
-  float t;
-  axis_cell(x32, sh0, bx->len32[0], bx->inv_w32[0], bx->nc[0], cx, t);
-  axis_cell(y32, sh1, bx->len32[1], bx->inv_w32[1], bx->nc[1], cy, t);
-  axis_cell(z32, sh2, bx->len32[2], bx->inv_w32[2], bx->nc[2], cz, t);
+  float tx, ty, tz;
+  axis_cell(x32, sh0, bx->len32[0], bx->inv_w32[0], bx->nc[0], cx, tx);
+  axis_cell(y32, sh1, bx->len32[1], bx->inv_w32[1], bx->nc[1], cy, ty);
+  axis_cell(z32, sh2, bx->len32[2], bx->inv_w32[2], bx->nc[2], cz, tz);
   const int c = cx + bx->nc[0] * (cy + bx->nc[1] * cz);
   const int k = atomicAdd(p.cnt[layout] + c, 1);
   if (k < p.cap) {
-    p.slot[layout][(size_t)c * p.cap + k] = Slot{x32, y32, z32, i};
+    p.slot[layout][(size_t)c * p.cap + k] = Slot{tx, ty, tz, i};
   } else {
     atomicOr(&p.st->status, ST_CELL_OVERFLOW);
   }
+
 }
 
 __global__ void k_advance(DevState *st, int n) { st->sweep_base += (unsigned long long)n; }
+
+// After a build: list the non-empty cells of each colour by occupancy, so a
+// move pass can hand cells of equal occupancy (equal trial counts) to the
+// lanes of one warp and start the fullest cells first.  Appends are counted
+// per block in shared memory and claimed with one global atomic per
+// (colour, occupancy) per block.
+template <bool BATCH>
+__global__ void __launch_bounds__(256) k_classify(SysPtrs p1, const SysPtrs *reps) {
+  const SysPtrs p = BATCH ? reps[blockIdx.y] : p1;
+  __shared__ int s_cnt[8 * NBUCKET], s_base[8 * NBUCKET];
+  const int layout = (int)(p.st->params.sweep & 1ull);
+  const Box *bx = p.box;
+  const int ncell = bx->ncell;
+  for (int q = threadIdx.x; q < 8 * NBUCKET; q += blockDim.x) s_cnt[q] = 0;
+  __syncthreads();
+  const int c = blockIdx.x * blockDim.x + threadIdx.x;
+  int key = -1, local = 0;
+  if (c < ncell) {
+    const int n = p.cnt[layout][c];
+    if (n > 0) {
+      const int ix = c % bx->nc[0], iyz = c / bx->nc[0], iy = iyz % bx->nc[1], iz = iyz / bx->nc[1];
+      key = cell_colour(ix, iy, iz) * NBUCKET + (n < NBUCKET - 1 ? n : NBUCKET - 1);
+      local = atomicAdd(&s_cnt[key], 1);
+    }
+  }
+  __syncthreads();
+  for (int q = threadIdx.x; q < 8 * NBUCKET; q += blockDim.x)
+    if (s_cnt[q] > 0) s_base[q] = atomicAdd(&p.st->list_len[layout][q / NBUCKET][q % NBUCKET], s_cnt[q]);
+  __syncthreads();
+  if (key >= 0) p.list[layout][(size_t)key * (p.ncell_alloc / 8) + s_base[key] + local] = c;
+}
+
 
 // ------------------------------------------------------------ volume move
 // vol_move (src/moves.c:83-153) as four launches so it stays on the device:
@@ -117,11 +156,11 @@ __global__ void __launch_bounds__(256) k_vol_scan(SysPtrs p) {
   const float reach = (float)(1.0 / sf) + 1e-3f;
   double x, y, z;
   load_xyz(p.pos, i, x, y, z);
-  const float xs[3] = {__double2float_rn(x), __double2float_rn(y), __double2float_rn(z)};
+  const float xr[3] = {__double2float_rn(x), __double2float_rn(y), __double2float_rn(z)};
+  float xs[3];  // grid coordinates, as the slots hold them
   int ci[3], k[3];
   for (int d = 0; d < 3; d++) {
-    float t;
-    axis_cell(xs[d], sh[d], L32[d], iw[d], nc[d], ci[d], t);
+    axis_cell(xr[d], sh[d], L32[d], iw[d], nc[d], ci[d], xs[d]);
     k[d] = (int)ceilf(reach * iw[d] * 1.0001f);
     if (2 * k[d] + 1 > nc[d]) k[d] = -1;
   }
@@ -226,7 +265,25 @@ void launch_volume_move(const SysPtrs &p, long long sweep_offset, double margin,
 void launch_build(const SysPtrs &p, long long sweep_offset, int num_sms, cudaStream_t s) {
   (void)num_sms;
   const int blocks = (p.n + 255) / 256;
-  k_build<<<blocks > 0 ? blocks : 1, 256, 0, s>>>(p, sweep_offset);
+  k_build<false><<<blocks > 0 ? blocks : 1, 256, 0, s>>>(p, nullptr, sweep_offset);
+  k_classify<false><<<(p.ncell_alloc + 255) / 256, 256, 0, s>>>(p, nullptr);
+}
+
+void launch_build_batch(const SysPtrs *reps, int n_reps, int max_n, int max_ncell, long long sweep_offset,
+                        cudaStream_t s) {
+  const dim3 grid((unsigned)((max_n + 255) / 256), (unsigned)n_reps);
+  k_build<true><<<grid, 256, 0, s>>>(SysPtrs{}, reps, sweep_offset);
+  const dim3 cgrid((unsigned)((max_ncell + 255) / 256), (unsigned)n_reps);
+  k_classify<true><<<cgrid, 256, 0, s>>>(SysPtrs{}, reps);
+}
+
+__global__ void k_advance_batch(const SysPtrs *reps, int n_reps, int n) {
+  const int r = blockIdx.x * blockDim.x + threadIdx.x;
+  if (r < n_reps) reps[r].st->sweep_base += (unsigned long long)n;
+}
+
+void launch_advance_batch(const SysPtrs *reps, int n_reps, int n_sweeps, cudaStream_t s) {
+  k_advance_batch<<<(n_reps + 127) / 128, 128, 0, s>>>(reps, n_reps, n_sweeps);
 }
 
 void launch_advance(const SysPtrs &p, int n_sweeps, cudaStream_t s) { k_advance<<<1, 1, 0, s>>>(p.st, n_sweeps); }

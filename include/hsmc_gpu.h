@@ -165,6 +165,29 @@ int hsmc_gpu_rng_set_state(hsmc_ctx *ctx, const uint64_t state[4]);
  * before exit(EXIT_FAILURE)); never NULL. */
 const char *hsmc_gpu_strerror(int status);
 
+/* ------------------------------------------------------ batched replicas
+ * Many independent NVT systems (different N, box and density) advanced
+ * together: every kernel of a sweep covers all replicas in one launch, and
+ * sweeps run as one CUDA graph.  Replica k's chain is the chain a context
+ * with the same parameters would run, except that k enters its random
+ * counters; replica 0 of a batch reproduces a single context exactly.
+ * Each system is the reference's single-system NVT run (hs_nvt,
+ * src/nvt.c:30-199); the batch has no reference counterpart. */
+typedef struct hsmc_batch hsmc_batch;
+
+int hsmc_batch_create(const hsmc_params *params, int n_systems, hsmc_batch **out);
+void hsmc_batch_destroy(hsmc_batch *b);
+int hsmc_batch_upload_config(hsmc_batch *b, int k, const double (*conf)[4], int n);
+int hsmc_batch_download_config(hsmc_batch *b, int k, double (*conf)[4], int n);
+int hsmc_batch_set_steps(hsmc_batch *b, const double *dr_max);
+/* counters: n_systems x 6 in the order of hsmc_gpu_sweeps (may be NULL) */
+int hsmc_batch_sweeps(hsmc_batch *b, int n_sweeps, uint64_t *counters);
+/* virial contact counts of every replica: counts[k * nbins + bin], with
+ * rmax = dr * nbins + 1 as hsmc_gpu_pressv takes it */
+int hsmc_batch_pressv(hsmc_batch *b, double dr, double rmax, int nbins, uint64_t *counts);
+/* device time of the last hsmc_batch_sweeps call, in milliseconds */
+int hsmc_batch_last_timing(hsmc_batch *b, double *total_ms);
+
 /* ----------------------------------------------------- replay and checks
  * Entry points that evaluate the reference's decisions on given inputs
  * without advancing the chain.  They exist so a caller (or a test) can compare

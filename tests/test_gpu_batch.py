@@ -1,0 +1,82 @@
+"""Batched replicas: one launch per kernel for all systems; each replica must
+be the chain a single context runs (replica 0 bit for bit), stay
+overlap-free, and give the single-context observables on its configuration."""
+import math
+
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+
+def test_replica_zero_is_the_single_system_chain(gpu_lib):
+    from hsmc_gb300.batch import ReplicaBatch
+
+    systems = [(0.80, 6, 0.15, 77), (0.50, 4, 0.30, 78), (0.92, 5, 0.08, 79)]
+    b = ReplicaBatch(systems)
+    c = b.sweeps(27)  # three graph launches and a remainder
+    s = gpu_lib.HardSphereSystem(rho=0.80, cells=6, dr_max=0.15, seed=77)
+    cs = s.sweep_nvt(27)
+    assert np.array_equal(b.download(0), s.download())
+    assert np.array_equal(c[0], cs)
+
+
+def test_uneven_replicas_stay_overlap_free(oracle_mod, gpu_lib):
+    from hsmc_gb300.batch import ReplicaBatch
+
+    rng = np.random.default_rng(3)
+    systems = []
+    for k in range(12):
+        n = int(rng.integers(3, 8))
+        rho = float(rng.uniform(0.3, 0.94))
+        systems.append((rho, n, 0.1 if rho > 0.8 else 0.25, 100 + k))
+    b = ReplicaBatch(systems)
+    c = b.sweeps(40)
+    for k, (rho, n, dr, seed) in enumerate(systems):
+        assert c[k, 0] == 40 * b.n[k]
+        assert 0.0 < c[k, 1] < c[k, 0]
+        conf = b.download(k)
+        L = b.box[k][0]
+        assert np.all(conf[:, 1:] >= 0) and np.all(conf[:, 1:] <= L)
+        for i in range(0, b.n[k], 7):
+            assert oracle_mod.OracleSim.brute_overlap(conf, b.box[k], i, *conf[i, 1:]) == 0
+
+
+def test_batched_virial_counts_match_single(gpu_lib):
+    from hsmc_gb300.batch import ReplicaBatch
+
+    systems = [(0.6, 5, 0.2, 1), (0.85, 6, 0.12, 2), (0.4, 4, 0.3, 3)]
+    b = ReplicaBatch(systems)
+    b.sweeps(30)
+    nb, dr = 5, 0.01
+    rmax = dr * nb + 1.0
+    got = b.pressv_counts(dr, rmax, nb)
+    for k, (rho, n, d, seed) in enumerate(systems):
+        s = gpu_lib.HardSphereSystem(rho=rho, cells=n, dr_max=d, seed=seed, conf=b.download(k))
+        assert np.array_equal(got[k], s.compute_pressv_counts(dr, rmax, nb))
+
+
+def test_replica_pressures_follow_carnahan_starling(gpu_lib):
+    """Per-replica contact pressure after equilibration, against CS within a
+    loose band set by the short run (the statistical gate is on C1)."""
+    from hsmc_gb300.batch import ReplicaBatch
+
+    rhos = [0.3, 0.5, 0.7]
+    b = ReplicaBatch([(r, 6, 0.3 if r < 0.6 else 0.15, 10 + i) for i, r in enumerate(rhos)])
+    b.sweeps(500)
+    nb, dr = 5, 0.01
+    rmax = dr * nb + 1.0
+    acc = np.zeros((len(rhos), nb))
+    samples = 50
+    for _ in range(samples):
+        b.sweeps(10)
+        acc += b.pressv_counts(dr, rmax, nb)
+    r = (np.arange(nb) + 0.5) * dr + 1.0
+    vol = 4 * np.pi / 3 * ((r + dr / 2) ** 3 - (r - dr / 2) ** 3)
+    for k, rho in enumerate(rhos):
+        g = acc[k] / samples / (vol * rho * b.n[k])
+        b1, b0 = np.polyfit(r, g, 1)
+        z = 1 + 2 * np.pi / 3 * rho * (b0 + b1)
+        eta = math.pi * rho / 6
+        z_cs = (1 + eta + eta**2 - eta**3) / (1 - eta) ** 3
+        assert abs(z - z_cs) < 0.12 * z_cs, (rho, z, z_cs)
