@@ -207,6 +207,7 @@ int hsmc_gpu_create(const hsmc_params *prm, hsmc_ctx **out) {
     cap = prm->cell_capacity <= 8 ? 8 : (prm->cell_capacity <= 16 ? 16 : 32);
   }
 
+  prepare_move_pass();
   hsmc_ctx *ctx = new hsmc_ctx();
   ctx->prm = *prm;
   ctx->n = prm->n_particles;
@@ -216,6 +217,10 @@ int hsmc_gpu_create(const hsmc_params *prm, hsmc_ctx **out) {
     case 0: ctx->group = kDefaultLanes; break;
     case 1: case 2: case 4: case 8: ctx->group = prm->lanes_per_cell; break;
     default: delete ctx; return HSMC_ERR_INVALID_ARG;
+  }
+  if (!move_pass_fits(ctx->group, cap)) {  // one lane per cell with 32-slot cells
+    delete ctx;
+    return HSMC_ERR_INVALID_ARG;
   }
   SysPtrs &sp = ctx->sp;
   sp.n = ctx->n;
@@ -237,7 +242,6 @@ int hsmc_gpu_create(const hsmc_params *prm, hsmc_ctx **out) {
     if ((ce = cudaMalloc(&sp.cnt[l], sizeof(int) * (size_t)sp.ncell_alloc)) != cudaSuccess) return fail(ce);
     if ((ce = cudaMalloc(&sp.slot[l], sizeof(Slot) * (size_t)sp.ncell_alloc * cap)) != cudaSuccess) return fail(ce);
     if ((ce = cudaMemset(sp.cnt[l], 0, sizeof(int) * (size_t)sp.ncell_alloc)) != cudaSuccess) return fail(ce);
-    if ((ce = cudaMalloc(&sp.list[l], sizeof(int) * (size_t)sp.ncell_alloc * NBUCKET)) != cudaSuccess) return fail(ce);
   }
   if ((ce = cudaMalloc(&sp.box, sizeof(Box))) != cudaSuccess) return fail(ce);
   if ((ce = cudaMalloc(&sp.st, sizeof(DevState))) != cudaSuccess) return fail(ce);
@@ -271,7 +275,6 @@ void hsmc_gpu_destroy(hsmc_ctx *ctx) {
   for (int l = 0; l < 2; l++) {
     cudaFree(sp.cnt[l]);
     cudaFree(sp.slot[l]);
-    cudaFree(sp.list[l]);
   }
   cudaFree(sp.box);
   cudaFree(sp.st);
@@ -303,7 +306,6 @@ int hsmc_gpu_upload_config(hsmc_ctx *ctx, const double (*conf)[4], int n) {
   for (int l = 0; l < 2; l++)
     HSMC_CUDA(cudaMemsetAsync(sp.cnt[l], 0, sizeof(int) * (size_t)sp.ncell_alloc, ctx->stream));
   HSMC_CUDA(cudaMemsetAsync(&sp.st->status, 0, sizeof(int), ctx->stream));
-  HSMC_CUDA(cudaMemsetAsync(&sp.st->list_len, 0, sizeof(sp.st->list_len), ctx->stream));
   launch_build(sp, -1, ctx->num_sms, ctx->stream);
   int e = check_kernels(ctx);
   if (e) return e;
@@ -378,7 +380,6 @@ static int ensure_graph(hsmc_ctx *ctx, bool npt) {
 static void rebuild_current_layout(hsmc_ctx *ctx) {
   const int layout = (int)((ctx->sweep_base - 1) & 1ull);
   cudaMemsetAsync(ctx->sp.cnt[layout], 0, sizeof(int) * (size_t)ctx->sp.ncell_alloc, ctx->stream);
-  cudaMemsetAsync(&ctx->sp.st->list_len[layout], 0, sizeof(ctx->sp.st->list_len[layout]), ctx->stream);
   launch_build(ctx->sp, -1, ctx->num_sms, ctx->stream);
 }
 
@@ -468,6 +469,7 @@ int hsmc_gpu_autotune(hsmc_ctx *ctx, int sweeps_per_variant, int *lanes_out) {
   int best = ctx->group;
   double best_ms = 1e300;
   for (int v = 0; v < 4; v++) {
+    if (!move_pass_fits(options[v], ctx->sp.cap)) continue;
     ctx->group = options[v];
     ctx->pass_grid = move_pass_grid(ctx->group, ctx->sp.cap, ctx->sp.ncell_alloc, ctx->num_sms);
     int e = run_sweeps(ctx, sweeps_per_variant, false, npt, nullptr);
@@ -770,7 +772,6 @@ int hsmc_gpu_rng_set_state(hsmc_ctx *ctx, const uint64_t st[4]) {
     SysPtrs &sp = ctx->sp;
     for (int l = 0; l < 2; l++)
       HSMC_CUDA(cudaMemsetAsync(sp.cnt[l], 0, sizeof(int) * (size_t)sp.ncell_alloc, ctx->stream));
-    HSMC_CUDA(cudaMemsetAsync(&sp.st->list_len, 0, sizeof(sp.st->list_len), ctx->stream));
     launch_build(sp, -1, ctx->num_sms, ctx->stream);
     int e = check_kernels(ctx);
     if (e) return e;

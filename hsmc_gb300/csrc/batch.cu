@@ -51,7 +51,7 @@ struct hsmc_batch {
   std::vector<char> uploaded;
   SysPtrs *d_reps = nullptr;
   double *pos = nullptr;
-  int *cnt[2] = {nullptr, nullptr}, *list[2] = {nullptr, nullptr};
+  int *cnt[2] = {nullptr, nullptr};
   Slot *slot[2] = {nullptr, nullptr};
   Box *box = nullptr;
   DevState *st = nullptr;
@@ -87,7 +87,6 @@ void hsmc_batch_destroy(hsmc_batch *b) {
   cudaFree(b->pos);
   for (int l = 0; l < 2; l++) {
     cudaFree(b->cnt[l]);
-    cudaFree(b->list[l]);
     cudaFree(b->slot[l]);
   }
   cudaFree(b->box);
@@ -145,12 +144,12 @@ int hsmc_batch_create(const hsmc_params *params, int n_systems, hsmc_batch **out
     return cuda_fail(e);
   };
   cudaError_t ce;
+  prepare_move_pass();
   if ((ce = cudaStreamCreateWithFlags(&b->stream, cudaStreamNonBlocking)) != cudaSuccess) return fail(ce);
   if ((ce = cudaMalloc(&b->pos, sizeof(double) * 4 * tot_n)) != cudaSuccess) return fail(ce);
   for (int l = 0; l < 2; l++) {
     if ((ce = cudaMalloc(&b->cnt[l], sizeof(int) * tot_cell)) != cudaSuccess) return fail(ce);
     if ((ce = cudaMemset(b->cnt[l], 0, sizeof(int) * tot_cell)) != cudaSuccess) return fail(ce);
-    if ((ce = cudaMalloc(&b->list[l], sizeof(int) * tot_cell * NBUCKET)) != cudaSuccess) return fail(ce);
     if ((ce = cudaMalloc(&b->slot[l], sizeof(Slot) * tot_cell * cap)) != cudaSuccess) return fail(ce);
   }
   if ((ce = cudaMalloc(&b->box, sizeof(Box) * n_systems)) != cudaSuccess) return fail(ce);
@@ -163,7 +162,6 @@ int hsmc_batch_create(const hsmc_params *params, int n_systems, hsmc_batch **out
     s.pos = b->pos + 4 * on;
     for (int l = 0; l < 2; l++) {
       s.cnt[l] = b->cnt[l] + oc;
-      s.list[l] = b->list[l] + oc * NBUCKET;
       s.slot[l] = b->slot[l] + oc * cap;
     }
     s.box = b->box + k;
@@ -212,7 +210,6 @@ int hsmc_batch_upload_config(hsmc_batch *b, int k, const double (*conf)[4], int 
   BATCH_CUDA(cudaMemcpyAsync(s.pos, conf, sizeof(double) * 4 * (size_t)n, cudaMemcpyHostToDevice, b->stream));
   for (int l = 0; l < 2; l++)
     BATCH_CUDA(cudaMemsetAsync(s.cnt[l], 0, sizeof(int) * (size_t)s.ncell_alloc, b->stream));
-  BATCH_CUDA(cudaMemsetAsync(&s.st->list_len, 0, sizeof(s.st->list_len), b->stream));
   BATCH_CUDA(cudaMemsetAsync(&s.st->status, 0, sizeof(int), b->stream));
   launch_build(s, -1, 0, b->stream);
   int e = batch_check(b);
@@ -244,7 +241,7 @@ int hsmc_batch_set_steps(hsmc_batch *b, const double *dr_max) {
 }
 
 static void enqueue_batch_sweep(hsmc_batch *b, long long offset, int grid_x) {
-  launch_build_batch(b->d_reps, b->reps, b->max_n, b->max_ncell, offset, b->stream);
+  launch_build_batch(b->d_reps, b->reps, b->max_n, offset, b->stream);
   for (int k = 0; k < 8; k++) launch_move_pass_batch(b->d_reps, b->reps, b->cap, k, b->group, grid_x, b->stream);
 }
 

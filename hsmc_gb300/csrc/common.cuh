@@ -202,9 +202,6 @@ struct DevState {
   int cells[3], per_cell;
   int nc_alloc[3];
   int pad2;
-  // non-empty cells per layout, colour and occupancy bucket (bucket b holds
-  // cells with min(n, NBUCKET - 1) = b particles), filled after each build
-  int list_len[2][8][9];
 };
 
 // One particle in a cell: its grid coordinates t (single precision, from
@@ -214,9 +211,6 @@ struct alignas(16) Slot {
   float x, y, z;
   int id;
 };
-
-// Occupancy buckets of the per-colour cell lists (n = 1..7, and 8 or more).
-constexpr int NBUCKET = 9;
 
 // Colour (0..7) of a cell of the 2x2x2 checkerboard.
 __host__ __device__ __forceinline__ int cell_colour(int ix, int iy, int iz) {

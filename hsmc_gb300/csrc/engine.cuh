@@ -14,8 +14,6 @@ struct SysPtrs {
   double *pos;         // N x 4 doubles: (id, x, y, z), the reference's layout
   int *cnt[2];         // per-cell particle counts, one array per layout
   Slot *slot[2];       // per-cell slots, capacity `cap`, one array per layout
-  int *list[2];        // per layout: the non-empty cells by colour and occupancy,
-                       // 8 x NBUCKET segments of ncell_alloc / 8 entries
   Box *box;            // box and cell grid
   DevState *st;        // counters, parameters, status
   uint32_t *trace;     // trace records (12 words each) or nullptr
@@ -24,6 +22,11 @@ struct SysPtrs {
   int cap;             // slots per cell
   int ncell_alloc;     // cells allocated per layout
 };
+
+// The arrays of one layout.  A select, not an index: indexing the parameter
+// struct by a runtime value would copy it to local memory.
+__device__ __forceinline__ int *cnt_of(const SysPtrs &p, int layout) { return layout ? p.cnt[1] : p.cnt[0]; }
+__device__ __forceinline__ Slot *slot_of(const SysPtrs &p, int layout) { return layout ? p.slot[1] : p.slot[0]; }
 
 // api.cu: device cell grid for a box (even count per axis, edge >= 1 + margin)
 int make_box(const double len[3], double rho, Box &b, int &cap);
@@ -35,10 +38,11 @@ void launch_advance(const SysPtrs &p, int n_sweeps, cudaStream_t s);
 void launch_volume_move(const SysPtrs &p, long long sweep_offset, double margin, cudaStream_t s);
 void launch_volume_scan(const SysPtrs &p, cudaStream_t s);
 int move_pass_grid(int group, int cap, int ncell_alloc, int num_sms);
+bool move_pass_fits(int group, int cap);  // its shared memory fits a block on this device
+void prepare_move_pass();                 // allow each variant its shared memory (current device)
 
 // batched replicas: reps is a device array of n_reps SysPtrs
-void launch_build_batch(const SysPtrs *reps, int n_reps, int max_n, int max_ncell, long long sweep_offset,
-                        cudaStream_t s);
+void launch_build_batch(const SysPtrs *reps, int n_reps, int max_n, long long sweep_offset, cudaStream_t s);
 void launch_move_pass_batch(const SysPtrs *reps, int n_reps, int cap, int pass, int group, int grid_x,
                             cudaStream_t s);
 void launch_advance_batch(const SysPtrs *reps, int n_reps, int n_sweeps, cudaStream_t s);

@@ -16,96 +16,11 @@
 // clearly beyond the cutoff.
 #include <cooperative_groups.h>
 
-#include "engine.cuh"
+#include "cellview.cuh"
 
 namespace cg = cooperative_groups;
 
 namespace hsmc {
-
-struct Stencil {
-  int k[3];  // half-width in cells per axis; -1 means every cell of the axis
-};
-
-struct CellView {
-  const int *cnt;
-  const Slot *slot;
-  int cap;
-  int nc[3];
-  float sh[3], L32[3], iw[3];
-};
-
-__device__ __forceinline__ CellView current_view(const SysPtrs &p) {
-  CellView v;
-  const DevState *st = p.st;
-  const Box *bx = p.box;
-  const int layout = (int)(st->params.sweep & 1ull);
-  v.cnt = p.cnt[layout];
-  v.slot = p.slot[layout];
-  v.cap = p.cap;
-  for (int d = 0; d < 3; d++) {
-    v.nc[d] = bx->nc[d];
-    v.sh[d] = st->params.shift32[d];
-    v.L32[d] = bx->len32[d];
-    v.iw[d] = bx->inv_w32[d];
-  }
-  return v;
-}
-
-// Visit every particle in the stencil of the cell holding (x, y, z).
-template <class F>
-__device__ __forceinline__ void for_each_near(const CellView &v, const Stencil &s, double x, double y, double z,
-                                              F &&visit) {
-  int ci[3];
-  float t;
-  axis_cell(__double2float_rn(x), v.sh[0], v.L32[0], v.iw[0], v.nc[0], ci[0], t);
-  axis_cell(__double2float_rn(y), v.sh[1], v.L32[1], v.iw[1], v.nc[1], ci[1], t);
-  axis_cell(__double2float_rn(z), v.sh[2], v.L32[2], v.iw[2], v.nc[2], ci[2], t);
-  int lo[3], span[3];
-  for (int d = 0; d < 3; d++) {
-    if (s.k[d] < 0) {
-      lo[d] = 0;
-      span[d] = v.nc[d];
-    } else {
-      lo[d] = ci[d] - s.k[d];
-      span[d] = 2 * s.k[d] + 1;
-    }
-  }
-  for (int a = 0; a < span[2]; a++) {
-    int cz = lo[2] + a;
-    cz = (cz % v.nc[2] + v.nc[2]) % v.nc[2];
-    for (int b = 0; b < span[1]; b++) {
-      int cy = lo[1] + b;
-      cy = (cy % v.nc[1] + v.nc[1]) % v.nc[1];
-      for (int e = 0; e < span[0]; e++) {
-        int cx = lo[0] + e;
-        cx = (cx % v.nc[0] + v.nc[0]) % v.nc[0];
-        const int c = cx + v.nc[0] * (cy + v.nc[1] * cz);
-        const int m = v.cnt[c];
-        const int n = m < v.cap ? m : v.cap;  // an overfull cell was flagged by the build
-        const Slot *sl = v.slot + (size_t)c * v.cap;
-        for (int q = 0; q < n; q++) visit(sl[q]);
-      }
-    }
-  }
-}
-
-// Grid coordinates of a point (the slots hold particles this way).
-__device__ __forceinline__ void grid_coords(const CellView &v, double x, double y, double z, float &tx, float &ty,
-                                            float &tz) {
-  int ci;
-  axis_cell(__double2float_rn(x), v.sh[0], v.L32[0], v.iw[0], v.nc[0], ci, tx);
-  axis_cell(__double2float_rn(y), v.sh[1], v.L32[1], v.iw[1], v.nc[1], ci, ty);
-  axis_cell(__double2float_rn(z), v.sh[2], v.L32[2], v.iw[2], v.nc[2], ci, tz);
-}
-
-// Single-precision squared minimum-image distance, for discarding far pairs.
-__device__ __forceinline__ float approx_r2(float ax, float ay, float az, const Slot &o, const float *L32) {
-  float dx = ax - o.x, dy = ay - o.y, dz = az - o.z;
-  dx -= L32[0] * rintf(dx / L32[0]);
-  dy -= L32[1] * rintf(dy / L32[1]);
-  dz -= L32[2] * rintf(dz / L32[2]);
-  return dx * dx + dy * dy + dz * dz;
-}
 
 // ------------------------------------------------------------ pair counts
 constexpr int HIST_SMEM_BINS = 4096;
@@ -232,26 +147,6 @@ void launch_scaled_scan(const SysPtrs &p, const double *sf, int n_sf, int stenci
 }
 
 // ----------------------------------------------------------------- Widom
-// widom_rand_pos (src/compute_widom_chem_pot.c:73-80): x = u * L with u the
-// reference's closed uniform; widom_compute_dist (:130-160): insertion minus
-// particle, one minimum-image branch, overlap when r < 1.
-__device__ __forceinline__ bool point_overlaps(const CellView &v, const SysPtrs &p, const Stencil &s, double x,
-                                               double y, double z, int skip, const double *len,
-                                               const double *half) {
-  float x32, y32, z32;  // grid coordinates, as the slots hold them
-  grid_coords(v, x, y, z, x32, y32, z32);
-  bool ov = false;
-  for_each_near(v, s, x, y, z, [&](const Slot &o) {
-    if (ov || o.id == skip) return;
-    const float r2 = approx_r2(x32, y32, z32, o, v.L32);
-    if (r2 > 1.01f) return;
-    double ox, oy, oz;
-    load_xyz(p.pos, o.id, ox, oy, oz);
-    if (ref_r2(x, y, z, ox, oy, oz, len, half) < 1.0) ov = true;
-  });
-  return ov;
-}
-
 __global__ void __launch_bounds__(256) k_widom(SysPtrs p, long long n, unsigned long long seq, const double *pos_in,
                                                uint8_t *ov_out) {
   const CellView v = current_view(p);

@@ -68,48 +68,15 @@ __global__ void __launch_bounds__(256) k_build(SysPtrs p1, const SysPtrs *reps, 
   axis_cell(y32, sh1, bx->len32[1], bx->inv_w32[1], bx->nc[1], cy, ty);
   axis_cell(z32, sh2, bx->len32[2], bx->inv_w32[2], bx->nc[2], cz, tz);
   const int c = cx + bx->nc[0] * (cy + bx->nc[1] * cz);
-  const int k = atomicAdd(p.cnt[layout] + c, 1);
+  const int k = atomicAdd(cnt_of(p, layout) + c, 1);
   if (k < p.cap) {
-    p.slot[layout][(size_t)c * p.cap + k] = Slot{tx, ty, tz, i};
+    slot_of(p, layout)[(size_t)c * p.cap + k] = Slot{tx, ty, tz, i};
   } else {
     atomicOr(&p.st->status, ST_CELL_OVERFLOW);
   }
-
 }
 
 __global__ void k_advance(DevState *st, int n) { st->sweep_base += (unsigned long long)n; }
-
-// After a build: list the non-empty cells of each colour by occupancy, so a
-// move pass can hand cells of equal occupancy (equal trial counts) to the
-// lanes of one warp and start the fullest cells first.  Appends are counted
-// per block in shared memory and claimed with one global atomic per
-// (colour, occupancy) per block.
-template <bool BATCH>
-__global__ void __launch_bounds__(256) k_classify(SysPtrs p1, const SysPtrs *reps) {
-  const SysPtrs p = BATCH ? reps[blockIdx.y] : p1;
-  __shared__ int s_cnt[8 * NBUCKET], s_base[8 * NBUCKET];
-  const int layout = (int)(p.st->params.sweep & 1ull);
-  const Box *bx = p.box;
-  const int ncell = bx->ncell;
-  for (int q = threadIdx.x; q < 8 * NBUCKET; q += blockDim.x) s_cnt[q] = 0;
-  __syncthreads();
-  const int c = blockIdx.x * blockDim.x + threadIdx.x;
-  int key = -1, local = 0;
-  if (c < ncell) {
-    const int n = p.cnt[layout][c];
-    if (n > 0) {
-      const int ix = c % bx->nc[0], iyz = c / bx->nc[0], iy = iyz % bx->nc[1], iz = iyz / bx->nc[1];
-      key = cell_colour(ix, iy, iz) * NBUCKET + (n < NBUCKET - 1 ? n : NBUCKET - 1);
-      local = atomicAdd(&s_cnt[key], 1);
-    }
-  }
-  __syncthreads();
-  for (int q = threadIdx.x; q < 8 * NBUCKET; q += blockDim.x)
-    if (s_cnt[q] > 0) s_base[q] = atomicAdd(&p.st->list_len[layout][q / NBUCKET][q % NBUCKET], s_cnt[q]);
-  __syncthreads();
-  if (key >= 0) p.list[layout][(size_t)key * (p.ncell_alloc / 8) + s_base[key] + local] = c;
-}
-
 
 // ------------------------------------------------------------ volume move
 // vol_move (src/moves.c:83-153) as four launches so it stays on the device:
@@ -146,8 +113,8 @@ __global__ void __launch_bounds__(256) k_vol_scan(SysPtrs p) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= p.n) return;
   const int layout = (int)(st->params.sweep & 1ull);
-  const int *cnt = p.cnt[layout];
-  const Slot *slot = p.slot[layout];
+  const int *cnt = cnt_of(p, layout);
+  const Slot *slot = slot_of(p, layout);
   const double len[3] = {bx->len[0], bx->len[1], bx->len[2]};
   const float L32[3] = {bx->len32[0], bx->len32[1], bx->len32[2]};
   const float iw[3] = {bx->inv_w32[0], bx->inv_w32[1], bx->inv_w32[2]};
@@ -266,15 +233,11 @@ void launch_build(const SysPtrs &p, long long sweep_offset, int num_sms, cudaStr
   (void)num_sms;
   const int blocks = (p.n + 255) / 256;
   k_build<false><<<blocks > 0 ? blocks : 1, 256, 0, s>>>(p, nullptr, sweep_offset);
-  k_classify<false><<<(p.ncell_alloc + 255) / 256, 256, 0, s>>>(p, nullptr);
 }
 
-void launch_build_batch(const SysPtrs *reps, int n_reps, int max_n, int max_ncell, long long sweep_offset,
-                        cudaStream_t s) {
+void launch_build_batch(const SysPtrs *reps, int n_reps, int max_n, long long sweep_offset, cudaStream_t s) {
   const dim3 grid((unsigned)((max_n + 255) / 256), (unsigned)n_reps);
   k_build<true><<<grid, 256, 0, s>>>(SysPtrs{}, reps, sweep_offset);
-  const dim3 cgrid((unsigned)((max_ncell + 255) / 256), (unsigned)n_reps);
-  k_classify<true><<<cgrid, 256, 0, s>>>(SysPtrs{}, reps);
 }
 
 __global__ void k_advance_batch(const SysPtrs *reps, int n_reps, int n) {

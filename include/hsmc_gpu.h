@@ -60,7 +60,8 @@ typedef struct {
   uint64_t seed;        /* random stream key (keyword "seed") */
   int cell_capacity;    /* particles per device cell; 0 chooses from the cell size */
   int lanes_per_cell;   /* GPU lanes sharing one active cell in a move pass: 1, 2, 4 or 8;
-                           0 picks the default */
+                           0 picks the default; 1 is refused for 32-slot cells (its
+                           shared memory does not fit a block) */
   int reserved[6];
 } hsmc_params;
 
