@@ -38,6 +38,10 @@ N = 4 * CELLS**3
 SWEEPS_PER_STEP = 100
 TARGET_ACC = 0.40
 B_MOVE = 24.0 * (2.0 + 27.0 * RHO)  # algorithmic bytes per trial move
+# DRAM bytes (read + write) of one k_move_pass launch on this workload, from an
+# ncu capture of this bench command (cache-flushed replay, so a cold-cache
+# upper bound; in the timed graph the working set stays in L2).
+MOVE_PASS_DRAM_BYTES = 31.65e6 + 256.0
 METRIC = "trial moves/s @N=256k rho=0.85"
 
 
@@ -281,7 +285,6 @@ def run_gpu_arm(args):
     moves_per_launch = N / 8.0  # one colour pass visits an eighth of the cells: N/8 trial moves on average
     kern_avg_ms = kern_ms / kern_n if kern_n else float("nan")
     achieved = B_MOVE * moves_per_launch / (kern_avg_ms * 1e-3) / 1e9
-    traffic = os.environ.get("HSMC_TRAFFIC_PER_LAUNCH")
     launches_per_step = SWEEPS_PER_STEP * 9 + math.ceil(SWEEPS_PER_STEP / 8)
     line = {
         "metric": METRIC, "value": value, "unit": "trial moves/s", "n_gpus": world, "steps": args.steps,
@@ -294,7 +297,8 @@ def run_gpu_arm(args):
                    "lanes_per_cell": lanes,
                    "l2": "flushed between steps (256 MB write)", "parallelism": f"replicas x{world}"},
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
-                     "frac": achieved / peak, "traffic": float(traffic) if traffic else None,
+                     "frac": achieved / peak, "traffic": MOVE_PASS_DRAM_BYTES,
+                     "traffic_kind": "ncu dram__bytes_read.sum + dram__bytes_write.sum per launch, cold cache",
                      "kernel": "k_move_pass", "bytes_per_move": B_MOVE, "moves_per_launch": moves_per_launch,
                      "avg_launch_ms": kern_avg_ms, "peak_kind": peak_kind},
         "e2e": {"value": e2e_val, "unit": "trial moves/s", "h2d_bytes_per_step": N * 32,
@@ -312,6 +316,164 @@ def run_gpu_arm(args):
     return 0
 
 
+# ------------------------------------------------- secondary workloads
+# Measurements of the other configurations; each prints one JSON line of its
+# own.  The default workload above is the headline.
+
+def run_replicas(args):
+    """512 independent NVT replicas (n ~ U{6..20} FCC cells per side, rho ~
+    U[0.30, 0.94]) advanced together by the batched engine; per-replica
+    dr_max tuned toward 40% acceptance; contact pressure per replica against
+    Carnahan-Starling."""
+    import numpy as np
+    from hsmc_gb300.batch import ReplicaBatch, carnahan_starling, contact_z
+
+    rng = np.random.default_rng(2024)
+    reps = args.replicas
+    ns = rng.integers(6, 21, reps)
+    rhos = rng.uniform(0.30, 0.94, reps)
+    systems = [(float(r), int(n), 0.1, 1000 + k) for k, (r, n) in enumerate(zip(rhos, ns))]
+    b = ReplicaBatch(systems)
+    n_tot = int(sum(b.n))
+    dr, acc = b.tune_steps(0.1, target=TARGET_ACC)
+    b.sweeps(args.equil)
+    sweeps = args.sweeps
+    per = 10
+    nb, bin_ = 5, 0.01
+    rmax = 1.0 + nb * bin_
+    blocks = 10
+    samples = sweeps // per
+    cnt = np.zeros((blocks, reps, nb))
+    t_gpu = 0.0
+    moves = 0
+    for k in range(samples):
+        c = b.sweeps(per)
+        t_gpu += b.last_timing()
+        moves += int(c[:, 0].sum())
+        cnt[k * blocks // samples] += b.pressv_counts(bin_, rmax, nb)
+    per_block = samples // blocks
+    z = np.array([[contact_z(cnt[j, i], per_block, b.n[i], rhos[i], bin_) for i in range(reps)]
+                  for j in range(blocks)])
+    zm = z.mean(axis=0)
+    se = z.std(axis=0, ddof=1) / np.sqrt(blocks)
+    zcs = np.array([carnahan_starling(r) for r in rhos])
+    dev = (zm - zcs) / se
+    fluid = rhos < 0.90
+    line = {
+        "metric": "trial moves/s, 512 batched replicas", "value": moves / (t_gpu * 1e-3), "unit": "trial moves/s",
+        "n_gpus": 1, "higher_is_better": True, "dtype": "f64", "data": "synthetic (FCC lattice starts)",
+        "config": {"workload": f"{reps} NVT replicas, n~U{{6..20}} (N 864..32000), rho~U[0.30,0.94], "
+                               f"{sweeps} sweeps after {args.equil}", "n_particles_total": n_tot,
+                   "acceptance_min_max": [float(acc.min()), float(acc.max())]},
+        "gpu_ms": t_gpu,
+        "pressure": {"within_3se_of_cs": float(np.mean(np.abs(dev) < 3)),
+                     "within_3se_of_cs_rho_below_0.90": float(np.mean(np.abs(dev[fluid]) < 3)),
+                     "median_abs_rel_dev": float(np.median(np.abs(zm - zcs) / zcs)),
+                     "worst": {"rho": float(rhos[np.argmax(np.abs(dev))]), "z": float(zm[np.argmax(np.abs(dev))]),
+                               "z_cs": float(zcs[np.argmax(np.abs(dev))]),
+                               "se": float(se[np.argmax(np.abs(dev))])}},
+    }
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+def run_widom(args):
+    """Learned versus uniform Widom at rho = 0.94, N = 110,592 (fluid):
+    self-training on 10^7 insertion outcomes, then 10^6 insertions per
+    sample for each estimator; efficiency = 1 / (variance per insertion x
+    device time per insertion), reported as the learned / uniform ratio."""
+    import numpy as np
+    from hsmc_gb300 import HardSphereSystem
+    from hsmc_gb300.lwidom import LearnedWidom
+
+    # a 30^3 face-centred start stays crystalline at rho = 0.94 for > 10^4
+    # sweeps; the fluid is melted from a simple-cubic lattice of about the
+    # same size (48^3 = 110,592 spheres)
+    s = HardSphereSystem(rho=0.94, cells=48, lattice_type=1, dr_max=0.05, seed=77)
+    s.sweep_nvt(3000)
+    dr, acc = tune_dr(s, dr0=0.08)
+    s.sweep_nvt(args.equil)
+    lw = LearnedWidom(s, 0.5, seed=78, train_capacity=10_000_000)
+    lw.use_prior()
+    log = lw.fit()
+    train_ms = sum(r[3] for r in log)
+    ins = 1_000_000
+    sw = sw2 = 0.0
+    t_l = t_u = 0.0
+    n_l = n_u = 0
+    ok_u = 0
+    per_sample = []
+    for _ in range(args.samples):
+        s.sweep_nvt(20)
+        t_l += lw.refresh()
+        st = lw.insert(ins, alpha=0.1)
+        t_l += lw.last_ms()
+        sw += st.sum_w
+        sw2 += st.sum_w2
+        n_l += st.n
+        per_sample.append(st.sum_w / st.n)
+        ok_u += lw.uniform(ins)
+        t_u += lw.last_ms()
+        n_u += ins
+    p = sw / n_l
+    var_l = sw2 / n_l - p * p
+    var_u = p * (1 - p)  # Bernoulli variance of uniform Widom at the same p
+    eff_l = 1.0 / (var_l * t_l / n_l)
+    eff_u = 1.0 / (var_u * t_u / n_u)
+    se_mu_l = math.sqrt(var_l / n_l) / p
+    se_mu_u = math.sqrt(var_u / n_u) / p
+    line = {
+        "metric": "mu_ex std-err per GPU-s, learned vs uniform @N=110592 rho=0.94", "value": eff_l / eff_u,
+        "unit": "x (efficiency ratio: uniform time / learned time at equal std-err)", "higher_is_better": True,
+        "n_gpus": 1, "dtype": "bf16 tensor-core MLP, f64 overlap test", "data": "synthetic (FCC start)",
+        "config": {"workload": "NVT rho=0.94 fluid N=110592 (melted 48^3 SC), sub-cells of edge >= 0.5, "
+                               "MLP 27-64-64-1, "
+                               "q = 0.9 learned + 0.1 uniform", "samples": args.samples,
+                   "insertions_per_sample": ins, "dr_max": dr, "acceptance": acc},
+        "learned": {"p_ins": p, "beta_mu_ex": -math.log(p), "var_per_insertion": var_l, "gpu_ms": t_l,
+                    "se_beta_mu": se_mu_l, "sample_sd": float(np.std(per_sample, ddof=1) / p)},
+        "uniform": {"successes": ok_u, "insertions": n_u, "var_per_insertion_at_p": var_u, "gpu_ms": t_u,
+                    "se_beta_mu_at_p": se_mu_u},
+        "training": {"kept_outcomes": int(log[-1][0]), "kept_successes": int(log[-1][1]),
+                     "insertions_examined": 8 * 125_000_000, "gpu_ms": train_ms},
+        "beta_mu_cs": (lambda e: (8 * e - 9 * e * e + 3 * e**3) / (1 - e) ** 3)(math.pi * 0.94 / 6),
+    }
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+def run_npt(args):
+    """NpT crystal: N = 1,048,576 (64^3 FCC) at beta P = 11, dv_max = 0.001,
+    one volume move per sweep; trial moves/s, density, q6 and the g(r) peak."""
+    import numpy as np
+    from hsmc_gb300 import HardSphereSystem
+
+    s = HardSphereSystem(rho=1.04, cells=64, dr_max=0.05, dv_max=0.001, pressure=11.0, seed=91)
+    s.sweep_npt(args.equil)
+    rho = []
+    t = 0.0
+    moves = 0
+    for _ in range(args.sweeps // 50):
+        c = s.sweep_npt(50)
+        t += s.last_timing()[0]
+        moves += int(c[0])
+        box = s.get_box()
+        rho.append(s.n / (box[0] * box[1] * box[2]))
+    q6 = s.global_ql(6, 1.5)
+    nb = 100
+    g = s.compute_rdf_counts(0.005, 1.0 + nb * 0.005, nb)
+    line = {
+        "metric": "trial moves/s, NpT N=1048576 betaP=11", "value": moves / (t * 1e-3), "unit": "trial moves/s",
+        "n_gpus": 1, "higher_is_better": True, "dtype": "f64", "data": "synthetic (FCC start)",
+        "config": {"workload": "NpT 64^3 FCC, beta P 11, dv_max 0.001, one volume move per sweep",
+                   "sweeps": args.sweeps, "equil": args.equil},
+        "rho_mean": float(np.mean(rho)), "rho_sd": float(np.std(rho)), "q6": float(q6),
+        "rdf_peak_bin": int(np.argmax(g)), "gpu_ms": t,
+    }
+    print(json.dumps(line), flush=True)
+    return 0
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -319,11 +481,22 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--workload", default="fluid", choices=["fluid", "replicas", "widom", "npt"])
+    ap.add_argument("--replicas", type=int, default=512)
+    ap.add_argument("--sweeps", type=int, default=5000)
+    ap.add_argument("--equil", type=int, default=500)
+    ap.add_argument("--samples", type=int, default=20)
     args = ap.parse_args()
     if args.warmup < 3 and args.impl == "gb300" and args.steps > 2:
         args.warmup = 3
     if args.impl == "reference":
         return run_reference_arm(args)
+    if args.workload == "replicas":
+        return run_replicas(args)
+    if args.workload == "widom":
+        return run_widom(args)
+    if args.workload == "npt":
+        return run_npt(args)
     return run_gpu_arm(args)
 
 

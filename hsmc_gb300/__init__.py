@@ -6,7 +6,7 @@ The product is the C ABI in ``include/hsmc_gpu.h`` implemented by
 built from ``host/``.  This Python package is a thin ctypes front-end over the
 same ABI, for tests, analysis and benchmarks.
 """
-from .system import HardSphereSystem, HsmcError, box_from_lattice, lattice_config  # noqa: F401
+from .system import HardSphereSystem, HsmcError, box_from_lattice, compress_to, lattice_config  # noqa: F401
 from . import _native  # noqa: F401
 
-__all__ = ["HardSphereSystem", "HsmcError", "box_from_lattice", "lattice_config"]
+__all__ = ["HardSphereSystem", "HsmcError", "box_from_lattice", "compress_to", "lattice_config"]

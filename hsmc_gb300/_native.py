@@ -51,7 +51,7 @@ def declared_symbols() -> list[str]:
     """Every entry point include/hsmc_gpu.h declares."""
     text = open(HEADER).read()
     text = re.sub(r"/\*.*?\*/", "", text, flags=re.S)
-    return sorted(set(re.findall(r"\b(hsmc_gpu_\w+)\s*\(", text)))
+    return sorted(set(re.findall(r"\b(hsmc_[a-z0-9_]+)\s*\(", text)))
 
 
 _lib = None

@@ -97,10 +97,60 @@ class ReplicaBatch:
         _check(self._lib.hsmc_batch_pressv(self._h, dr, rmax, nbins, out.ctypes.data), "hsmc_batch_pressv")
         return out
 
+    def tune_steps(self, dr0, target: float = 0.4, sweeps: int = 20, rounds: int = 8, melt: int = 50):
+        """Per-replica secant search of dr_max toward the target acceptance
+        (the reference's optimiser, src/optimizer.c:23-64, run on every
+        replica at once).  Returns (dr, acceptance) arrays."""
+        d1 = np.broadcast_to(np.asarray(dr0, dtype=np.float64), (self.reps,)).copy()
+
+        def acc(d):
+            self.set_steps(d)
+            c = self.sweeps(sweeps).astype(np.float64)
+            return c[:, 1] / c[:, 0]
+
+        self.set_steps(d1)
+        self.sweeps(melt)
+        a1 = acc(d1)
+        d2 = np.where(a1 > target, d1 * 2, d1 / 2)
+        a2 = acc(d2)
+        for _ in range(rounds):
+            moving = a2 != a1
+            if not moving.any():
+                break
+            d = np.where(moving, d2 - (a2 - target) * (d2 - d1) / np.where(moving, a2 - a1, 1.0), d2)
+            d = np.minimum(np.maximum(np.abs(d), 1e-3), 1.0)
+            d1, a1 = d2, a2
+            d2 = d
+            a2 = acc(d2)
+        self.set_steps(d2)
+        self.dr = d2
+        return d2, a2
+
     def last_timing(self):
         t = C.c_double()
         _check(self._lib.hsmc_batch_last_timing(self._h, C.byref(t)), "hsmc_batch_last_timing")
         return t.value
 
 
-__all__ = ["ReplicaBatch", "HsmcError"]
+def contact_z(counts, samples: int, n: int, rho: float, dr: float):
+    """Compressibility factor from the virial contact histogram, as the
+    reference's analysis does (compute_pressv, src/compute_press.c:277-307;
+    fit in python/hsmc_pressure.py): counts of ordered pairs with r in
+    [1 + k dr, 1 + (k+1) dr), normalised to g(r) at the bin centres, a linear
+    fit extrapolated to r = 1, Z = 1 + (2 pi / 3) rho g(1)."""
+    counts = np.asarray(counts, dtype=np.float64)
+    nb = counts.shape[-1]
+    r = 1.0 + (np.arange(nb) + 0.5) * dr
+    shell = 4.0 * np.pi / 3.0 * ((r + dr / 2) ** 3 - (r - dr / 2) ** 3)
+    g = counts / (samples * shell * rho * n)
+    b1, b0 = np.polyfit(r, g, 1)
+    return 1.0 + 2.0 * np.pi / 3.0 * rho * (b0 + b1)
+
+
+def carnahan_starling(rho: float) -> float:
+    """Z_CS = (1 + eta + eta^2 - eta^3) / (1 - eta)^3 (coeff_vw, src/analytic.c:112)."""
+    eta = np.pi * rho / 6.0
+    return (1 + eta + eta**2 - eta**3) / (1 - eta) ** 3
+
+
+__all__ = ["ReplicaBatch", "HsmcError", "contact_z", "carnahan_starling"]

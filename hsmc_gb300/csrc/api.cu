@@ -71,6 +71,16 @@ struct hsmc_ctx {
 
 // ----------------------------------------------------------------- helpers
 
+int hsmc::ctx_view(hsmc_ctx *ctx, CtxView *out) {
+  if (!ctx || !out) return HSMC_ERR_INVALID_ARG;
+  out->sp = ctx->sp;
+  out->box = ctx->hbox;
+  out->stream = ctx->stream;
+  out->num_sms = ctx->num_sms;
+  out->uploaded = ctx->uploaded;
+  return HSMC_OK;
+}
+
 static int cuda_status(cudaError_t e) {
   if (e == cudaSuccess) return HSMC_OK;
   fprintf(stderr, "hsmc_gpu: CUDA error %s\n", cudaGetErrorString(e));

@@ -6,6 +6,8 @@
 
 #include "common.cuh"
 
+struct hsmc_ctx;
+
 namespace hsmc {
 
 // Pointers every kernel of one system needs.  All are device addresses that
@@ -27,6 +29,16 @@ struct SysPtrs {
 // struct by a runtime value would copy it to local memory.
 __device__ __forceinline__ int *cnt_of(const SysPtrs &p, int layout) { return layout ? p.cnt[1] : p.cnt[0]; }
 __device__ __forceinline__ Slot *slot_of(const SysPtrs &p, int layout) { return layout ? p.slot[1] : p.slot[0]; }
+
+// api.cu: what other parts of the library see of a context
+struct CtxView {
+  SysPtrs sp;
+  Box box;              // host copy of the current box
+  cudaStream_t stream;  // the context's stream; calls are synchronous on it
+  int num_sms;
+  bool uploaded;        // a configuration is on the device and laid out
+};
+int ctx_view(::hsmc_ctx *ctx, CtxView *out);
 
 // api.cu: device cell grid for a box (even count per axis, edge >= 1 + margin)
 int make_box(const double len[3], double rho, Box &b, int &cap);

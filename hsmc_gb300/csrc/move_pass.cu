@@ -140,7 +140,10 @@ __global__ void __launch_bounds__(128, PassSmem<G, CAP>::min_blocks)
     const int ix = 2 * ax + cx, iy = 2 * ay + cy, iz = 2 * az + cz;
     const int c = ix + nc[0] * (iy + nc[1] * iz);
 
-    // (1) counts of the cell and of this lane's neighbour cells, issued together
+    // (1) counts of the cell and of this lane's neighbour cells, issued
+    // together.  An interior cell (most of them) reaches its neighbours by a
+    // linear offset and sees no periodic image.
+    const bool interior = ix > 0 && iy > 0 && iz > 0 && ix < nc[0] - 1 && iy < nc[1] - 1 && iz < nc[2] - 1;
     int nb_c[NB], nb_n[NB];
 #pragma unroll
     for (int q = 0; q < NB; q++) {
@@ -148,11 +151,16 @@ __global__ void __launch_bounds__(128, PassSmem<G, CAP>::min_blocks)
       nb_c[q] = c;
       if (o26 < 26) {
         const unsigned code = c_nbr[o26];
-        int x = ix + (int)(code & 3u) - 1, y = iy + (int)((code >> 2) & 3u) - 1, z = iz + (int)(code >> 4) - 1;
-        x += x < 0 ? nc[0] : (x >= nc[0] ? -nc[0] : 0);
-        y += y < 0 ? nc[1] : (y >= nc[1] ? -nc[1] : 0);
-        z += z < 0 ? nc[2] : (z >= nc[2] ? -nc[2] : 0);
-        nb_c[q] = x + nc[0] * (y + nc[1] * z);
+        const int ox = (int)(code & 3u) - 1, oy = (int)((code >> 2) & 3u) - 1, oz = (int)(code >> 4) - 1;
+        if (interior) {
+          nb_c[q] = c + ox + nc[0] * (oy + nc[1] * oz);
+        } else {
+          int x = ix + ox, y = iy + oy, z = iz + oz;
+          x += x < 0 ? nc[0] : (x >= nc[0] ? -nc[0] : 0);
+          y += y < 0 ? nc[1] : (y >= nc[1] ? -nc[1] : 0);
+          z += z < 0 ? nc[2] : (z >= nc[2] ? -nc[2] : 0);
+          nb_c[q] = x + nc[0] * (y + nc[1] * z);
+        }
       }
     }
     const int n = cnt[c];
@@ -191,8 +199,10 @@ __global__ void __launch_bounds__(128, PassSmem<G, CAP>::min_blocks)
       }
     }
     for (int j = lane; j < n; j += G) cp_async16(&own_t[j * GPB + gl], slot + (size_t)c * CAP + j);
+    // the first trial's draws, computed while the copies are in flight
+    U32x4 r_next = draw4(seed, rep << 8, (uint32_t)c, seq, TAG_MOVE);
     cp_async_wait_all();
-    if (!direct) {  // periodic images of the entries this lane copied
+    if (!direct && !interior) {  // periodic images of the entries this lane copied
       int e = first;
 #pragma unroll
       for (int q = 0; q < NB; q++) {
@@ -230,7 +240,8 @@ __global__ void __launch_bounds__(128, PassSmem<G, CAP>::min_blocks)
     const int rows = (!direct && total > lane) ? (total - lane + G - 1) / G : 0;
     unsigned moved = 0;
     for (int trial = 0; trial < n; trial++) {
-      const U32x4 r = draw4(seed, (rep << 8) | (uint32_t)trial, (uint32_t)c, seq, TAG_MOVE);
+      const U32x4 r = r_next;
+      if (trial + 1 < n) r_next = draw4(seed, (rep << 8) | (uint32_t)(trial + 1), (uint32_t)c, seq, TAG_MOVE);
       const int s = (int)__umulhi(r.x, (unsigned)n);  // rank of the moving particle
       const int js = order[s * GPB + gl] & (CAP - 1);  // a slot index below CAP
       const double nx = propose_axis(own_x[js * GPB + gl], centred_offset(r.y), dr, len[0]);

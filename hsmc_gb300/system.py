@@ -278,3 +278,41 @@ class HardSphereSystem:
         k = C.c_int()
         _check(self._lib.hsmc_gpu_last_timing(self._h, C.byref(t), C.byref(m), C.byref(k)), "hsmc_gpu_last_timing")
         return t.value, m.value, k.value
+
+
+def compress_to(system: HardSphereSystem, rho_target: float, sweeps: int = 20, dr_max: float | None = None,
+                max_rounds: int = 5000) -> HardSphereSystem:
+    """Prepare a dense fluid (a preparation step of this package; the
+    reference starts only from lattices): alternate `sweeps` NVT sweeps with
+    an affine compression of the box by 90% of the largest scale factor that
+    the reference's FP64 scaled-overlap scan (vol_move, src/moves.c:104-112)
+    accepts, never past rho_target, until rho_target is reached exactly.
+    Each compression uploads the scaled configuration into a new context;
+    the old one is closed.  Returns the system at rho_target."""
+    s = system
+    for _ in range(max_rounds):
+        if s.rho >= rho_target:
+            return s
+        s.sweep_nvt(sweeps)
+        sf_t = (s.rho / rho_target) ** (1.0 / 3.0)
+        if not s.scan_overlap(sf_t):
+            sf = sf_t
+        else:
+            lo, hi = sf_t, 1.0  # overlap at lo, none at hi
+            for _ in range(20):
+                mid = 0.5 * (lo + hi)
+                if s.scan_overlap(mid):
+                    lo = mid
+                else:
+                    hi = mid
+            sf = 1.0 - 0.9 * (1.0 - hi)
+        conf = s.download()
+        conf[:, 1:] *= sf
+        box = tuple(b * sf for b in s.box)
+        rho = rho_target if sf == sf_t else s.n / (box[0] * box[1] * box[2])
+        step = dr_max if dr_max is not None else s.dr_max
+        new = HardSphereSystem(rho=rho, cells=s.cells, lattice_type=s.lattice_type, dr_max=step, dv_max=s.dv_max,
+                               seed=int(s.rng_state()[0]) + 1, conf=conf, box=box)
+        s.close()
+        s = new
+    raise HsmcError(1, "compress_to: target density not reached")

@@ -231,6 +231,77 @@ int hsmc_gpu_autotune(hsmc_ctx *ctx, int sweeps_per_variant, int *lanes_out);
 int hsmc_gpu_set_profiling(hsmc_ctx *ctx, int on);
 int hsmc_gpu_last_timing(hsmc_ctx *ctx, double *total_ms, double *move_kernel_ms, int *move_launches);
 
+/* ------------------------------------------------------------------------
+ * Learned Widom proposal: an importance-sampled form of compute_mu
+ * (src/compute_widom_chem_pot.c:32-182); no counterpart in the reference.
+ *
+ * Insertion points are drawn from q(x) = alpha / V + (1 - alpha) q_L(x):
+ * q_L picks a sub-cell (edge >= subcell_edge, at most 1/sqrt(3) so that a
+ * sub-cell holds at most one sphere) with probability proportional to
+ * pi_c = sqrt(sigmoid(z_c)) and a point uniformly inside it, where z_c is
+ * the output of an MLP 27 -> 64 -> 64 -> 1 (BF16 tensor-core products, FP32
+ * accumulation) on the 27 occupancy bits of the sub-cell's 3x3x3
+ * neighbourhood.  Each point carries w = 1 / (V q(x)); the mean of
+ * w * [no overlap] estimates the insertion probability without bias, and
+ * beta mu_ex = -ln of it.  The overlap test is the reference's FP64 test.
+ * The network is trained on insertion outcomes the sampler itself collects
+ * (pattern bits | success << 31), with weighted binary cross-entropy and
+ * Adam.  All calls are synchronous on the context's stream. */
+typedef struct hsmc_lwidom hsmc_lwidom;
+
+#define HSMC_LWIDOM_NPARAMS 6273 /* W1[64][32] (column 27 = bias), W2[64][64], b2[64], w3[64], b3 */
+
+typedef struct {
+  double sum_w;       /* sum of w over successful insertions */
+  double sum_w2;      /* sum of w^2 over successful insertions */
+  uint64_t n;         /* insertions */
+  uint64_t n_ok;      /* successful insertions */
+  uint64_t n_learned; /* insertions drawn from the learned component */
+} hsmc_lwidom_stats;
+
+/* train_capacity: outcomes the training buffer holds (0 = none). */
+int hsmc_lwidom_create(hsmc_ctx *ctx, double subcell_edge, uint64_t seed, int64_t train_capacity,
+                       hsmc_lwidom **out);
+void hsmc_lwidom_destroy(hsmc_lwidom *lw);
+int hsmc_lwidom_set_params(hsmc_lwidom *lw, const float *params); /* also resets Adam */
+int hsmc_lwidom_get_params(hsmc_lwidom *lw, float *params);
+int hsmc_lwidom_subgrid(hsmc_lwidom *lw, int ns[3]);
+/* Occupancy, patterns, logits and the proposal CDF for the context's
+ * current configuration; required before insertions on it. */
+int hsmc_lwidom_refresh(hsmc_lwidom *lw);
+int hsmc_lwidom_patterns(hsmc_lwidom *lw, uint32_t *out, int64_t n_subcells);
+int hsmc_lwidom_proposal(hsmc_lwidom *lw, double *pi, double *cdf, int64_t n_subcells);
+/* Network output for given patterns (replaces the refreshed logits). */
+int hsmc_lwidom_logits(hsmc_lwidom *lw, const uint32_t *patterns, int64_t n, float *logits);
+/* Gradient of the mean weighted loss over samples (pattern | label << 31),
+ * weight w_pos for label 1 and w_neg for label 0; *loss = the mean loss. */
+int hsmc_lwidom_grad(hsmc_lwidom *lw, const uint32_t *samples, int64_t n, float w_pos, float w_neg, float *grad,
+                     double *loss);
+/* One Adam step (b1 0.9, b2 0.999, eps 1e-8) with the given gradient. */
+int hsmc_lwidom_adam_step(hsmc_lwidom *lw, const float *grad, float lr);
+/* n insertions with mixture weight alpha in (0, 1].  keep_failures >= 0
+ * appends outcomes to the training buffer while it has room: every success,
+ * and each failure with probability keep_failures (an independent draw), so
+ * failures are trained with weight 1 / keep_failures; < 0 collects nothing.
+ * Collected outcomes land in the buffer in atomic-claim order. */
+int hsmc_lwidom_insert(hsmc_lwidom *lw, int64_t n, double alpha, double keep_failures, hsmc_lwidom_stats *st);
+/* The same, returning every point, its learned sub-cell (-1 for a uniform
+ * draw), branch, weight and outcome. */
+int hsmc_lwidom_insert_traced(hsmc_lwidom *lw, int64_t n, double alpha, double *points, int32_t *subcell,
+                              uint8_t *uniform, double *weight, uint8_t *ok, hsmc_lwidom_stats *st);
+/* Plain uniform Widom (the reference's estimator) through the same overlap
+ * test and timing; *accepted = successful insertions. */
+int hsmc_lwidom_uniform(hsmc_lwidom *lw, int64_t n, uint64_t *accepted);
+/* Minibatch Adam over the collected outcomes, loss weight w_pos for
+ * successes and w_neg for failures; *last_loss = mean weighted loss of the
+ * last minibatch. */
+int hsmc_lwidom_train(hsmc_lwidom *lw, int epochs, int64_t batch, float lr, float w_pos, float w_neg,
+                      double *last_loss);
+int hsmc_lwidom_samples(hsmc_lwidom *lw, int64_t *n, int64_t *n_pos);
+int hsmc_lwidom_clear_samples(hsmc_lwidom *lw);
+/* Device time of the last refresh, insert, uniform or train call (ms). */
+int hsmc_lwidom_last_timing(hsmc_lwidom *lw, double *ms);
+
 #ifdef __cplusplus
 }
 #endif
