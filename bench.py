@@ -38,10 +38,10 @@ N = 4 * CELLS**3
 SWEEPS_PER_STEP = 100
 TARGET_ACC = 0.40
 B_MOVE = 24.0 * (2.0 + 27.0 * RHO)  # algorithmic bytes per trial move
-# DRAM bytes (read + write) of one k_move_pass launch on this workload, from an
-# ncu capture of this bench command (cache-flushed replay, so a cold-cache
-# upper bound; in the timed graph the working set stays in L2).
-MOVE_PASS_DRAM_BYTES = 31.65e6 + 256.0
+# DRAM bytes (read + write) of one launch of the move kernels on this
+# workload, from ncu captures of this bench command (cache-flushed replay, so
+# cold-cache upper bounds; in the timed graph the working set stays in L2).
+MOVE_DRAM_BYTES = {"k_move_pass": 31.65e6 + 256.0, "k_move_flow": None}
 METRIC = "trial moves/s @N=256k rho=0.85"
 
 
@@ -106,6 +106,21 @@ class ClockSampler:
                     reasons.add(name)
         return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(smax) if smax else None,
                 "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def reduce_over_ranks(moves, total_ms, e2e_moves, e2e_s, world, device):
+    """Whole-job figures: the moves of every rank over the slowest rank's
+    time, for the device-timed region and for the end-to-end loop."""
+    if world > 1:
+        import torch
+
+        work = torch.tensor([float(moves), float(e2e_moves)], dtype=torch.float64, device=device)
+        times = torch.tensor([float(total_ms), float(e2e_s)], dtype=torch.float64, device=device)
+        torch.distributed.all_reduce(work)
+        torch.distributed.all_reduce(times, op=torch.distributed.ReduceOp.MAX)
+        moves, e2e_moves = float(work[0]), float(work[1])
+        total_ms, e2e_s = float(times[0]), float(times[1])
+    return moves / (total_ms * 1e-3), e2e_moves / e2e_s, total_ms
 
 
 def tune_dr(sysm, dr0=0.12, sweeps=20, rounds=8):
@@ -217,7 +232,8 @@ def run_gpu_arm(args):
 
     sysm = hsmc_gb300.HardSphereSystem(rho=RHO, cells=CELLS, dr_max=0.12, seed=2026 + rank)
     dr, acc = tune_dr(sysm)
-    lanes = sysm.autotune(5)
+    lanes = sysm.autotune(8)
+    schedule, _ = sysm.get_schedule()  # 1: dataflow sweep (one launch), 0: one launch per colour pass
     # The reference restarts from the lattice after optimising (src/nvt.c:58-62).
     sysm.upload(hsmc_gb300.lattice_config(RHO, (CELLS,) * 3))
     sysm.set_step(dr)
@@ -272,20 +288,18 @@ def run_gpu_arm(args):
     barrier()
     e2e_s = time.perf_counter() - t0
 
-    value = moves / (total_ms * 1e-3)
-    e2e_val = e2e_steps * SWEEPS_PER_STEP * N / e2e_s
-    if world > 1:
-        t = torch.tensor([value, e2e_val], dtype=torch.float64, device="cuda")
-        ms = torch.tensor([total_ms], dtype=torch.float64, device="cuda")
-        torch.distributed.all_reduce(t)
-        torch.distributed.all_reduce(ms, op=torch.distributed.ReduceOp.MAX)
-        value, e2e_val = float(t[0]), float(t[1])
-        total_ms = float(ms[0])
+    value, e2e_val, total_ms = reduce_over_ranks(moves, total_ms, e2e_steps * SWEEPS_PER_STEP * N, e2e_s, world,
+                                                 "cuda")
     peak, peak_kind = peaks()
-    moves_per_launch = N / 8.0  # one colour pass visits an eighth of the cells: N/8 trial moves on average
+    # a dataflow launch makes a whole sweep (N trial moves); a colour pass
+    # visits an eighth of the cells (N/8 trial moves on average)
+    moves_per_launch = float(N) if schedule == 1 else N / 8.0
+    kernel = "k_move_flow" if schedule == 1 else "k_move_pass"
     kern_avg_ms = kern_ms / kern_n if kern_n else float("nan")
     achieved = B_MOVE * moves_per_launch / (kern_avg_ms * 1e-3) / 1e9
-    launches_per_step = SWEEPS_PER_STEP * 9 + math.ceil(SWEEPS_PER_STEP / 8)
+    per_sweep = 2 if schedule == 1 else 9  # build + move launches
+    launches_per_step = SWEEPS_PER_STEP * per_sweep + math.ceil(SWEEPS_PER_STEP / 8)
+    traffic = MOVE_DRAM_BYTES.get(kernel)
     line = {
         "metric": METRIC, "value": value, "unit": "trial moves/s", "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": total_ms / args.steps, "higher_is_better": True,
@@ -295,11 +309,12 @@ def run_gpu_arm(args):
                                "checkerboard sweeps", "n_particles": N, "rho": RHO,
                    "sweeps_per_step": SWEEPS_PER_STEP, "dr_max": dr, "acceptance": acc_moves / max(moves, 1),
                    "lanes_per_cell": lanes,
+                   "schedule": "dataflow (8 passes per launch)" if schedule == 1 else "one launch per pass",
                    "l2": "flushed between steps (256 MB write)", "parallelism": f"replicas x{world}"},
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
-                     "frac": achieved / peak, "traffic": MOVE_PASS_DRAM_BYTES,
+                     "frac": achieved / peak, "traffic": traffic,
                      "traffic_kind": "ncu dram__bytes_read.sum + dram__bytes_write.sum per launch, cold cache",
-                     "kernel": "k_move_pass", "bytes_per_move": B_MOVE, "moves_per_launch": moves_per_launch,
+                     "kernel": kernel, "bytes_per_move": B_MOVE, "moves_per_launch": moves_per_launch,
                      "avg_launch_ms": kern_avg_ms, "peak_kind": peak_kind},
         "e2e": {"value": e2e_val, "unit": "trial moves/s", "h2d_bytes_per_step": N * 32,
                 "d2h_bytes_per_step": N * 32 + 6 * 8 + 4 * 8},

@@ -67,9 +67,22 @@ struct hsmc_ctx {
   double last_total_ms = 0.0, last_move_ms = 0.0;
   int last_move_launches = 0;
   Scratch hist, qbuf, flags, qpos, qids, trace;
+  // dataflow schedule: one cooperative launch per sweep, progress words per
+  // 2x2x2 region; `flow_graph` records whether such launches capture
+  bool flow = false;
+  int flow_grid = 0;
+  int flow_graph = -1;  // -1 untested, 0 no, 1 yes
+  uint32_t *prog = nullptr;
 };
 
 // ----------------------------------------------------------------- helpers
+
+// Progress words of the dataflow schedule: "every pass of the sweep before
+// sweep_base is done", written whenever the sweep index is set.
+static void reset_progress(hsmc_ctx *ctx) {
+  launch_fill_u32(ctx->prog, ctx->sp.ncell_alloc / 8 + 1, (uint32_t)(ctx->sweep_base * 8ull), ctx->stream);
+}
+
 
 int hsmc::ctx_view(hsmc_ctx *ctx, CtxView *out) {
   if (!ctx || !out) return HSMC_ERR_INVALID_ARG;
@@ -99,6 +112,7 @@ static int status_to_code(int st) {
   if (st & ST_OUT_OF_BOX) return HSMC_ERR_OUT_OF_BOX;
   if (st & ST_TRACE_FULL) return HSMC_ERR_INVALID_ARG;
   if (st & ST_BAD_CELL) return HSMC_ERR_CELL_OVERFLOW;
+  if (st & ST_FLOW_TIMEOUT) return HSMC_ERR_TIMEOUT;
   return HSMC_OK;
 }
 
@@ -271,6 +285,9 @@ int hsmc_gpu_create(const hsmc_params *prm, hsmc_ctx **out) {
   if ((ce = cudaEventCreate(&ctx->ev_start)) != cudaSuccess) return fail(ce);
   if ((ce = cudaEventCreate(&ctx->ev_stop)) != cudaSuccess) return fail(ce);
   ctx->pass_grid = move_pass_grid(ctx->group, cap, sp.ncell_alloc, ctx->num_sms);
+  if ((ce = cudaMalloc(&ctx->prog, sizeof(uint32_t) * (size_t)(sp.ncell_alloc / 8 + 1))) != cudaSuccess)
+    return fail(ce);
+  ctx->flow = false;  // one launch per pass unless hsmc_gpu_set_schedule or the autotuner picks the dataflow sweep
   *out = ctx;
   return HSMC_OK;
 }
@@ -288,6 +305,7 @@ void hsmc_gpu_destroy(hsmc_ctx *ctx) {
   }
   cudaFree(sp.box);
   cudaFree(sp.st);
+  cudaFree(ctx->prog);
   ctx->hist.release();
   ctx->qbuf.release();
   ctx->flags.release();
@@ -317,6 +335,7 @@ int hsmc_gpu_upload_config(hsmc_ctx *ctx, const double (*conf)[4], int n) {
     HSMC_CUDA(cudaMemsetAsync(sp.cnt[l], 0, sizeof(int) * (size_t)sp.ncell_alloc, ctx->stream));
   HSMC_CUDA(cudaMemsetAsync(&sp.st->status, 0, sizeof(int), ctx->stream));
   launch_build(sp, -1, ctx->num_sms, ctx->stream);
+  reset_progress(ctx);
   int e = check_kernels(ctx);
   if (e) return e;
   DevState s;
@@ -361,10 +380,19 @@ int hsmc_gpu_last_timing(hsmc_ctx *ctx, double *total_ms, double *move_kernel_ms
   return HSMC_OK;
 }
 
-static void enqueue_sweep(hsmc_ctx *ctx, long long offset, bool trace, bool npt) {
-  launch_build(ctx->sp, offset, ctx->num_sms, ctx->stream);
+// The eight passes of one sweep: one dataflow launch, or eight launches with
+// a kernel boundary after each colour.
+static cudaError_t enqueue_moves(hsmc_ctx *ctx, bool trace) {
+  if (ctx->flow) return launch_move_flow(ctx->sp, ctx->prog, ctx->group, trace, ctx->flow_grid, ctx->stream);
   for (int k = 0; k < 8; k++) launch_move_pass(ctx->sp, k, ctx->group, trace, ctx->pass_grid, ctx->stream);
+  return cudaSuccess;
+}
+
+static cudaError_t enqueue_sweep(hsmc_ctx *ctx, long long offset, bool trace, bool npt) {
+  launch_build(ctx->sp, offset, ctx->num_sms, ctx->stream);
+  cudaError_t e = enqueue_moves(ctx, trace);
   if (npt) launch_volume_move(ctx->sp, offset, ctx->margin, ctx->stream);
+  return e;
 }
 
 static int ensure_graph(hsmc_ctx *ctx, bool npt) {
@@ -372,16 +400,31 @@ static int ensure_graph(hsmc_ctx *ctx, bool npt) {
   if (exec) return HSMC_OK;
   cudaGraph_t g = nullptr;
   HSMC_CUDA(cudaStreamBeginCapture(ctx->stream, cudaStreamCaptureModeThreadLocal));
-  for (int s = 0; s < kGraphSweeps; s++) enqueue_sweep(ctx, s, false, npt);
+  cudaError_t le = cudaSuccess;
+  for (int s = 0; s < kGraphSweeps && le == cudaSuccess; s++) le = enqueue_sweep(ctx, s, false, npt);
   launch_advance(ctx->sp, kGraphSweeps, ctx->stream);
   cudaError_t e = cudaStreamEndCapture(ctx->stream, &g);
-  if (e != cudaSuccess) return cuda_status(e);
+  if (le != cudaSuccess || e != cudaSuccess) {
+    if (g) cudaGraphDestroy(g);
+    cudaGetLastError();
+    if (ctx->flow) {  // cooperative launches do not capture here: launch sweeps directly
+      ctx->flow_graph = 0;
+      return HSMC_OK;
+    }
+    return cuda_status(le != cudaSuccess ? le : e);
+  }
   e = cudaGraphInstantiate(&exec, g, 0);
   cudaGraphDestroy(g);
   if (e != cudaSuccess) {
     exec = nullptr;
+    cudaGetLastError();
+    if (ctx->flow) {
+      ctx->flow_graph = 0;
+      return HSMC_OK;
+    }
     return cuda_status(e);
   }
+  if (ctx->flow) ctx->flow_graph = 1;
   return HSMC_OK;
 }
 
@@ -400,10 +443,11 @@ static int run_sweeps(hsmc_ctx *ctx, int n_sweeps, bool trace, bool npt, uint64_
   HSMC_CUDA(cudaMemsetAsync(&ctx->sp.st->status, 0, sizeof(int), ctx->stream));
   ctx->last_move_ms = 0.0;
   ctx->last_move_launches = 0;
-  const bool direct = trace || ctx->profiling;
+  bool direct = trace || ctx->profiling;
   if (!direct) {
     int e = ensure_graph(ctx, npt);
     if (e) return e;
+    if (ctx->flow && ctx->flow_graph == 0) direct = true;
   }
   const bool timing = ctx->profiling && !trace;
   if (timing) {
@@ -423,12 +467,19 @@ static int run_sweeps(hsmc_ctx *ctx, int n_sweeps, bool trace, bool npt, uint64_
     }
   }
   const int rest = n_sweeps - done;
+  const int per_sweep = ctx->flow ? 1 : 8;  // move-kernel launches per sweep
   for (int s = 0; s < rest; s++) {
     launch_build(ctx->sp, s, ctx->num_sms, ctx->stream);
-    for (int k = 0; k < 8; k++) {
-      if (timing) HSMC_CUDA(cudaEventRecord(ctx->ev_pass[16 * s + 2 * k], ctx->stream));
-      launch_move_pass(ctx->sp, k, ctx->group, trace, ctx->pass_grid, ctx->stream);
-      if (timing) HSMC_CUDA(cudaEventRecord(ctx->ev_pass[16 * s + 2 * k + 1], ctx->stream));
+    if (ctx->flow) {
+      if (timing) HSMC_CUDA(cudaEventRecord(ctx->ev_pass[16 * s], ctx->stream));
+      HSMC_CUDA(launch_move_flow(ctx->sp, ctx->prog, ctx->group, trace, ctx->flow_grid, ctx->stream));
+      if (timing) HSMC_CUDA(cudaEventRecord(ctx->ev_pass[16 * s + 1], ctx->stream));
+    } else {
+      for (int k = 0; k < 8; k++) {
+        if (timing) HSMC_CUDA(cudaEventRecord(ctx->ev_pass[16 * s + 2 * k], ctx->stream));
+        launch_move_pass(ctx->sp, k, ctx->group, trace, ctx->pass_grid, ctx->stream);
+        if (timing) HSMC_CUDA(cudaEventRecord(ctx->ev_pass[16 * s + 2 * k + 1], ctx->stream));
+      }
     }
     if (npt) launch_volume_move(ctx->sp, s, ctx->margin, ctx->stream);
   }
@@ -444,13 +495,13 @@ static int run_sweeps(hsmc_ctx *ctx, int n_sweeps, bool trace, bool npt, uint64_
   if (timing) {
     double sum = 0.0;
     for (int s = 0; s < rest; s++)
-      for (int k = 0; k < 8; k++) {
+      for (int k = 0; k < per_sweep; k++) {
         float t = 0.f;
         HSMC_CUDA(cudaEventElapsedTime(&t, ctx->ev_pass[16 * s + 2 * k], ctx->ev_pass[16 * s + 2 * k + 1]));
         sum += t;
       }
     ctx->last_move_ms = sum;
-    ctx->last_move_launches = 8 * rest;
+    ctx->last_move_launches = per_sweep * rest;
   }
   DevState s;
   if ((e = read_state(ctx, s))) return e;
@@ -470,35 +521,74 @@ static int run_sweeps(hsmc_ctx *ctx, int n_sweeps, bool trace, bool npt, uint64_
   return HSMC_OK;
 }
 
+static void drop_graphs(hsmc_ctx *ctx) {
+  if (ctx->graph) cudaGraphExecDestroy(ctx->graph);
+  if (ctx->graph_npt) cudaGraphExecDestroy(ctx->graph_npt);
+  ctx->graph = ctx->graph_npt = nullptr;
+}
+
+// Lanes per cell and schedule; the grids follow.  Returns false when the
+// combination cannot run on this device.
+static bool apply_schedule(hsmc_ctx *ctx, int flow, int group) {
+  if (!move_pass_fits(group, ctx->sp.cap)) return false;
+  int fg = 0;
+  if (flow) {
+    int dev = 0, coop = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&coop, cudaDevAttrCooperativeLaunch, dev);
+    if (!coop) return false;
+    fg = move_flow_grid(group, ctx->sp.cap, ctx->sp.ncell_alloc, ctx->num_sms);
+    if (fg <= 0) return false;
+  }
+  ctx->group = group;
+  ctx->flow = flow != 0;
+  ctx->flow_grid = fg;
+  ctx->pass_grid = move_pass_grid(group, ctx->sp.cap, ctx->sp.ncell_alloc, ctx->num_sms);
+  ctx->flow_graph = -1;
+  drop_graphs(ctx);
+  return true;
+}
+
 int hsmc_gpu_autotune(hsmc_ctx *ctx, int sweeps_per_variant, int *lanes_out) {
   if (!ctx || sweeps_per_variant <= 0 || !ctx->uploaded) return HSMC_ERR_INVALID_ARG;
   const int options[4] = {1, 2, 4, 8};
   const bool was_profiling = ctx->profiling;
   const bool npt = ctx->prm.pressure > 0;
-  ctx->profiling = true;
-  int best = ctx->group;
+  const int sweeps = ((sweeps_per_variant + kGraphSweeps - 1) / kGraphSweeps) * kGraphSweeps;
+  ctx->profiling = false;  // time the production path: graphs of sweeps
+  int best_g = ctx->group, best_f = ctx->flow ? 1 : 0;
   double best_ms = 1e300;
-  for (int v = 0; v < 4; v++) {
-    if (!move_pass_fits(options[v], ctx->sp.cap)) continue;
-    ctx->group = options[v];
-    ctx->pass_grid = move_pass_grid(ctx->group, ctx->sp.cap, ctx->sp.ncell_alloc, ctx->num_sms);
-    int e = run_sweeps(ctx, sweeps_per_variant, false, npt, nullptr);
-    if (e) {
-      ctx->profiling = was_profiling;
-      return e;
+  for (int f = 1; f >= 0; f--)
+    for (int v = 0; v < 4; v++) {
+      if (!apply_schedule(ctx, f, options[v])) continue;
+      int e = run_sweeps(ctx, sweeps, false, npt, nullptr);
+      if (e) {
+        ctx->profiling = was_profiling;
+        return e;
+      }
+      if (ctx->last_total_ms < best_ms) {
+        best_ms = ctx->last_total_ms;
+        best_g = options[v];
+        best_f = f;
+      }
     }
-    if (ctx->last_move_ms < best_ms) {
-      best_ms = ctx->last_move_ms;
-      best = options[v];
-    }
-  }
   ctx->profiling = was_profiling;
-  ctx->group = best;
-  ctx->pass_grid = move_pass_grid(ctx->group, ctx->sp.cap, ctx->sp.ncell_alloc, ctx->num_sms);
-  if (ctx->graph) cudaGraphExecDestroy(ctx->graph);
-  if (ctx->graph_npt) cudaGraphExecDestroy(ctx->graph_npt);
-  ctx->graph = ctx->graph_npt = nullptr;
-  if (lanes_out) *lanes_out = best;
+  apply_schedule(ctx, best_f, best_g);
+  if (lanes_out) *lanes_out = best_g;
+  return HSMC_OK;
+}
+
+int hsmc_gpu_set_schedule(hsmc_ctx *ctx, int schedule, int lanes_per_cell) {
+  if (!ctx || (schedule != 0 && schedule != 1)) return HSMC_ERR_INVALID_ARG;
+  const int g = lanes_per_cell == 0 ? ctx->group : lanes_per_cell;
+  if (g != 1 && g != 2 && g != 4 && g != 8) return HSMC_ERR_INVALID_ARG;
+  return apply_schedule(ctx, schedule, g) ? HSMC_OK : HSMC_ERR_INVALID_ARG;
+}
+
+int hsmc_gpu_get_schedule(hsmc_ctx *ctx, int *schedule, int *lanes_per_cell) {
+  if (!ctx) return HSMC_ERR_INVALID_ARG;
+  if (schedule) *schedule = ctx->flow ? 1 : 0;
+  if (lanes_per_cell) *lanes_per_cell = ctx->group;
   return HSMC_OK;
 }
 
@@ -776,6 +866,7 @@ int hsmc_gpu_rng_set_state(hsmc_ctx *ctx, const uint64_t st[4]) {
   ctx->widom_seq = st[2];
   HSMC_CUDA(cudaMemcpyAsync(&ctx->sp.st->seed, &st[0], sizeof(uint64_t), cudaMemcpyHostToDevice, ctx->stream));
   HSMC_CUDA(cudaMemcpyAsync(&ctx->sp.st->sweep_base, &st[1], sizeof(uint64_t), cudaMemcpyHostToDevice, ctx->stream));
+  reset_progress(ctx);
   if (ctx->uploaded) {
     // The layout a sweep writes follows the parity of its index: rebuild the
     // current one for the new position in the stream.

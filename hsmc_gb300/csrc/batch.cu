@@ -44,6 +44,9 @@ struct hsmc_batch {
   int cap = 8;
   int group = kBatchLanes;
   int max_n = 0, max_ncell = 0;
+  int tot_n = 0, tot_groups = 0;   // particles and active cells (one colour) of all replicas
+  long long tot_cell = 0;
+  int *d_nstart = nullptr, *d_gstart = nullptr;  // their prefix sums by replica (n_reps + 1)
   cudaStream_t stream = nullptr;
   std::vector<hsmc_params> prm;
   std::vector<SysPtrs> sp;  // host copies of the device table
@@ -84,6 +87,8 @@ void hsmc_batch_destroy(hsmc_batch *b) {
   if (b->stream) cudaStreamSynchronize(b->stream);
   if (b->graph) cudaGraphExecDestroy(b->graph);
   cudaFree(b->d_reps);
+  cudaFree(b->d_nstart);
+  cudaFree(b->d_gstart);
   cudaFree(b->pos);
   for (int l = 0; l < 2; l++) {
     cudaFree(b->cnt[l]);
@@ -192,6 +197,28 @@ int hsmc_batch_create(const hsmc_params *params, int n_systems, hsmc_batch **out
   if ((ce = cudaMemcpy(b->d_reps, b->sp.data(), sizeof(SysPtrs) * n_systems, cudaMemcpyHostToDevice)) !=
       cudaSuccess)
     return fail(ce);
+  // flat launches: prefix sums of particles and of active cells per replica
+  {
+    std::vector<int> ns(n_systems + 1, 0), gs(n_systems + 1, 0);
+    long long tn = 0, tg = 0;
+    for (int k = 0; k < n_systems; k++) {
+      ns[k] = (int)tn;
+      gs[k] = (int)tg;
+      tn += params[k].n_particles;
+      tg += (long long)b->hbox[k].ncell / 8;
+    }
+    if (tn > 0x7fffffffll || tg * 8 > 0x7fffffffll) return fail(cudaErrorInvalidValue);
+    ns[n_systems] = (int)tn;
+    gs[n_systems] = (int)tg;
+    b->tot_n = (int)tn;
+    b->tot_groups = (int)tg;
+    b->tot_cell = (long long)oc;
+    if ((ce = cudaMalloc(&b->d_nstart, sizeof(int) * (n_systems + 1))) != cudaSuccess) return fail(ce);
+    if ((ce = cudaMalloc(&b->d_gstart, sizeof(int) * (n_systems + 1))) != cudaSuccess) return fail(ce);
+    if ((ce = cudaMemcpy(b->d_nstart, ns.data(), sizeof(int) * (n_systems + 1), cudaMemcpyHostToDevice)) ||
+        (ce = cudaMemcpy(b->d_gstart, gs.data(), sizeof(int) * (n_systems + 1), cudaMemcpyHostToDevice)))
+      return fail(ce);
+  }
   if ((ce = cudaEventCreate(&b->ev0)) != cudaSuccess) return fail(ce);
   if ((ce = cudaEventCreate(&b->ev1)) != cudaSuccess) return fail(ce);
   *out = b;
@@ -240,20 +267,21 @@ int hsmc_batch_set_steps(hsmc_batch *b, const double *dr_max) {
   return HSMC_OK;
 }
 
-static void enqueue_batch_sweep(hsmc_batch *b, long long offset, int grid_x) {
-  launch_build_batch(b->d_reps, b->reps, b->max_n, offset, b->stream);
-  for (int k = 0; k < 8; k++) launch_move_pass_batch(b->d_reps, b->reps, b->cap, k, b->group, grid_x, b->stream);
+static void enqueue_batch_sweep(hsmc_batch *b, long long offset) {
+  launch_build_batch(b->d_reps, b->d_nstart, b->reps, b->tot_n, offset, b->stream);
+  for (int k = 0; k < 8; k++)
+    launch_move_pass_batch(b->d_reps, b->d_gstart, b->reps, b->tot_groups, b->cap, k, b->group, b->cnt[0], b->cnt[1],
+                           b->tot_cell, b->stream);
 }
 
 int hsmc_batch_sweeps(hsmc_batch *b, int n_sweeps, uint64_t *counters) {
   if (!b || n_sweeps < 0) return HSMC_ERR_INVALID_ARG;
   for (int k = 0; k < b->reps; k++)
     if (!b->uploaded[k]) return HSMC_ERR_INVALID_ARG;
-  const int grid_x = move_pass_grid_batch(b->group, b->max_ncell);
   if (!b->graph) {
     cudaGraph_t g = nullptr;
     BATCH_CUDA(cudaStreamBeginCapture(b->stream, cudaStreamCaptureModeThreadLocal));
-    for (int s = 0; s < kBatchGraphSweeps; s++) enqueue_batch_sweep(b, s, grid_x);
+    for (int s = 0; s < kBatchGraphSweeps; s++) enqueue_batch_sweep(b, s);
     launch_advance_batch(b->d_reps, b->reps, kBatchGraphSweeps, b->stream);
     cudaError_t e = cudaStreamEndCapture(b->stream, &g);
     if (e != cudaSuccess) return cuda_fail(e);
@@ -275,7 +303,7 @@ int hsmc_batch_sweeps(hsmc_batch *b, int n_sweeps, uint64_t *counters) {
     done += kBatchGraphSweeps;
   }
   const int rest = n_sweeps - done;
-  for (int s = 0; s < rest; s++) enqueue_batch_sweep(b, s, grid_x);
+  for (int s = 0; s < rest; s++) enqueue_batch_sweep(b, s);
   if (rest > 0) launch_advance_batch(b->d_reps, b->reps, rest, b->stream);
   BATCH_CUDA(cudaEventRecord(b->ev1, b->stream));
   int e = batch_check(b);

@@ -178,6 +178,7 @@ enum : int {
   ST_OUT_OF_BOX = 4,
   ST_TRACE_FULL = 8,
   ST_BAD_CELL = 16,
+  ST_FLOW_TIMEOUT = 32,  // a dataflow wait gave up (the sweep's result is invalid)
 };
 
 struct DevState {

@@ -25,6 +25,18 @@ struct SysPtrs {
   int ncell_alloc;     // cells allocated per layout
 };
 
+// The replica holding flat index x, for batched launches over all replicas:
+// the last r with start[r] <= x (start has n + 1 ascending entries).
+__device__ __forceinline__ int find_rep(const int *start, int n, int x) {
+  int lo = 0, hi = n - 1;
+  while (lo < hi) {
+    const int mid = (lo + hi + 1) >> 1;
+    if (__ldg(start + mid) <= x) lo = mid;
+    else hi = mid - 1;
+  }
+  return lo;
+}
+
 // The arrays of one layout.  A select, not an index: indexing the parameter
 // struct by a runtime value would copy it to local memory.
 __device__ __forceinline__ int *cnt_of(const SysPtrs &p, int layout) { return layout ? p.cnt[1] : p.cnt[0]; }
@@ -47,18 +59,25 @@ int make_box(const double len[3], double rho, Box &b, int &cap);
 void launch_build(const SysPtrs &p, long long sweep_offset, int num_sms, cudaStream_t s);
 void launch_move_pass(const SysPtrs &p, int pass, int group, bool trace, int grid, cudaStream_t s);
 void launch_advance(const SysPtrs &p, int n_sweeps, cudaStream_t s);
+void launch_fill_u32(uint32_t *p, int n, uint32_t v, cudaStream_t s);
 void launch_volume_move(const SysPtrs &p, long long sweep_offset, double margin, cudaStream_t s);
 void launch_volume_scan(const SysPtrs &p, cudaStream_t s);
 int move_pass_grid(int group, int cap, int ncell_alloc, int num_sms);
 bool move_pass_fits(int group, int cap);  // its shared memory fits a block on this device
 void prepare_move_pass();                 // allow each variant its shared memory (current device)
+// dataflow sweep (all eight passes, cooperative launch); prog holds one
+// progress word per 2x2x2 region (ncell_alloc / 8)
+int move_flow_grid(int group, int cap, int ncell_alloc, int num_sms);
+cudaError_t launch_move_flow(const SysPtrs &p, uint32_t *prog, int group, bool trace, int grid, cudaStream_t s);
 
 // batched replicas: reps is a device array of n_reps SysPtrs
-void launch_build_batch(const SysPtrs *reps, int n_reps, int max_n, long long sweep_offset, cudaStream_t s);
-void launch_move_pass_batch(const SysPtrs *reps, int n_reps, int cap, int pass, int group, int grid_x,
-                            cudaStream_t s);
+// nstart / gstart: prefix sums over replicas of particles / active cells
+// (cells of one colour); launches cover all of them in one flat grid.
+void launch_build_batch(const SysPtrs *reps, const int *nstart, int n_reps, int tot_n, long long sweep_offset,
+                        cudaStream_t s);
+void launch_move_pass_batch(const SysPtrs *reps, const int *gstart, int n_reps, int tot_groups, int cap, int pass,
+                            int group, int *cnt_pool0, int *cnt_pool1, long long pool_cells, cudaStream_t s);
 void launch_advance_batch(const SysPtrs *reps, int n_reps, int n_sweeps, cudaStream_t s);
-int move_pass_grid_batch(int group, int max_ncell);
 void launch_pair_hist_batch(const SysPtrs *reps, int n_reps, int max_n, double bin, double rmax, int nbins,
                             unsigned long long *counts, cudaStream_t s);
 

@@ -23,13 +23,20 @@ namespace hsmc {
 // ------------------------------------------------------------------ build
 // Bins every particle into the layout of sweep s = sweep_base + offset.
 // Thread 0 also publishes that sweep's shift and colour order.
-// In a batch (BATCH), blockIdx.y is the replica and its pointers come from
-// reps; the replica index enters every random counter, so replica 0 draws
-// what a single system draws.
+// In a batch (BATCH), the grid covers every replica's particles (nstart:
+// their prefix sums) and each thread finds its replica; the replica index
+// enters every random counter, so replica 0 draws what a single system draws.
 template <bool BATCH>
-__global__ void __launch_bounds__(256) k_build(SysPtrs p1, const SysPtrs *reps, long long offset) {
-  const SysPtrs p = BATCH ? reps[blockIdx.y] : p1;
-  const uint32_t rep = BATCH ? blockIdx.y : 0u;
+__global__ void __launch_bounds__(256) k_build(SysPtrs p1, const SysPtrs *reps, const int *nstart, int n_reps,
+                                               long long offset) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  uint32_t rep = 0u;
+  if (BATCH) {
+    if (i >= __ldg(nstart + n_reps)) return;
+    rep = (uint32_t)find_rep(nstart, n_reps, i);
+    i -= __ldg(nstart + rep);
+  }
+  const SysPtrs p = BATCH ? reps[rep] : p1;
   const DevState *st = p.st;
   const Box *bx = p.box;
   const unsigned long long s = st->sweep_base + (unsigned long long)offset;
@@ -40,7 +47,6 @@ __global__ void __launch_bounds__(256) k_build(SysPtrs p1, const SysPtrs *reps, 
   const float sh1 = __fmul_rn(__uint2float_rn(rs.y >> 8) * 5.9604644775390625e-08f, w1);
   const float sh2 = __fmul_rn(__uint2float_rn(rs.z >> 8) * 5.9604644775390625e-08f, w2);
   const int layout = (int)(s & 1ull);
-  const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i == 0) {
     DevState *ws = p.st;
     ws->params.sweep = s;
@@ -77,6 +83,16 @@ __global__ void __launch_bounds__(256) k_build(SysPtrs p1, const SysPtrs *reps, 
 }
 
 __global__ void k_advance(DevState *st, int n) { st->sweep_base += (unsigned long long)n; }
+
+__global__ void k_fill_u32(uint32_t *p, int n, uint32_t v) {
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) p[i] = v;
+}
+
+void launch_fill_u32(uint32_t *p, int n, uint32_t v, cudaStream_t s) {
+  int blocks = (n + 255) / 256;
+  if (blocks > 1024) blocks = 1024;
+  k_fill_u32<<<blocks > 0 ? blocks : 1, 256, 0, s>>>(p, n, v);
+}
 
 // ------------------------------------------------------------ volume move
 // vol_move (src/moves.c:83-153) as four launches so it stays on the device:
@@ -232,12 +248,12 @@ void launch_volume_move(const SysPtrs &p, long long sweep_offset, double margin,
 void launch_build(const SysPtrs &p, long long sweep_offset, int num_sms, cudaStream_t s) {
   (void)num_sms;
   const int blocks = (p.n + 255) / 256;
-  k_build<false><<<blocks > 0 ? blocks : 1, 256, 0, s>>>(p, nullptr, sweep_offset);
+  k_build<false><<<blocks > 0 ? blocks : 1, 256, 0, s>>>(p, nullptr, nullptr, 0, sweep_offset);
 }
 
-void launch_build_batch(const SysPtrs *reps, int n_reps, int max_n, long long sweep_offset, cudaStream_t s) {
-  const dim3 grid((unsigned)((max_n + 255) / 256), (unsigned)n_reps);
-  k_build<true><<<grid, 256, 0, s>>>(SysPtrs{}, reps, sweep_offset);
+void launch_build_batch(const SysPtrs *reps, const int *nstart, int n_reps, int tot_n, long long sweep_offset,
+                        cudaStream_t s) {
+  k_build<true><<<(tot_n + 255) / 256, 256, 0, s>>>(SysPtrs{}, reps, nstart, n_reps, sweep_offset);
 }
 
 __global__ void k_advance_batch(const SysPtrs *reps, int n_reps, int n) {

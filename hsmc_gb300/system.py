@@ -269,6 +269,15 @@ class HardSphereSystem:
         _check(self._lib.hsmc_gpu_autotune(self._h, sweeps_per_variant, C.byref(lanes)), "hsmc_gpu_autotune")
         return lanes.value
 
+    def set_schedule(self, schedule: int, lanes_per_cell: int = 0) -> None:
+        """0: one launch per colour pass; 1: dataflow sweep (same chain)."""
+        _check(self._lib.hsmc_gpu_set_schedule(self._h, schedule, lanes_per_cell), "hsmc_gpu_set_schedule")
+
+    def get_schedule(self):
+        sch, lanes = C.c_int(), C.c_int()
+        _check(self._lib.hsmc_gpu_get_schedule(self._h, C.byref(sch), C.byref(lanes)), "hsmc_gpu_get_schedule")
+        return sch.value, lanes.value
+
     def set_profiling(self, on: bool) -> None:
         _check(self._lib.hsmc_gpu_set_profiling(self._h, 1 if on else 0), "hsmc_gpu_set_profiling")
 

@@ -216,12 +216,21 @@ int hsmc_gpu_sweeps_traced(hsmc_ctx *ctx, int n_sweeps, uint32_t *rec, int64_t c
  * inv_w32[3] (float), capacity; for checking traced moves. */
 int hsmc_gpu_grid_info(hsmc_ctx *ctx, int nc[3], float len32[3], float inv_w32[3], int *capacity);
 
-/* Times the move pass for each lanes-per-cell mapping (1, 2, 4, 8) over
- * sweeps_per_variant sweeps each and keeps the fastest; *lanes_out receives
- * it.  The chain does not depend on the mapping (same random counters, exact
- * decisions), so these are ordinary sweeps of the run: the configuration
- * advances by 4 * sweeps_per_variant sweeps. */
+/* Times every schedule (below) with every lanes-per-cell mapping (1, 2, 4,
+ * 8) over sweeps_per_variant sweeps each (rounded up to a multiple of 8) and
+ * keeps the fastest; *lanes_out receives its mapping.  The chain depends on
+ * neither (same random counters, exact decisions), so these are ordinary
+ * sweeps of the run. */
 int hsmc_gpu_autotune(hsmc_ctx *ctx, int sweeps_per_variant, int *lanes_out);
+
+/* Schedule of the eight colour passes of a sweep: 0 = one launch per pass
+ * with a kernel boundary between passes (the default); 1 = dataflow, all
+ * eight passes in one cooperative launch where a cell waits only for the 26
+ * cells around it to finish the previous pass.  Both give the same chain;
+ * hsmc_gpu_autotune picks the faster.  lanes_per_cell 0 keeps the current
+ * mapping. */
+int hsmc_gpu_set_schedule(hsmc_ctx *ctx, int schedule, int lanes_per_cell);
+int hsmc_gpu_get_schedule(hsmc_ctx *ctx, int *schedule, int *lanes_per_cell);
 
 /* Timing of the last sweep call, from CUDA events on the context's stream:
  * total device time, and (only with profiling on) the summed time and count

@@ -180,3 +180,29 @@ def test_error_paths_report_reference_messages(gpu_lib):
     assert ei.value.code == 4
     g.upload(conf)
     g.sweep_nvt(2)
+
+
+@pytest.mark.parametrize("lanes", [1, 2, 4, 8])
+def test_dataflow_schedule_is_the_pass_barrier_chain(gpu_lib, lanes):
+    """All eight passes in one cooperative launch, each cell waiting only for
+    its neighbourhood, give the chain of one launch per pass bit for bit."""
+    confs = []
+    for schedule in (0, 1):
+        s = gpu_lib.HardSphereSystem(rho=0.8, cells=8, dr_max=0.15, seed=42)
+        s.set_schedule(schedule, lanes)
+        assert s.get_schedule() == (schedule, lanes)
+        c = s.sweep_nvt(27)
+        confs.append((s.download(), c))
+    assert np.array_equal(confs[0][0], confs[1][0])
+    assert np.array_equal(confs[0][1], confs[1][1])
+
+
+def test_dataflow_schedule_npt_matches(gpu_lib):
+    confs = []
+    for schedule in (0, 1):
+        s = gpu_lib.HardSphereSystem(rho=0.6, cells=6, dr_max=0.2, dv_max=0.01, pressure=5.0, seed=7)
+        s.set_schedule(schedule)
+        s.sweep_npt(24)
+        confs.append((s.download(), s.get_box()))
+    assert np.array_equal(confs[0][0], confs[1][0])
+    assert np.array_equal(confs[0][1], confs[1][1])
