@@ -457,13 +457,50 @@ def run_widom(args):
     return 0
 
 
+def opt_npt(s, part_target, vol_target, opt_sweeps=1000, opt_samples=10):
+    """The reference's NpT optimiser (opt_npt, src/optimizer.c:82-147): two
+    samples after doubling or halving, then secant steps on dr_max and (with
+    vol_target set) dv_max toward their acceptance targets, with its clamps.
+    vol_target None keeps dv_max."""
+    sample_iter = opt_sweeps // opt_samples
+
+    def sample():
+        c = s.sweep_npt(sample_iter).astype(float)
+        return s.dr_max, c[1] / c[0], s.dv_max, (c[4] / c[3] if c[3] else 0.0)
+
+    dr1, a1, dv1, v1 = sample()
+    tune_v = vol_target is not None
+    s.set_step(s.dr_max * 2 if a1 > part_target else s.dr_max / 2,
+               (s.dv_max * 2 if v1 > vol_target else s.dv_max / 2) if tune_v else s.dv_max)
+    dr2, a2, dv2, v2 = sample()
+    for _ in range(opt_samples):
+        dr = dr2 - (a2 - part_target) * (dr2 - dr1) / (a2 - a1) if a2 != a1 else dr2
+        dv = dv2 - (v2 - vol_target) * (dv2 - dv1) / (v2 - v1) if (tune_v and v2 != v1) else dv2
+        dr = min(dr, 1.0)
+        if dr <= 0.0:
+            dr = -dr
+            if dr > 1.0:
+                dr = dr2 / 2
+        if dv <= 0.0:
+            dv = -dv
+            if dv > 0.1:
+                dv = dv2 / 2
+        s.set_step(dr, dv)
+        dr1, a1, dv1, v1 = dr2, a2, dv2, v2
+        dr2, a2, dv2, v2 = sample()
+    return dr2, a2, dv2, v2
+
+
 def run_npt(args):
-    """NpT crystal: N = 1,048,576 (64^3 FCC) at beta P = 11, dv_max = 0.001,
-    one volume move per sweep; trial moves/s, density, q6 and the g(r) peak."""
+    """NpT crystal: N = 1,048,576 (64^3 FCC) at beta P = 11, dv_max = 0.001
+    (the configured maximum deformation), dr_max tuned toward 40 % by the
+    reference's optimiser, one volume move per sweep; trial moves/s, density,
+    q6 and the g(r) peak."""
     import numpy as np
     from hsmc_gb300 import HardSphereSystem
 
     s = HardSphereSystem(rho=1.04, cells=64, dr_max=0.05, dv_max=0.001, pressure=11.0, seed=91)
+    dr, acc, dv, vacc = opt_npt(s, TARGET_ACC, None)
     s.sweep_npt(args.equil)
     rho = []
     t = 0.0
@@ -480,8 +517,9 @@ def run_npt(args):
     line = {
         "metric": "trial moves/s, NpT N=1048576 betaP=11", "value": moves / (t * 1e-3), "unit": "trial moves/s",
         "n_gpus": 1, "higher_is_better": True, "dtype": "f64", "data": "synthetic (FCC start)",
-        "config": {"workload": "NpT 64^3 FCC, beta P 11, dv_max 0.001, one volume move per sweep",
-                   "sweeps": args.sweeps, "equil": args.equil},
+        "config": {"workload": "NpT 64^3 FCC, beta P 11, dv_max 0.001, dr_max tuned by the reference's optimiser, "
+                               "one volume move per sweep", "sweeps": args.sweeps, "equil": args.equil,
+                   "dr_max": dr, "acceptance": acc, "dv_max": dv, "volume_acceptance": vacc},
         "rho_mean": float(np.mean(rho)), "rho_sd": float(np.std(rho)), "q6": float(q6),
         "rdf_peak_bin": int(np.argmax(g)), "gpu_ms": t,
     }

@@ -17,7 +17,6 @@ using namespace hsmc;
 namespace {
 
 constexpr int kBatchGraphSweeps = 8;
-constexpr int kBatchLanes = 2;
 
 int cuda_fail(cudaError_t e) {
   fprintf(stderr, "hsmc_gpu: CUDA error %s\n", cudaGetErrorString(e));
@@ -41,8 +40,14 @@ int code_of(int st) {
 
 struct hsmc_batch {
   int reps = 0;
-  int cap = 8;
-  int group = kBatchLanes;
+  // replicas of one cell capacity move in one flat launch; lanes per cell
+  // grow with the capacity so a block's shared memory stays the same
+  struct CapClass {
+    int cap = 8, group = 2, n = 0, tot_groups = 0;
+    SysPtrs *d_reps = nullptr;
+    int *d_gstart = nullptr, *d_ids = nullptr;
+  };
+  std::vector<CapClass> classes;
   int max_n = 0, max_ncell = 0;
   int tot_n = 0, tot_groups = 0;   // particles and active cells (one colour) of all replicas
   long long tot_cell = 0;
@@ -89,6 +94,11 @@ void hsmc_batch_destroy(hsmc_batch *b) {
   cudaFree(b->d_reps);
   cudaFree(b->d_nstart);
   cudaFree(b->d_gstart);
+  for (auto &q : b->classes) {
+    cudaFree(q.d_reps);
+    cudaFree(q.d_ids);
+    cudaFree(q.d_gstart);
+  }
   cudaFree(b->pos);
   for (int l = 0; l < 2; l++) {
     cudaFree(b->cnt[l]);
@@ -118,7 +128,8 @@ int hsmc_batch_create(const hsmc_params *params, int n_systems, hsmc_batch **out
   b->sp.resize(n_systems);
   b->uploaded.assign(n_systems, 0);
   size_t tot_n = 0, tot_cell = 0;
-  int cap = 8;
+  std::vector<int> caps(n_systems, 8);
+  size_t tot_slot = 0;
   for (int k = 0; k < n_systems; k++) {
     const hsmc_params &p = params[k];
     if (p.n_particles <= 0 || p.pressure > 0 || !(p.dr_max >= 0)) {
@@ -137,13 +148,13 @@ int hsmc_batch_create(const hsmc_params *params, int n_systems, hsmc_batch **out
       delete b;
       return e;
     }
-    cap = ck > cap ? ck : cap;
+    caps[k] = ck;
+    tot_slot += (size_t)b->hbox[k].ncell * ck;
     tot_n += (size_t)p.n_particles;
     tot_cell += (size_t)b->hbox[k].ncell;
     b->max_n = p.n_particles > b->max_n ? p.n_particles : b->max_n;
     b->max_ncell = b->hbox[k].ncell > b->max_ncell ? b->hbox[k].ncell : b->max_ncell;
   }
-  b->cap = cap;
   auto fail = [&](cudaError_t e) {
     hsmc_batch_destroy(b);
     return cuda_fail(e);
@@ -155,26 +166,26 @@ int hsmc_batch_create(const hsmc_params *params, int n_systems, hsmc_batch **out
   for (int l = 0; l < 2; l++) {
     if ((ce = cudaMalloc(&b->cnt[l], sizeof(int) * tot_cell)) != cudaSuccess) return fail(ce);
     if ((ce = cudaMemset(b->cnt[l], 0, sizeof(int) * tot_cell)) != cudaSuccess) return fail(ce);
-    if ((ce = cudaMalloc(&b->slot[l], sizeof(Slot) * tot_cell * cap)) != cudaSuccess) return fail(ce);
+    if ((ce = cudaMalloc(&b->slot[l], sizeof(Slot) * tot_slot)) != cudaSuccess) return fail(ce);
   }
   if ((ce = cudaMalloc(&b->box, sizeof(Box) * n_systems)) != cudaSuccess) return fail(ce);
   if ((ce = cudaMalloc(&b->st, sizeof(DevState) * n_systems)) != cudaSuccess) return fail(ce);
   if ((ce = cudaMalloc(&b->d_reps, sizeof(SysPtrs) * n_systems)) != cudaSuccess) return fail(ce);
   std::vector<DevState> st0(n_systems);
-  size_t on = 0, oc = 0;
+  size_t on = 0, oc = 0, os = 0;
   for (int k = 0; k < n_systems; k++) {
     SysPtrs &s = b->sp[k];
     s.pos = b->pos + 4 * on;
     for (int l = 0; l < 2; l++) {
       s.cnt[l] = b->cnt[l] + oc;
-      s.slot[l] = b->slot[l] + oc * cap;
+      s.slot[l] = b->slot[l] + os;
     }
     s.box = b->box + k;
     s.st = b->st + k;
     s.trace = nullptr;
     s.trace_cap = 0;
     s.n = params[k].n_particles;
-    s.cap = cap;
+    s.cap = caps[k];
     s.ncell_alloc = b->hbox[k].ncell;
     DevState &d = st0[k];
     d = DevState{};
@@ -189,6 +200,7 @@ int hsmc_batch_create(const hsmc_params *params, int n_systems, hsmc_batch **out
     }
     on += (size_t)params[k].n_particles;
     oc += (size_t)b->hbox[k].ncell;
+    os += (size_t)b->hbox[k].ncell * caps[k];
   }
   if ((ce = cudaMemcpy(b->box, b->hbox.data(), sizeof(Box) * n_systems, cudaMemcpyHostToDevice)) != cudaSuccess)
     return fail(ce);
@@ -217,6 +229,31 @@ int hsmc_batch_create(const hsmc_params *params, int n_systems, hsmc_batch **out
     if ((ce = cudaMalloc(&b->d_gstart, sizeof(int) * (n_systems + 1))) != cudaSuccess) return fail(ce);
     if ((ce = cudaMemcpy(b->d_nstart, ns.data(), sizeof(int) * (n_systems + 1), cudaMemcpyHostToDevice)) ||
         (ce = cudaMemcpy(b->d_gstart, gs.data(), sizeof(int) * (n_systems + 1), cudaMemcpyHostToDevice)))
+      return fail(ce);
+  }
+  for (int c : {8, 16, 32}) {
+    std::vector<SysPtrs> sp;
+    std::vector<int> ids, gs(1, 0);
+    for (int k = 0; k < n_systems; k++)
+      if (caps[k] == c) {
+        sp.push_back(b->sp[k]);
+        ids.push_back(k);
+        gs.push_back(gs.back() + b->hbox[k].ncell / 8);
+      }
+    if (sp.empty()) continue;
+    hsmc_batch::CapClass cl;
+    cl.cap = c;
+    cl.group = c / 4;
+    cl.n = (int)sp.size();
+    cl.tot_groups = gs.back();
+    b->classes.push_back(cl);
+    hsmc_batch::CapClass &q = b->classes.back();
+    if ((ce = cudaMalloc(&q.d_reps, sizeof(SysPtrs) * q.n)) || (ce = cudaMalloc(&q.d_ids, sizeof(int) * q.n)) ||
+        (ce = cudaMalloc(&q.d_gstart, sizeof(int) * (q.n + 1))))
+      return fail(ce);
+    if ((ce = cudaMemcpy(q.d_reps, sp.data(), sizeof(SysPtrs) * q.n, cudaMemcpyHostToDevice)) ||
+        (ce = cudaMemcpy(q.d_ids, ids.data(), sizeof(int) * q.n, cudaMemcpyHostToDevice)) ||
+        (ce = cudaMemcpy(q.d_gstart, gs.data(), sizeof(int) * (q.n + 1), cudaMemcpyHostToDevice)))
       return fail(ce);
   }
   if ((ce = cudaEventCreate(&b->ev0)) != cudaSuccess) return fail(ce);
@@ -270,8 +307,14 @@ int hsmc_batch_set_steps(hsmc_batch *b, const double *dr_max) {
 static void enqueue_batch_sweep(hsmc_batch *b, long long offset) {
   launch_build_batch(b->d_reps, b->d_nstart, b->reps, b->tot_n, offset, b->stream);
   for (int k = 0; k < 8; k++)
-    launch_move_pass_batch(b->d_reps, b->d_gstart, b->reps, b->tot_groups, b->cap, k, b->group, b->cnt[0], b->cnt[1],
-                           b->tot_cell, b->stream);
+    for (size_t q = 0; q < b->classes.size(); q++) {
+      const hsmc_batch::CapClass &cl = b->classes[q];
+      // the first launch of the sweep's first pass clears the other layout
+      const bool clear = q == 0;
+      launch_move_pass_batch(cl.d_reps, cl.d_gstart, cl.d_ids, cl.n, cl.tot_groups, cl.cap, k, cl.group,
+                             clear ? b->cnt[0] : nullptr, clear ? b->cnt[1] : nullptr, clear ? b->tot_cell : 0,
+                             b->stream);
+    }
 }
 
 int hsmc_batch_sweeps(hsmc_batch *b, int n_sweeps, uint64_t *counters) {

@@ -75,8 +75,12 @@ cudaError_t launch_move_flow(const SysPtrs &p, uint32_t *prog, int group, bool t
 // (cells of one colour); launches cover all of them in one flat grid.
 void launch_build_batch(const SysPtrs *reps, const int *nstart, int n_reps, int tot_n, long long sweep_offset,
                         cudaStream_t s);
-void launch_move_pass_batch(const SysPtrs *reps, const int *gstart, int n_reps, int tot_groups, int cap, int pass,
-                            int group, int *cnt_pool0, int *cnt_pool1, long long pool_cells, cudaStream_t s);
+// one launch per cell capacity: reps / gstart / ids over the replicas of
+// that capacity (ids: their index in the batch); pools non-null clears the
+// other layout of the pooled counts on pass 0
+void launch_move_pass_batch(const SysPtrs *reps, const int *gstart, const int *ids, int n_reps, int tot_groups,
+                            int cap, int pass, int group, int *cnt_pool0, int *cnt_pool1, long long pool_cells,
+                            cudaStream_t s);
 void launch_advance_batch(const SysPtrs *reps, int n_reps, int n_sweeps, cudaStream_t s);
 void launch_pair_hist_batch(const SysPtrs *reps, int n_reps, int max_n, double bin, double rmax, int nbins,
                             unsigned long long *counts, cudaStream_t s);

@@ -467,14 +467,15 @@ __device__ __forceinline__ void add_tally(const PassTally &t, DevState *ws) {
 }
 
 // One colour pass: every active cell of the colour, then a kernel boundary.
-// In a batch (BATCH) the grid covers the active cells of every replica
-// (gstart: their prefix sums); each group finds its replica, whose index
-// enters the random counters, and the counters are summed per replica.  The
-// first pass also clears the other layout of the pooled count arrays.
+// In a batch (BATCH) the grid covers the active cells of every replica of
+// one cell capacity (gstart: their prefix sums); each group finds its
+// replica, whose batch index (rep_ids) enters the random counters, and the
+// counters are summed per replica.  Given the pooled count arrays, the first
+// pass also clears their other layout.
 template <int G, int CAP, bool TRACE, bool BATCH>
 __global__ void __launch_bounds__(128, PassSmem<G, CAP>::min_blocks)
-    k_move_pass(SysPtrs p1, const SysPtrs *reps, const int *gstart, int n_reps, int pass, int *pool0, int *pool1,
-                long long pool_cells) {
+    k_move_pass(SysPtrs p1, const SysPtrs *reps, const int *gstart, const int *rep_ids, int n_reps, int pass,
+                int *pool0, int *pool1, long long pool_cells) {
   static_assert(G == 1 || G == 2 || G == 4 || G == 8, "group size");
   extern __shared__ __align__(16) unsigned char smem_raw[];
   const PassSm m = pass_smem_ptrs<G, CAP>(smem_raw);
@@ -513,7 +514,7 @@ __global__ void __launch_bounds__(128, PassSmem<G, CAP>::min_blocks)
     return;
   }
 
-  if (pass == 0) {
+  if (pass == 0 && pool_cells > 0) {
     const int layout0 = (int)(reps[0].st->params.sweep & 1ull);
     int *other = layout0 ? pool0 : pool1;
     for (long long c = blockIdx.x * (long long)blockDim.x + threadIdx.x; c < pool_cells;
@@ -525,7 +526,7 @@ __global__ void __launch_bounds__(128, PassSmem<G, CAP>::min_blocks)
     r = find_rep(gstart, n_reps, group);
     const SysPtrs p = reps[r];
     const unsigned long long sweep = p.st->params.sweep;
-    PassEnv e = pass_env(p, (uint32_t)r, (int)(sweep & 1ull));
+    PassEnv e = pass_env(p, (uint32_t)__ldg(rep_ids + r), (int)(sweep & 1ull));
     e.seq = sweep * 8ull + (unsigned long long)pass;
     const int colour = p.st->params.perm[pass];
     const int hx = e.nc[0] >> 1, hy = e.nc[1] >> 1;
@@ -745,26 +746,29 @@ int move_pass_grid(int group, int cap, int ncell_alloc, int num_sms) {
 template <int G, int CAP>
 static void launch_gc(const SysPtrs &p, int pass, bool trace, int grid, cudaStream_t s) {
   const size_t sm = pass_smem<G, CAP>();
-  if (trace) k_move_pass<G, CAP, true, false><<<grid, 128, sm, s>>>(p, nullptr, nullptr, 0, pass, nullptr, nullptr, 0);
-  else k_move_pass<G, CAP, false, false><<<grid, 128, sm, s>>>(p, nullptr, nullptr, 0, pass, nullptr, nullptr, 0);
+  if (trace)
+    k_move_pass<G, CAP, true, false><<<grid, 128, sm, s>>>(p, nullptr, nullptr, nullptr, 0, pass, nullptr, nullptr, 0);
+  else
+    k_move_pass<G, CAP, false, false><<<grid, 128, sm, s>>>(p, nullptr, nullptr, nullptr, 0, pass, nullptr, nullptr, 0);
 }
 
 template <int G, int CAP>
-static void launch_batch_gc(const SysPtrs *reps, const int *gstart, int n_reps, int tot_groups, int pass, int *pool0,
-                            int *pool1, long long pool_cells, cudaStream_t s) {
+static void launch_batch_gc(const SysPtrs *reps, const int *gstart, const int *ids, int n_reps, int tot_groups,
+                            int pass, int *pool0, int *pool1, long long pool_cells, cudaStream_t s) {
   const long long threads = (long long)tot_groups * G;
   const int grid = (int)((threads + 127) / 128);
   k_move_pass<G, CAP, false, true><<<grid > 0 ? grid : 1, 128, pass_smem<G, CAP>(), s>>>(
-      SysPtrs{}, reps, gstart, n_reps, pass, pool0, pool1, pool_cells);
+      SysPtrs{}, reps, gstart, ids, n_reps, pass, pool0, pool1, pool_cells);
 }
 
-void launch_move_pass_batch(const SysPtrs *reps, const int *gstart, int n_reps, int tot_groups, int cap, int pass,
-                            int group, int *cnt_pool0, int *cnt_pool1, long long pool_cells, cudaStream_t s) {
-#define HSMC_BATCH_CAP(G)                                                                                    \
-  switch (cap) {                                                                                             \
-    case 8: launch_batch_gc<G, 8>(reps, gstart, n_reps, tot_groups, pass, cnt_pool0, cnt_pool1, pool_cells, s); break;   \
-    case 16: launch_batch_gc<G, 16>(reps, gstart, n_reps, tot_groups, pass, cnt_pool0, cnt_pool1, pool_cells, s); break; \
-    default: launch_batch_gc<G, 32>(reps, gstart, n_reps, tot_groups, pass, cnt_pool0, cnt_pool1, pool_cells, s); break; \
+void launch_move_pass_batch(const SysPtrs *reps, const int *gstart, const int *ids, int n_reps, int tot_groups,
+                            int cap, int pass, int group, int *cnt_pool0, int *cnt_pool1, long long pool_cells,
+                            cudaStream_t s) {
+#define HSMC_BATCH_CAP(G)                                                                                  \
+  switch (cap) {                                                                                           \
+    case 8: launch_batch_gc<G, 8>(reps, gstart, ids, n_reps, tot_groups, pass, cnt_pool0, cnt_pool1, pool_cells, s); break; \
+    case 16: launch_batch_gc<G, 16>(reps, gstart, ids, n_reps, tot_groups, pass, cnt_pool0, cnt_pool1, pool_cells, s); break; \
+    default: launch_batch_gc<G, 32>(reps, gstart, ids, n_reps, tot_groups, pass, cnt_pool0, cnt_pool1, pool_cells, s); break; \
   }
   switch (group) {
     case 1: HSMC_BATCH_CAP(1) break;
