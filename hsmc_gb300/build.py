@@ -2,7 +2,8 @@
 
 Compiles the CUDA sources in ``csrc/`` for sm_103a into
 ``hsmc_gb300/libhsmc_gpu.so`` (the C-ABI library declared in
-``include/hsmc_gpu.h``) and the drop-in host program ``hsmc_gb300/bin/hsmc``.
+``include/hsmc_gpu.h``), the drop-in host program ``hsmc_gb300/bin/hsmc`` and
+the analysis tool ``hsmc_gb300/bin/hsmc_stat``.
 Translation units are compiled in parallel; nothing is installed outside the
 package directory.
 """
@@ -90,9 +91,22 @@ def build_host() -> str | None:
     return EXE
 
 
+STAT_SRC = os.path.join(PKG, "analysis", "hsmc_stat.c")
+STAT_EXE = os.path.join(BIN_DIR, "hsmc_stat")
+
+
+def build_stat() -> str:
+    """The analysis tool (blocking, jackknife, contact fits) in plain C."""
+    os.makedirs(BIN_DIR, exist_ok=True)
+    if not _newer(STAT_EXE, [STAT_SRC]):
+        subprocess.run(["gcc", "-O2", "-std=gnu99", "-Wall", "-o", STAT_EXE, STAT_SRC, "-lm"], check=True)
+    return STAT_EXE
+
+
 def build(verbose_ptxas: bool = False) -> None:
     build_library(verbose_ptxas)
     build_host()
+    build_stat()
 
 
 if __name__ == "__main__":
