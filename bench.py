@@ -369,11 +369,23 @@ def run_replicas(args):
     per_block = samples // blocks
     z = np.array([[contact_z(cnt[j, i], per_block, b.n[i], rhos[i], bin_) for i in range(reps)]
                   for j in range(blocks)])
+    z2 = np.array([[contact_z(cnt[j, i], per_block, b.n[i], rhos[i], bin_, degree=2) for i in range(reps)]
+                   for j in range(blocks)]).mean(axis=0)
     zm = z.mean(axis=0)
     se = z.std(axis=0, ddof=1) / np.sqrt(blocks)
     zcs = np.array([carnahan_starling(r) for r in rhos])
     dev = (zm - zcs) / se
     fluid = rhos < 0.90
+    edges = [0.30, 0.50, 0.70, 0.85, 0.94]
+    by_rho = []
+    for lo, hi in zip(edges[:-1], edges[1:]):
+        sel = (rhos >= lo) & (rhos < hi)
+        if sel.any():
+            by_rho.append({"rho": [lo, hi], "replicas": int(sel.sum()),
+                           "within_3se": float(np.mean(np.abs(dev[sel]) < 3)),
+                           "mean_rel_dev": float(np.mean((zm[sel] - zcs[sel]) / zcs[sel])),
+                           "median_rel_se": float(np.median(se[sel] / zcs[sel])),
+                           "mean_rel_dev_quadratic_fit": float(np.mean((z2[sel] - zcs[sel]) / zcs[sel]))})
     line = {
         "metric": "trial moves/s, 512 batched replicas", "value": moves / (t_gpu * 1e-3), "unit": "trial moves/s",
         "n_gpus": 1, "higher_is_better": True, "dtype": "f64", "data": "synthetic (FCC lattice starts)",
@@ -384,6 +396,7 @@ def run_replicas(args):
         "pressure": {"within_3se_of_cs": float(np.mean(np.abs(dev) < 3)),
                      "within_3se_of_cs_rho_below_0.90": float(np.mean(np.abs(dev[fluid]) < 3)),
                      "median_abs_rel_dev": float(np.median(np.abs(zm - zcs) / zcs)),
+                     "by_density": by_rho,
                      "worst": {"rho": float(rhos[np.argmax(np.abs(dev))]), "z": float(zm[np.argmax(np.abs(dev))]),
                                "z_cs": float(zcs[np.argmax(np.abs(dev))]),
                                "se": float(se[np.argmax(np.abs(dev))])}},

@@ -95,6 +95,7 @@ def load() -> C.CDLL:
     L.hsmc_gpu_autotune.argtypes = [_vp, C.c_int, _P(C.c_int)]
     L.hsmc_gpu_set_schedule.argtypes = [_vp, C.c_int, C.c_int]
     L.hsmc_gpu_get_schedule.argtypes = [_vp, _P(C.c_int), _P(C.c_int)]
+    L.hsmc_gpu_hold_region.argtypes = [_vp, C.c_int]
     L.hsmc_gpu_last_timing.argtypes = [_vp, _P(C.c_double), _P(C.c_double), _P(C.c_int)]
     _lib = L
     return L

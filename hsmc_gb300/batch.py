@@ -132,19 +132,20 @@ class ReplicaBatch:
         return t.value
 
 
-def contact_z(counts, samples: int, n: int, rho: float, dr: float):
+def contact_z(counts, samples: int, n: int, rho: float, dr: float, degree: int = 1):
     """Compressibility factor from the virial contact histogram, as the
     reference's analysis does (compute_pressv, src/compute_press.c:277-307;
     fit in python/hsmc_pressure.py): counts of ordered pairs with r in
     [1 + k dr, 1 + (k+1) dr), normalised to g(r) at the bin centres, a linear
-    fit extrapolated to r = 1, Z = 1 + (2 pi / 3) rho g(1)."""
+    fit extrapolated to r = 1, Z = 1 + (2 pi / 3) rho g(1).  degree 2 fits a
+    parabola instead, to gauge the bias of the straight line."""
     counts = np.asarray(counts, dtype=np.float64)
     nb = counts.shape[-1]
     r = 1.0 + (np.arange(nb) + 0.5) * dr
     shell = 4.0 * np.pi / 3.0 * ((r + dr / 2) ** 3 - (r - dr / 2) ** 3)
     g = counts / (samples * shell * rho * n)
-    b1, b0 = np.polyfit(r, g, 1)
-    return 1.0 + 2.0 * np.pi / 3.0 * rho * (b0 + b1)
+    coef = np.polyfit(r, g, degree)
+    return 1.0 + 2.0 * np.pi / 3.0 * rho * float(np.polyval(coef, 1.0))
 
 
 def carnahan_starling(rho: float) -> float:

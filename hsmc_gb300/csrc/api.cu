@@ -277,6 +277,7 @@ int hsmc_gpu_create(const hsmc_params *prm, hsmc_ctx **out) {
   s0.pressure = prm->pressure;
   s0.seed = prm->seed;
   s0.per_cell = prm->lattice_type == 1 ? 1 : 4;
+  s0.flow_hold = -1;
   for (int d = 0; d < 3; d++) {
     s0.cells[d] = prm->cells[d];
     s0.nc_alloc[d] = balloc.nc[d];
@@ -583,6 +584,14 @@ int hsmc_gpu_set_schedule(hsmc_ctx *ctx, int schedule, int lanes_per_cell) {
   const int g = lanes_per_cell == 0 ? ctx->group : lanes_per_cell;
   if (g != 1 && g != 2 && g != 4 && g != 8) return HSMC_ERR_INVALID_ARG;
   return apply_schedule(ctx, schedule, g) ? HSMC_OK : HSMC_ERR_INVALID_ARG;
+}
+
+int hsmc_gpu_hold_region(hsmc_ctx *ctx, int region) {
+  if (!ctx || region < -1 || region >= ctx->sp.ncell_alloc / 8) return HSMC_ERR_INVALID_ARG;
+  HSMC_CUDA(cudaMemcpyAsync(&ctx->sp.st->flow_hold, &region, sizeof(int), cudaMemcpyHostToDevice, ctx->stream));
+  reset_progress(ctx);
+  HSMC_CUDA(cudaStreamSynchronize(ctx->stream));
+  return HSMC_OK;
 }
 
 int hsmc_gpu_get_schedule(hsmc_ctx *ctx, int *schedule, int *lanes_per_cell) {

@@ -194,6 +194,7 @@ int hsmc_batch_create(const hsmc_params *params, int n_systems, hsmc_batch **out
     d.dv_max = params[k].dv_max;
     d.seed = params[k].seed;
     d.per_cell = params[k].lattice_type == 1 ? 1 : 4;
+    d.flow_hold = -1;
     for (int q = 0; q < 3; q++) {
       d.cells[q] = params[k].cells[q];
       d.nc_alloc[q] = b->hbox[k].nc[q];

@@ -202,7 +202,7 @@ struct DevState {
   int vol_overlap, vol_accept;
   int cells[3], per_cell;
   int nc_alloc[3];
-  int pad2;
+  int flow_hold;  // dataflow schedule: a region that does not publish (diagnostic), -1 for none
 };
 
 // One particle in a cell: its grid coordinates t (single precision, from

@@ -609,6 +609,7 @@ __global__ void __launch_bounds__(128, PassSmem<G, CAP>::min_blocks) k_move_flow
   const int n_active = hx * hy * hz;
   const int iters = (n_active + groups - 1) / groups;  // the same for every thread
   const uint32_t base = (uint32_t)(sweep * 8ull);
+  const int hold = p.st->flow_hold;
 
   PassTally t;
   for (int pass = 0; pass < 8; pass++) {
@@ -637,7 +638,7 @@ __global__ void __launch_bounds__(128, PassSmem<G, CAP>::min_blocks) k_move_flow
       if (valid)
         move_cell<G, CAP, TRACE, true>(e, m, tid, lane, gl, col0, gmask, 2 * ax + cx, 2 * ay + cy, 2 * az + cz, t);
       __syncwarp();
-      if (valid && lane == 0) {
+      if (valid && lane == 0 && ac != hold) {
         __threadfence();
         st_release(prog + ac, base + (uint32_t)pass + 1u);
       }

@@ -232,6 +232,13 @@ int hsmc_gpu_autotune(hsmc_ctx *ctx, int sweeps_per_variant, int *lanes_out);
 int hsmc_gpu_set_schedule(hsmc_ctx *ctx, int schedule, int lanes_per_cell);
 int hsmc_gpu_get_schedule(hsmc_ctx *ctx, int *schedule, int *lanes_per_cell);
 
+/* Diagnostic of the dataflow schedule's bounded waits: region (a 2x2x2
+ * block of cells, index x + hx (y + hy z) over the half-grid) stops
+ * publishing its progress, so every wait on it runs out after 1 s and the
+ * sweep returns HSMC_ERR_TIMEOUT; -1 restores normal operation (and the
+ * progress words).  The context stays usable throughout. */
+int hsmc_gpu_hold_region(hsmc_ctx *ctx, int region);
+
 /* Timing of the last sweep call, from CUDA events on the context's stream:
  * total device time, and (only with profiling on) the summed time and count
  * of the move-pass kernel launches.  With profiling on, sweeps are launched

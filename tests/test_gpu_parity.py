@@ -206,3 +206,23 @@ def test_dataflow_schedule_npt_matches(gpu_lib):
         confs.append((s.download(), s.get_box()))
     assert np.array_equal(confs[0][0], confs[1][0])
     assert np.array_equal(confs[0][1], confs[1][1])
+
+
+def test_dataflow_wait_runs_out_and_reports(gpu_lib):
+    """Failure detection without a fault: one region that never publishes its
+    progress (a flag nothing sets) makes its neighbours' waits run out, each
+    bounded at 1 s; the sweep reports a time-out, and once the region is
+    released the context carries on."""
+    from hsmc_gb300.system import HsmcError
+
+    s = gpu_lib.HardSphereSystem(rho=0.5, cells=4, dr_max=0.2, seed=3)
+    s.set_schedule(1, 2)
+    s.sweep_nvt(2)
+    assert s._lib.hsmc_gpu_hold_region(s._h, 0) == 0
+    with pytest.raises(HsmcError) as err:
+        s.sweep_nvt(1)
+    assert err.value.code == 7  # HSMC_ERR_TIMEOUT
+    assert s._lib.hsmc_gpu_hold_region(s._h, -1) == 0
+    s.rng_set_state(s.rng_state())  # rebuild the layout for the next sweep
+    c = s.sweep_nvt(2)
+    assert c[0] == 2 * s.n
