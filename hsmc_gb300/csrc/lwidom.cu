@@ -516,9 +516,12 @@ __global__ void k_adam(float *prm, float *m, float *v, const float *grad, float 
 }
 
 // ------------------------------------------------------------- proposal
+// pi_c = sqrt(sigmoid(z_c)) in FP32 (the FP64 pipe of this GPU is narrow);
+// the proposal and the weights both use this same value, so the estimate
+// stays unbiased.
 __global__ void k_pi(const float *z, double *pi, int n) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i < n) pi[i] = sqrt(1.0 / (1.0 + exp(-(double)z[i])));
+  if (i < n) pi[i] = (double)sqrtf(1.0f / (1.0f + expf(-z[i])));
 }
 
 // Inclusive FP64 prefix sum: 4096 values per block (4 per thread), block
@@ -612,10 +615,14 @@ __global__ void __launch_bounds__(IS_THREADS) k_widom_is(SysPtrs p, SubGrid g, c
       x[2] = __dmul_rn(open_unit(r.w), len[2]);
     } else {
       const double t = __dmul_rn(__dmul_rn(__dadd_rn((double)((unsigned long long)r.x - thr), 0.5), inv_span), total);
-      int lo = 0, hi = g.nsub - 1;  // first index with cdf > t
+      // first index with cdf > t; positive doubles order as their bit
+      // patterns, so the comparisons stay off the FP64 pipe
+      const long long tb = __double_as_longlong(t);
+      const long long *cdf_bits = reinterpret_cast<const long long *>(cdf);
+      int lo = 0, hi = g.nsub - 1;
       while (lo < hi) {
         const int mid = (lo + hi) >> 1;
-        if (cdf[mid] > t) hi = mid;
+        if (__ldg(cdf_bits + mid) > tb) hi = mid;
         else lo = mid + 1;
       }
       cell = lo;

@@ -195,12 +195,14 @@ def adam(pv, gv, m, v, step, lr, b1=0.9, b2=0.999, eps=1e-8):
 
 # ------------------------------------------------------------------ proposal
 def proposal_weights(z):
-    """Sub-cell proposal weights pi = sqrt(sigmoid(z)): for a proposal that is
-    uniform inside each sub-cell, the variance of the importance-sampling
-    estimate of P(success) is smallest with q_c proportional to the square
-    root of the success probability in sub-cell c."""
-    z = np.asarray(z, dtype=np.float64)
-    return np.sqrt(1.0 / (1.0 + np.exp(-z)))
+    """Sub-cell proposal weights pi = sqrt(sigmoid(z)), in float32 as on the
+    device: for a proposal that is uniform inside each sub-cell, the variance
+    of the importance-sampling estimate of P(success) is smallest with q_c
+    proportional to the square root of the success probability in sub-cell
+    c."""
+    z = np.asarray(z, dtype=np.float32)
+    one = np.float32(1.0)
+    return np.sqrt(one / (one + np.exp(-z))).astype(np.float64)
 
 
 def replay_points(seed, seq, n, alpha, cdf, ns, box):
