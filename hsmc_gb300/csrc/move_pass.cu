@@ -76,6 +76,19 @@ __device__ __forceinline__ void image_of(unsigned code, int ix, int iy, int iz, 
   imz = (iz + oz < 0) ? -L32[2] : (iz + oz >= nc[2] ? L32[2] : 0.f);
 }
 
+// Index of neighbour `code` of cell c = (ix, iy, iz): a linear offset for an
+// interior cell, periodic wrapping otherwise.
+__device__ __forceinline__ int neighbour_cell(unsigned code, int ix, int iy, int iz, int c, const int *nc,
+                                              bool interior) {
+  const int ox = (int)(code & 3u) - 1, oy = (int)((code >> 2) & 3u) - 1, oz = (int)(code >> 4) - 1;
+  if (interior) return c + ox + nc[0] * (oy + nc[1] * oz);
+  int x = ix + ox, y = iy + oy, z = iz + oz;
+  x += x < 0 ? nc[0] : (x >= nc[0] ? -nc[0] : 0);
+  y += y < 0 ? nc[1] : (y >= nc[1] ? -nc[1] : 0);
+  z += z < 0 ? nc[2] : (z >= nc[2] ? -nc[2] : 0);
+  return x + nc[0] * (y + nc[1] * z);
+}
+
 __device__ __forceinline__ float dist2(float ux, float uy, float uz, const float4 &q) {
   const float dx = ux - q.x, dy = uy - q.y, dz = uz - q.z;
   return dx * dx + dy * dy + dz * dz;
@@ -161,20 +174,7 @@ __device__ __forceinline__ void move_cell(const PassEnv &e, const PassSm &m, int
 #pragma unroll
   for (int q = 0; q < NB; q++) {
     const int o26 = lane + q * G;
-    nb_c[q] = c;
-    if (o26 < 26) {
-      const unsigned code = c_nbr[o26];
-      const int ox = (int)(code & 3u) - 1, oy = (int)((code >> 2) & 3u) - 1, oz = (int)(code >> 4) - 1;
-      if (interior) {
-        nb_c[q] = c + ox + nc[0] * (oy + nc[1] * oz);
-      } else {
-        int x = ix + ox, y = iy + oy, z = iz + oz;
-        x += x < 0 ? nc[0] : (x >= nc[0] ? -nc[0] : 0);
-        y += y < 0 ? nc[1] : (y >= nc[1] ? -nc[1] : 0);
-        z += z < 0 ? nc[2] : (z >= nc[2] ? -nc[2] : 0);
-        nb_c[q] = x + nc[0] * (y + nc[1] * z);
-      }
-    }
+    nb_c[q] = o26 < 26 ? neighbour_cell(c_nbr[o26], ix, iy, iz, c, nc, interior) : c;
   }
   const int n = e.cnt[c];
 #pragma unroll
@@ -333,11 +333,18 @@ __device__ __forceinline__ void move_cell(const PassEnv &e, const PassSm &m, int
       } else {
 #pragma unroll
         for (int q = 0; q < NB; q++) {
-          if (nb_n[q] == 0) continue;
+          // recomputed here so the staging arrays need not live through the trials
+          const int o26 = lane + q * G;
+          if (o26 >= 26) continue;
+          const unsigned code = c_nbr[o26];
+          const int nbc = neighbour_cell(code, ix, iy, iz, c, nc, interior);
+          const int mm = e.cnt[nbc];
+          const int nbn = mm < CAP ? mm : CAP;
+          if (nbn == 0) continue;
           float imx, imy, imz;
-          image_of(c_nbr[lane + q * G], ix, iy, iz, nc, e.L32, imx, imy, imz);
-          for (int k = 0; k < nb_n[q] && !ov; k++) {
-            const Slot *sp = e.slot + (size_t)nb_c[q] * CAP + k;
+          image_of(code, ix, iy, iz, nc, e.L32, imx, imy, imz);
+          for (int k = 0; k < nbn && !ov; k++) {
+            const Slot *sp = e.slot + (size_t)nbc * CAP + k;
             Slot o;
             if (FLOW) {
               const float4 v = __ldcg(reinterpret_cast<const float4 *>(sp));

@@ -1,4 +1,4 @@
-"""Python mirror of the HSMC reference's local-move driver on the GB300 engine.
+"""Python mirror of the HSMC reference's local-move run loop on the GB300 engine.
 
 ``HardSphereSystem`` follows the reference's flow and names:
 
