@@ -348,7 +348,8 @@ def run_replicas(args):
     ns = rng.integers(6, 21, reps)
     rhos = rng.uniform(0.30, 0.94, reps)
     systems = [(float(r), int(n), 0.1, 1000 + k) for k, (r, n) in enumerate(zip(rhos, ns))]
-    b = ReplicaBatch(systems)
+    edge = args.cell_edge if args.cell_edge == "auto" else float(args.cell_edge)
+    b = ReplicaBatch(systems, min_cell_edge=edge)
     n_tot = int(sum(b.n))
     dr, acc = b.tune_steps(0.1, target=TARGET_ACC)
     b.sweeps(args.equil)
@@ -391,6 +392,7 @@ def run_replicas(args):
         "n_gpus": 1, "higher_is_better": True, "dtype": "f64", "data": "synthetic (FCC lattice starts)",
         "config": {"workload": f"{reps} NVT replicas, n~U{{6..20}} (N 864..32000), rho~U[0.30,0.94], "
                                f"{sweeps} sweeps after {args.equil}", "n_particles_total": n_tot,
+                   "min_cell_edge": args.cell_edge,
                    "acceptance_min_max": [float(acc.min()), float(acc.max())]},
         "gpu_ms": t_gpu,
         "pressure": {"within_3se_of_cs": float(np.mean(np.abs(dev) < 3)),
@@ -549,6 +551,8 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--workload", default="fluid", choices=["fluid", "replicas", "widom", "npt"])
     ap.add_argument("--replicas", type=int, default=512)
+    ap.add_argument("--cell-edge", default="0",
+                    help='replicas: smallest device-cell edge, a number or "auto" (min(rho^-1/3, 1.4))')
     ap.add_argument("--sweeps", type=int, default=5000)
     ap.add_argument("--equil", type=int, default=500)
     ap.add_argument("--samples", type=int, default=20)

@@ -43,7 +43,8 @@ class HsmcParams(C.Structure):
         ("seed", C.c_uint64),
         ("cell_capacity", C.c_int),
         ("lanes_per_cell", C.c_int),
-        ("reserved", C.c_int * 6),
+        ("min_cell_edge", C.c_double),
+        ("reserved", C.c_int * 4),
     ]
 
 

@@ -28,9 +28,11 @@ def _bind(lib):
 
 class ReplicaBatch:
     """Independent NVT systems on FCC/SC lattice starts, one per entry of
-    ``systems`` = [(rho, cells, dr_max, seed), ...]."""
+    ``systems`` = [(rho, cells, dr_max, seed), ...].  min_cell_edge: a number
+    for every replica, or "auto" for min(rho^(-1/3), 1.4), about one sphere
+    per device cell (below 1.41 a cell holds at most 14)."""
 
-    def __init__(self, systems, lattice_type: int = 2):
+    def __init__(self, systems, lattice_type: int = 2, min_cell_edge=0.0):
         lib = _native.load()
         _bind(lib)
         self._lib = lib
@@ -52,6 +54,8 @@ class ReplicaBatch:
             p.dr_max = dr
             p.dv_max = 0.001
             p.seed = seed
+            p.min_cell_edge = (min(rho ** (-1.0 / 3.0), 1.4) if min_cell_edge == "auto"
+                               else float(min_cell_edge))
             self.n.append(conf.shape[0])
             self.box.append(box)
             confs.append(conf)

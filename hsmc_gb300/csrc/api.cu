@@ -119,14 +119,15 @@ static int status_to_code(int st) {
 // Cell grid for a box: an even number of cells per axis, each edge at least
 // 1 + margin, the margin covering single-precision rounding of coordinates
 // up to the box length.
-int hsmc::make_box(const double len[3], double rho, Box &b, int &cap) {
+int hsmc::make_box(const double len[3], double rho, Box &b, int &cap, double min_edge) {
   double lmax = len[0];
   for (int d = 1; d < 3; d++) lmax = len[d] > lmax ? len[d] : lmax;
   const double u = 5.9604644775390625e-08;  // 2^-24
   const double margin = u * (64.0 * lmax + 64.0);
   double wmax = 0.0;
+  const double wmin = min_edge > 1.0 + margin ? min_edge : 1.0 + margin;
   for (int d = 0; d < 3; d++) {
-    int nc = 2 * (int)std::floor(len[d] / (2.0 * (1.0 + margin)));
+    int nc = 2 * (int)std::floor(len[d] / (2.0 * wmin));
     if (nc < 4) return HSMC_ERR_CELL_TOO_SMALL;
     b.len[d] = len[d];
     b.half[d] = len[d] / 2.0;
@@ -205,6 +206,8 @@ int hsmc_gpu_create(const hsmc_params *prm, hsmc_ctx **out) {
     return HSMC_ERR_INVALID_ARG;
   for (int d = 0; d < 3; d++)
     if (!(prm->dr_max < prm->box[d])) return HSMC_ERR_INVALID_ARG;
+  // the device re-derives an NpT grid with the standard edge only
+  if (!(prm->min_cell_edge >= 0.0) || (prm->min_cell_edge > 0.0 && prm->pressure > 0)) return HSMC_ERR_INVALID_ARG;
   int dev = 0;
   if (cudaGetDevice(&dev) != cudaSuccess) return HSMC_ERR_NO_DEVICE;
   cudaDeviceProp p{};
@@ -216,7 +219,7 @@ int hsmc_gpu_create(const hsmc_params *prm, hsmc_ctx **out) {
   Box b{};
   int cap = 8;
   const double rho = prm->n_particles / (prm->box[0] * prm->box[1] * prm->box[2]);
-  int e = make_box(prm->box, prm->rho > 0 ? prm->rho : rho, b, cap);
+  int e = make_box(prm->box, prm->rho > 0 ? prm->rho : rho, b, cap, prm->min_cell_edge);
   if (e) return e;
   // NpT boxes change: cells are allocated for a box 25% longer per side, and
   // the grid margin is fixed for that largest box.

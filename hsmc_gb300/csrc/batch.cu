@@ -143,7 +143,11 @@ int hsmc_batch_create(const hsmc_params *params, int n_systems, hsmc_batch **out
       }
     int ck = 8;
     const double rho = p.rho > 0 ? p.rho : p.n_particles / (p.box[0] * p.box[1] * p.box[2]);
-    int e = make_box(p.box, rho, b->hbox[k], ck);
+    if (!(p.min_cell_edge >= 0.0)) {
+      delete b;
+      return HSMC_ERR_INVALID_ARG;
+    }
+    int e = make_box(p.box, rho, b->hbox[k], ck, p.min_cell_edge);
     if (e) {
       delete b;
       return e;

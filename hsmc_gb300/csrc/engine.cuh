@@ -53,7 +53,7 @@ struct CtxView {
 int ctx_view(::hsmc_ctx *ctx, CtxView *out);
 
 // api.cu: device cell grid for a box (even count per axis, edge >= 1 + margin)
-int make_box(const double len[3], double rho, Box &b, int &cap);
+int make_box(const double len[3], double rho, Box &b, int &cap, double min_edge = 0.0);
 
 // sweep.cu
 void launch_build(const SysPtrs &p, long long sweep_offset, int num_sms, cudaStream_t s);

@@ -81,7 +81,7 @@ class HardSphereSystem:
 
     def __init__(self, rho: float, cells, lattice_type: int = 2, dr_max: float = 0.05, dv_max: float = 0.001,
                  pressure: float = 0.0, seed: int = 0, conf: np.ndarray | None = None, cell_capacity: int = 0,
-                 box=None, lanes_per_cell: int = 0):
+                 box=None, lanes_per_cell: int = 0, min_cell_edge: float = 0.0):
         lib = _native.load()
         self._lib = lib
         if np.isscalar(cells):
@@ -112,6 +112,7 @@ class HardSphereSystem:
         p.seed = seed
         p.cell_capacity = cell_capacity
         p.lanes_per_cell = lanes_per_cell
+        p.min_cell_edge = min_cell_edge
         h = C.c_void_p()
         _check(lib.hsmc_gpu_create(C.byref(p), C.byref(h)), "hsmc_gpu_create")
         self._h = h

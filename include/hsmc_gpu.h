@@ -62,7 +62,11 @@ typedef struct {
   int lanes_per_cell;   /* GPU lanes sharing one active cell in a move pass: 1, 2, 4 or 8;
                            0 picks the default; 1 is refused for 32-slot cells (its
                            shared memory does not fit a block) */
-  int reserved[6];
+  double min_cell_edge; /* NVT only: smallest edge of the device cells (0 = 1 plus the rounding
+                           margin).  Larger cells hold more spheres each; for a sparse fluid an
+                           edge near rho^(-1/3) spreads the per-cell cost over about one sphere.
+                           Part of the chain's definition, like the seed. */
+  int reserved[4];
 } hsmc_params;
 
 /* Replaces the set-up in hs_nvt / hs_npt (src/nvt.c:30-62, src/npt.c:25-70):

@@ -21,6 +21,25 @@ def test_replica_zero_is_the_single_system_chain(gpu_lib):
     assert np.array_equal(c[0], cs)
 
 
+def test_replica_with_larger_cells_is_the_single_system_chain(gpu_lib):
+    """A minimum cell edge is part of the chain's definition: the replica and
+    a single context given the same edge run the same chain (replica 0; the
+    replica index is part of the others' random counters)."""
+    from hsmc_gb300.batch import ReplicaBatch
+
+    systems = [(0.45, 6, 0.3, 5), (0.80, 6, 0.15, 6), (0.30, 7, 0.4, 7)]
+    b = ReplicaBatch(systems, min_cell_edge="auto")
+    c = b.sweeps(23)
+    rho, n, dr, seed = systems[0]
+    s = gpu_lib.HardSphereSystem(rho=rho, cells=n, dr_max=dr, seed=seed,
+                                 min_cell_edge=min(rho ** (-1.0 / 3.0), 1.4))
+    cs = s.sweep_nvt(23)
+    assert np.array_equal(b.download(0), s.download())
+    assert np.array_equal(c[0], cs)
+    for k in (1, 2):
+        assert 0 < c[k, 1] < c[k, 0]
+
+
 def test_uneven_replicas_stay_overlap_free(oracle_mod, gpu_lib):
     from hsmc_gb300.batch import ReplicaBatch
 

@@ -12,7 +12,7 @@ import pytest
 pytestmark = pytest.mark.gpu
 
 
-def fluid(oracle_mod, gpu, rho, n, seed, dr, sweeps=30, neigh_dr=1.05, lanes=0):
+def fluid(oracle_mod, gpu, rho, n, seed, dr, sweeps=30, neigh_dr=1.05, lanes=0, min_edge=0.0):
     """An oracle system run from the lattice (the reference's own chain) and a
     GPU system started from the same configuration."""
     o = oracle_mod.OracleSim(rho=rho, n_cells=n, seed=seed, dr_max=dr, neigh_dr=neigh_dr,
@@ -20,7 +20,8 @@ def fluid(oracle_mod, gpu, rho, n, seed, dr, sweeps=30, neigh_dr=1.05, lanes=0):
     if sweeps:
         o.sweeps_nvt(sweeps)
     conf = o.get_config()
-    g = gpu.HardSphereSystem(rho=rho, cells=n, dr_max=dr, seed=seed + 1000, conf=conf, lanes_per_cell=lanes)
+    g = gpu.HardSphereSystem(rho=rho, cells=n, dr_max=dr, seed=seed + 1000, conf=conf, lanes_per_cell=lanes,
+                             min_cell_edge=min_edge)
     return o, g, conf
 
 
@@ -60,11 +61,23 @@ def test_overlap_decisions_bit_exact(oracle_mod, gpu_lib, rho, n, seed, dr):
 
 
 @pytest.mark.parametrize("lanes", [1, 2, 4, 8])
-@pytest.mark.parametrize("rho,n,seed,dr", CASES + [(0.70, 10, 5, 0.2)])
-def test_traced_sweeps_replay_bit_exact(oracle_mod, gpu_lib, rho, n, seed, dr, lanes):
+@pytest.mark.parametrize("rho,n,seed,dr,edge", [c + (0.0,) for c in CASES] +
+                         [(0.70, 10, 5, 0.2, 0.0), (0.40, 8, 9, 0.3, 1.2), (0.60, 8, 11, 0.25, 1.6)])
+def test_traced_sweeps_replay_bit_exact(oracle_mod, gpu_lib, rho, n, seed, dr, edge, lanes):
+    """Every trial of a few sweeps replayed on the oracle; edge > 0 asks for
+    larger device cells (edges 1.23 and 1.88 here: capacity 16 and 32)."""
     from oracle.philox import TAG_MOVE, draw4
 
-    o, g, conf = fluid(oracle_mod, gpu_lib, rho, n, seed, dr, sweeps=10, lanes=lanes)
+    if edge > 1.41 and lanes == 1:
+        # 32-slot cells with one lane each do not fit a block's shared memory
+        with pytest.raises(gpu_lib.HsmcError) as ei:
+            fluid(oracle_mod, gpu_lib, rho, n, seed, dr, sweeps=0, lanes=lanes, min_edge=edge)
+        assert ei.value.code == 1
+        return
+    o, g, conf = fluid(oracle_mod, gpu_lib, rho, n, seed, dr, sweeps=10, lanes=lanes, min_edge=edge)
+    if edge:
+        nc, _, _, _ = g.grid_info()
+        assert all(g.box[d] / nc[d] >= edge for d in range(3))
     sweeps = 4
     rec, cnt = g.sweeps_traced(sweeps)
     assert len(rec) == o.n * sweeps
@@ -180,6 +193,10 @@ def test_error_paths_report_reference_messages(gpu_lib):
     assert ei.value.code == 4
     g.upload(conf)
     g.sweep_nvt(2)
+    # an NpT run re-derives its grid on the device with the standard edge
+    with pytest.raises(gpu_lib.HsmcError) as ei:
+        gpu_lib.HardSphereSystem(rho=0.5, cells=5, pressure=3.0, dv_max=0.01, min_cell_edge=1.2)
+    assert ei.value.code == 1
 
 
 @pytest.mark.parametrize("lanes", [1, 2, 4, 8])
