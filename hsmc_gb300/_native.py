@@ -97,6 +97,8 @@ def load() -> C.CDLL:
     L.hsmc_gpu_set_schedule.argtypes = [_vp, C.c_int, C.c_int]
     L.hsmc_gpu_get_schedule.argtypes = [_vp, _P(C.c_int), _P(C.c_int)]
     L.hsmc_gpu_hold_region.argtypes = [_vp, C.c_int]
+    L.hsmc_gpu_cluster_moves.argtypes = [_vp, C.c_int, _vp, _vp]
+    L.hsmc_gpu_cluster_move_at.argtypes = [_vp, _vp, C.c_int, C.c_int, _P(C.c_int64)]
     L.hsmc_gpu_last_timing.argtypes = [_vp, _P(C.c_double), _P(C.c_double), _P(C.c_int)]
     _lib = L
     return L

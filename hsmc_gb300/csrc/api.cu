@@ -73,6 +73,11 @@ struct hsmc_ctx {
   int flow_grid = 0;
   int flow_graph = -1;  // -1 untested, 0 no, 1 yes
   uint32_t *prog = nullptr;
+  // cluster moves: queue (N ints), marks (N words), counters, per-move output
+  Scratch cl_queue, cl_mark, cl_ctr, cl_out;
+  unsigned long long cluster_seq = 0;  // cluster moves drawn from the stream so far
+  uint32_t cl_epoch = 0;               // epoch of the last move (marks hold older ones)
+  int cl_grid = 0;
 };
 
 // ----------------------------------------------------------------- helpers
@@ -112,7 +117,7 @@ static int status_to_code(int st) {
   if (st & ST_OUT_OF_BOX) return HSMC_ERR_OUT_OF_BOX;
   if (st & ST_TRACE_FULL) return HSMC_ERR_INVALID_ARG;
   if (st & ST_BAD_CELL) return HSMC_ERR_CELL_OVERFLOW;
-  if (st & ST_FLOW_TIMEOUT) return HSMC_ERR_TIMEOUT;
+  if (st & (ST_FLOW_TIMEOUT | ST_CLUSTER_TIMEOUT)) return HSMC_ERR_TIMEOUT;
   return HSMC_OK;
 }
 
@@ -316,6 +321,10 @@ void hsmc_gpu_destroy(hsmc_ctx *ctx) {
   ctx->qpos.release();
   ctx->qids.release();
   ctx->trace.release();
+  ctx->cl_queue.release();
+  ctx->cl_mark.release();
+  ctx->cl_ctr.release();
+  ctx->cl_out.release();
   if (ctx->ev_start) cudaEventDestroy(ctx->ev_start);
   if (ctx->ev_stop) cudaEventDestroy(ctx->ev_stop);
   for (cudaEvent_t e : ctx->ev_pass) cudaEventDestroy(e);
@@ -862,12 +871,85 @@ int hsmc_gpu_ql(hsmc_ctx *ctx, int l, double rc, double *ql_mean, double *per_pa
   return HSMC_OK;
 }
 
+// Geometric cluster moves (cluster.cu).  Each move is one cooperative
+// launch over the current layout, then the layout is rebuilt in place from
+// the moved positions.
+static int cluster_run(hsmc_ctx *ctx, int n_moves, const double *pivot, int axis, int seed_particle,
+                       int64_t *sizes, double *drawn) {
+  if (!ctx || n_moves < 0 || !ctx->uploaded || ctx->prm.pressure > 0) return HSMC_ERR_INVALID_ARG;
+  if (n_moves == 0) return HSMC_OK;
+  const size_t n = (size_t)ctx->n;
+  if (!ctx->cl_mark.ptr) {
+    HSMC_CUDA(ctx->cl_mark.ensure(sizeof(uint32_t) * n));
+    HSMC_CUDA(cudaMemsetAsync(ctx->cl_mark.ptr, 0, sizeof(uint32_t) * n, ctx->stream));
+    ctx->cl_epoch = 0;
+  }
+  HSMC_CUDA(ctx->cl_queue.ensure(sizeof(int) * n));
+  HSMC_CUDA(ctx->cl_ctr.ensure(sizeof(uint32_t) * 4));
+  const size_t per = sizeof(long long) + 5 * sizeof(double);
+  HSMC_CUDA(ctx->cl_out.ensure(per * (size_t)n_moves));
+  if (ctx->cl_grid == 0) ctx->cl_grid = cluster_grid(ctx->n, ctx->num_sms);
+  long long *d_size = (long long *)ctx->cl_out.ptr;
+  double *d_drawn = (double *)(d_size + n_moves);
+  HSMC_CUDA(cudaMemsetAsync(&ctx->sp.st->status, 0, sizeof(int), ctx->stream));
+  ClusterJob job{};
+  job.queue = (int *)ctx->cl_queue.ptr;
+  job.mark = (uint32_t *)ctx->cl_mark.ptr;
+  job.ctr = (uint32_t *)ctx->cl_ctr.ptr;
+  job.cost = std::cos(M_PI);
+  job.sint = std::sin(M_PI);
+  if (pivot) {
+    job.given = 1;
+    for (int d = 0; d < 3; d++) job.pivot[d] = pivot[d];
+    job.axis = axis;
+    job.seed_id = seed_particle;
+  }
+  for (int k = 0; k < n_moves; k++) {
+    if (++ctx->cl_epoch == 0) {  // marks of 2^32 moves ago could match again
+      HSMC_CUDA(cudaMemsetAsync(ctx->cl_mark.ptr, 0, sizeof(uint32_t) * n, ctx->stream));
+      ctx->cl_epoch = 1;
+    }
+    job.epoch = ctx->cl_epoch;
+    job.seq = ctx->cluster_seq + (unsigned long long)k;
+    job.size_out = d_size + k;
+    job.drawn = d_drawn + 5 * (size_t)k;
+    HSMC_CUDA(cudaMemsetAsync(job.ctr, 0, sizeof(uint32_t) * 4, ctx->stream));
+    HSMC_CUDA(launch_cluster(ctx->sp, job, ctx->cl_grid, ctx->stream));
+    rebuild_current_layout(ctx);
+  }
+  if (!pivot) ctx->cluster_seq += (unsigned long long)n_moves;
+  int e = check_kernels(ctx);
+  if (e) return e;
+  DevState s;
+  if ((e = read_state(ctx, s))) return e;
+  if (s.status) return status_to_code(s.status);
+  if (sizes) {
+    std::vector<long long> h((size_t)n_moves);
+    HSMC_CUDA(cudaMemcpy(h.data(), d_size, sizeof(long long) * (size_t)n_moves, cudaMemcpyDeviceToHost));
+    for (int k = 0; k < n_moves; k++) sizes[k] = (int64_t)h[(size_t)k];
+  }
+  if (drawn) HSMC_CUDA(cudaMemcpy(drawn, d_drawn, sizeof(double) * 5 * (size_t)n_moves, cudaMemcpyDeviceToHost));
+  return HSMC_OK;
+}
+
+int hsmc_gpu_cluster_moves(hsmc_ctx *ctx, int n_moves, int64_t *sizes, double *drawn) {
+  return cluster_run(ctx, n_moves, nullptr, 0, 0, sizes, drawn);
+}
+
+int hsmc_gpu_cluster_move_at(hsmc_ctx *ctx, const double pivot[3], int axis, int seed_particle, int64_t *size) {
+  if (!ctx || !pivot || axis < 0 || axis > 2 || seed_particle < 0 || seed_particle >= ctx->n)
+    return HSMC_ERR_INVALID_ARG;
+  for (int d = 0; d < 3; d++)
+    if (!(pivot[d] >= 0.0 && pivot[d] <= ctx->hbox.len[d])) return HSMC_ERR_INVALID_ARG;
+  return cluster_run(ctx, 1, pivot, axis, seed_particle, size, nullptr);
+}
+
 int hsmc_gpu_rng_state(hsmc_ctx *ctx, uint64_t out[4]) {
   if (!ctx || !out) return HSMC_ERR_INVALID_ARG;
   out[0] = ctx->prm.seed;
   out[1] = ctx->sweep_base;
   out[2] = ctx->widom_seq;
-  out[3] = 0;
+  out[3] = ctx->cluster_seq;
   return HSMC_OK;
 }
 
@@ -876,6 +958,7 @@ int hsmc_gpu_rng_set_state(hsmc_ctx *ctx, const uint64_t st[4]) {
   ctx->prm.seed = st[0];
   ctx->sweep_base = st[1];
   ctx->widom_seq = st[2];
+  ctx->cluster_seq = st[3];
   HSMC_CUDA(cudaMemcpyAsync(&ctx->sp.st->seed, &st[0], sizeof(uint64_t), cudaMemcpyHostToDevice, ctx->stream));
   HSMC_CUDA(cudaMemcpyAsync(&ctx->sp.st->sweep_base, &st[1], sizeof(uint64_t), cudaMemcpyHostToDevice, ctx->stream));
   reset_progress(ctx);

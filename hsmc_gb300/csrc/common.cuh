@@ -45,6 +45,7 @@ enum : uint32_t {
   TAG_PERM = 3u,
   TAG_WIDOM = 4u,
   TAG_VOLUME = 5u,
+  TAG_CLUSTER = 7u,  // 6 is the learned Widom sampler's
 };
 
 __host__ __device__ inline U32x4 draw4(uint64_t seed, uint32_t a, uint32_t b, uint64_t seq, uint32_t tag) {
@@ -178,7 +179,8 @@ enum : int {
   ST_OUT_OF_BOX = 4,
   ST_TRACE_FULL = 8,
   ST_BAD_CELL = 16,
-  ST_FLOW_TIMEOUT = 32,  // a dataflow wait gave up (the sweep's result is invalid)
+  ST_FLOW_TIMEOUT = 32,     // a dataflow wait gave up (the sweep's result is invalid)
+  ST_CLUSTER_TIMEOUT = 64,  // a cluster move's grid-wide wait gave up (its result is invalid)
 };
 
 struct DevState {

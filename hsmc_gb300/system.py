@@ -185,6 +185,26 @@ class HardSphereSystem:
         self._counters += c
         return rec[: got.value].copy(), c
 
+    def cluster_moves(self, n_moves: int, drawn: bool = False):
+        """n_moves geometric cluster moves (cluster_sweep_nvt,
+        src/cluster_nvt.c:221-228); returns the cluster sizes, and with
+        drawn=True also each move's (pivot x, y, z, axis, seed particle)."""
+        sizes = np.zeros(n_moves, dtype=np.int64)
+        d = np.zeros((n_moves, 5), dtype=np.float64) if drawn else None
+        _check(self._lib.hsmc_gpu_cluster_moves(self._h, n_moves, sizes.ctypes.data,
+                                                d.ctypes.data if d is not None else None),
+               "hsmc_gpu_cluster_moves")
+        return (sizes, d) if drawn else sizes
+
+    def cluster_move_at(self, pivot, axis: int, seed_particle: int) -> int:
+        """One cluster move from a given pivot, axis (0, 1, 2) and seed
+        particle; returns its size."""
+        piv = np.ascontiguousarray(pivot, dtype=np.float64)
+        size = C.c_int64(0)
+        _check(self._lib.hsmc_gpu_cluster_move_at(self._h, piv.ctypes.data, int(axis), int(seed_particle),
+                                                  C.byref(size)), "hsmc_gpu_cluster_move_at")
+        return int(size.value)
+
     def get_moves_counters(self) -> np.ndarray:
         return self._counters.copy()
 

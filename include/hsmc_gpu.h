@@ -162,13 +162,39 @@ int hsmc_gpu_ql(hsmc_ctx *ctx, int l, double rc, double *ql_mean, double *per_pa
 /* Random stream position for restart files, replacing the GSL state block of
  * write_restart / read_restart (src/io_config.c:61-62, 115-116):
  * state[0] = seed, state[1] = sweeps done, state[2] = Widom calls done,
- * state[3] = reserved (0). */
+ * state[3] = cluster moves done. */
 int hsmc_gpu_rng_state(hsmc_ctx *ctx, uint64_t out[4]);
 int hsmc_gpu_rng_set_state(hsmc_ctx *ctx, const uint64_t state[4]);
 
 /* Reference message for a status code (the printf text the reference emits
  * before exit(EXIT_FAILURE)); never NULL. */
 const char *hsmc_gpu_strerror(int status);
+
+/* ---------------------------------------------------------- cluster moves
+ * Geometric cluster moves (cluster_move / cluster_move_part / pocket_add,
+ * src/cluster_nvt.c:232-410; Dress & Krauth, J. Phys. A 28, L597, 1995):
+ * a pivot point and a coordinate axis are drawn, and the seed particle is
+ * rotated by pi about the line through the pivot along that axis with the
+ * reference's rotate() arithmetic (src/cluster_nvt.c:342-365, cos and sin of
+ * M_PI as the host's libm gives them), then wrapped once into the box
+ * (apply_pbc).  Every particle that overlaps a moved particle joins the
+ * cluster and is moved the same way, until none overlaps.  The move is
+ * always accepted.  The reference grows the cluster from a randomly ordered
+ * pocket; the device grows it breadth-first over the whole GPU.  Both give
+ * the same set of moved particles and bit-identical positions: the rotation
+ * is an isometry, so a moved particle never overlaps another moved one.
+ *
+ * hsmc_gpu_cluster_moves makes n_moves moves with pivot, axis and seed drawn
+ * from the context's random stream.  sizes (n_moves entries, or NULL)
+ * receives each cluster's size (the reference's cluster_size); drawn
+ * (5 x n_moves doubles, or NULL) receives pivot x, y, z, axis (0 = x, 1 = y,
+ * 2 = z) and seed particle of each move.
+ * hsmc_gpu_cluster_move_at makes one move with the given pivot, axis and
+ * seed particle and does not advance the stream.
+ * Both are NVT only (HSMC_ERR_INVALID_ARG on an NpT context).  A wait of the
+ * device-wide breadth-first search that runs out (1 s) is HSMC_ERR_TIMEOUT. */
+int hsmc_gpu_cluster_moves(hsmc_ctx *ctx, int n_moves, int64_t *sizes, double *drawn);
+int hsmc_gpu_cluster_move_at(hsmc_ctx *ctx, const double pivot[3], int axis, int seed_particle, int64_t *size);
 
 /* ------------------------------------------------------ batched replicas
  * Many independent NVT systems (different N, box and density) advanced

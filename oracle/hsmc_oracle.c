@@ -519,6 +519,112 @@ int hso_sweeps_npt(hso_sim *s, int n) {
   return s->err;
 }
 
+/* ----------------------------------------------------------- cluster moves */
+
+/* rotate (src/cluster_nvt.c:342-365): point (xx, yy, zz) about the line
+ * through (aa, bb, cc) with direction (uu, vv, ww) by theta. */
+static void cluster_rotate(double xx, double yy, double zz, double aa, double bb, double cc, double uu, double vv,
+                           double ww, double theta, double *xr, double *yr, double *zr) {
+  double cost = cos(theta), sint = sin(theta);
+  double uu2 = uu * uu, vv2 = vv * vv, ww2 = ww * ww;
+  *xr = (aa * (vv2 + ww2) - uu * (bb * vv + cc * ww - uu * xx - vv * yy - ww * zz)) * (1 - cost) + xx * cost +
+        (-cc * vv + bb * ww - ww * yy + vv * zz) * sint;
+  *yr = (bb * (uu2 + ww2) - vv * (aa * uu + cc * ww - uu * xx - vv * yy - ww * zz)) * (1 - cost) + yy * cost +
+        (cc * uu - aa * ww + ww * xx - uu * zz) * sint;
+  *zr = (cc * (uu2 + vv2) - ww * (aa * uu + bb * vv - uu * xx - vv * yy - ww * zz)) * (1 - cost) + zz * cost +
+        (-bb * uu + aa * vv - vv * xx + uu * yy) * sint;
+}
+
+/* cluster_move_part (src/cluster_nvt.c:312-339): rotate by pi, wrap, and
+ * follow the particle in the cell list. */
+static void cluster_move_one(hso_sim *s, int id, const double *piv, const double *axis) {
+  double *p = s->conf[id];
+  int c_old = cell_of_particle(s, id);
+  cluster_rotate(p[1], p[2], p[3], piv[0], piv[1], piv[2], axis[0], axis[1], axis[2], M_PI, &p[1], &p[2], &p[3]);
+  wrap_into_box(s, p);
+  int c_new = cell_of_particle(s, id);
+  if (c_new != c_old) {
+    int e = cell_move(s, c_old, c_new, id);
+    if (e) s->err = e;
+  }
+}
+
+/* pocket_add (src/cluster_nvt.c:369-410): every particle of the 27 cells
+ * around the moved one that it overlaps joins the pocket once. */
+static void pocket_grow(hso_sim *s, int id, int *pocket, int *count) {
+  int c = cell_of_particle(s, id);
+  if (c < 0 || c >= s->num_tot) {
+    s->err = HSO_ERR_ARG;
+    return;
+  }
+  const int *nb = s->neigh_mat + (size_t)c * 27;
+  for (int q = 0; q < 27; q++) {
+    const int *r = row(s, nb[q]);
+    for (int j = 1; j <= r[0]; j++) {
+      int other = r[j];
+      double d = pair_dist(s, s->conf[id], s->conf[other], 1.0);
+      if (d < 1.0 && other != id) {
+        int seen = 0;
+        for (int k = 0; k < *count; k++) seen |= pocket[k] == other;
+        if (!seen) pocket[(*count)++] = other;
+      }
+    }
+  }
+}
+
+/* cluster_move (src/cluster_nvt.c:232-310) after its draws: move the seed,
+ * then empty the pocket in random order (pocket_del keeps the survivors in
+ * order, src/cluster_nvt.c:412-431). */
+static int cluster_grow(hso_sim *s, const double *piv, int axis_id, int seed_id) {
+  double axis[3] = {0.0, 0.0, 0.0};
+  axis[axis_id] = 1.0;
+  int *pocket = malloc(sizeof(int) * (size_t)s->n);
+  if (!pocket) {
+    s->err = HSO_ERR_ALLOC;
+    return -1;
+  }
+  int count = 0, size = 1;
+  cluster_move_one(s, seed_id, piv, axis);
+  pocket_grow(s, seed_id, pocket, &count);
+  while (count > 0 && !s->err) {
+    int k = draw_int(s, count);
+    int id = pocket[k];
+    cluster_move_one(s, id, piv, axis);
+    memmove(pocket + k, pocket + k + 1, sizeof(int) * (size_t)(count - k - 1));
+    count--;
+    pocket_grow(s, id, pocket, &count);
+    size++;
+  }
+  free(pocket);
+  return size;
+}
+
+/* One cluster move with the given pivot, axis (0, 1, 2 = x, y, z) and seed
+ * particle; the pocket order still comes from the generator. */
+int hso_cluster_move_at(hso_sim *s, const double *pivot, int axis, int seed_id, int *size) {
+  if (axis < 0 || axis > 2 || seed_id < 0 || seed_id >= s->n) return HSO_ERR_ARG;
+  int k = cluster_grow(s, pivot, axis, seed_id);
+  if (size) *size = k;
+  return s->err;
+}
+
+/* cluster_sweep_nvt (src/cluster_nvt.c:221-228) for n moves with the
+ * reference's draws: pivot u * L per axis, axis rng_get_int(3), seed
+ * rng_get_int(N). */
+int hso_cluster_moves(hso_sim *s, int n, int *sizes) {
+  for (int m = 0; m < n && !s->err; m++) {
+    double piv[3];
+    piv[0] = draw_double(s) * s->lx;
+    piv[1] = draw_double(s) * s->ly;
+    piv[2] = draw_double(s) * s->lz;
+    int axis = draw_int(s, 3);
+    int seed_id = draw_int(s, s->n);
+    int k = cluster_grow(s, piv, axis, seed_id);
+    if (sizes) sizes[m] = k;
+  }
+  return s->err;
+}
+
 /* part_move (src/moves.c:27-80) with u - 0.5 = (2r - 2^32 + 1) * 2^-33 per
  * axis, the step factor the GPU draws; the reference's own code forms the
  * same value from the draw 2r + 1 with maximum 2^33. */

@@ -50,6 +50,10 @@ void hso_counters(const hso_sim *s, unsigned long long *out6);
 void hso_reset_counters(hso_sim *s);
 
 int hso_replay_moves(hso_sim *s, int n, const int *ids, const uint32_t *raw, int *accepted);
+
+/* Geometric cluster moves (src/cluster_nvt.c:221-431). */
+int hso_cluster_move_at(hso_sim *s, const double *pivot, int axis, int seed_id, int *size);
+int hso_cluster_moves(hso_sim *s, int n, int *sizes);
 int hso_replay_moves_offsets(hso_sim *s, int n, const int *ids, const uint32_t *raw, int *accepted);
 int hso_check_overlap_at(hso_sim *s, int i, double x, double y, double z);
 int hso_scan_overlap(hso_sim *s, double sf);

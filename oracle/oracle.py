@@ -196,6 +196,8 @@ class OracleSim(_SimBase):
                                                   _f32p, _f32p, _i32p]
             L.hso_cell_of32.restype = C.c_uint32
             L.hso_cell_of32.argtypes = [C.c_float, C.c_float, C.c_float, C.c_float, C.c_int]
+            L.hso_cluster_move_at.argtypes = [C.c_void_p, _dp, C.c_int, C.c_int, _i32p]
+            L.hso_cluster_moves.argtypes = [C.c_void_p, C.c_int, _i32p]
             cls._lib = L
         return cls._lib
 
@@ -314,6 +316,24 @@ class OracleSim(_SimBase):
         self._lib.hso_opt_nvt(self._h, opt_sweeps, opt_samples, target, C.byref(dr), C.byref(acc))
         return dr.value, acc.value
 
+    def cluster_move_at(self, pivot, axis, seed_id) -> int:
+        """One cluster move (src/cluster_nvt.c:232-310) from the given pivot,
+        axis and seed particle; returns the cluster size."""
+        piv = np.ascontiguousarray(pivot, dtype=np.float64)
+        size = np.zeros(1, dtype=np.int32)
+        e = self._lib.hso_cluster_move_at(self._h, piv, int(axis), int(seed_id), size)
+        if e:
+            raise RuntimeError(f"oracle cluster move failed ({e})")
+        return int(size[0])
+
+    def cluster_moves(self, n):
+        """n cluster moves with the reference's draws; their sizes."""
+        sizes = np.zeros(n, dtype=np.int32)
+        e = self._lib.hso_cluster_moves(self._h, n, sizes)
+        if e:
+            raise RuntimeError(f"oracle cluster moves failed ({e})")
+        return sizes
+
     def replay_checkerboard(self, ids, raw, cells, shift32, nc, len32, inv_w32):
         ids = np.ascontiguousarray(ids, dtype=np.int32)
         raw = np.ascontiguousarray(raw, dtype=np.uint32).reshape(-1)
@@ -394,6 +414,8 @@ class RefSim(_SimBase):
             L.ref_ql.argtypes = [C.c_int, C.c_double, _dp, C.POINTER(C.c_double)]
             L.ref_rng_raw.argtypes = [C.c_ulong, C.c_int, _u32p]
             L.ref_rng_uniform_int.argtypes = [C.c_ulong, C.c_ulong, C.c_int, _i32p]
+            L.ref_cluster_moves.argtypes = [C.c_int, _i32p]
+            L.ref_cluster_move_at.argtypes = [_dp, C.c_int, C.c_int]
             cls._lib = L
         return cls._lib
 
@@ -455,6 +477,14 @@ class RefSim(_SimBase):
     def vol_move_replay(self, raw) -> int:
         raw = np.ascontiguousarray(raw, dtype=np.uint32)
         return self._lib.ref_vol_move_replay(raw, raw.size)
+
+    def cluster_moves(self, n):
+        sizes = np.zeros(n, dtype=np.int32)
+        self._lib.ref_cluster_moves(n, sizes)
+        return sizes
+
+    def cluster_move_at(self, pivot, axis, seed_id) -> int:
+        return self._lib.ref_cluster_move_at(np.ascontiguousarray(pivot, dtype=np.float64), int(axis), int(seed_id))
 
     def _lib_rdf(self, *a):
         return self._lib.ref_rdf_counts(*a)

@@ -33,6 +33,7 @@
 #include "compute_press.h"
 #include "compute_widom_chem_pot.h"
 #include "compute_order_parameter.h"
+#include "cluster_nvt.h"
 #include "gsl/gsl_rng.h"
 
 /* Globalised statics of the reference objects. */
@@ -48,6 +49,7 @@ extern int wtest;
 extern double ql_ave;
 extern double *ql;
 extern unsigned long r_num_max;
+extern int cluster_size;
 
 void global_ql_compute();
 void ql_alloc();
@@ -129,6 +131,39 @@ void ref_counters(unsigned long *out) {
 }
 
 void ref_reset_counters(void) { reset_moves_counters(); }
+
+/* n calls of cluster_move() (src/cluster_nvt.c:232-310) with the generator;
+ * sizes[k] receives the reference's cluster_size after call k. */
+void ref_cluster_moves(int n, int *sizes) {
+  for (int k = 0; k < n; k++) {
+    cluster_move();
+    if (sizes) sizes[k] = cluster_size;
+  }
+}
+
+/* The body of cluster_move after its draws, through the reference's own
+ * cluster_move_part, pocket_add and pocket_del, for a given pivot, axis and
+ * seed particle; the pocket order comes from the generator.  Returns the
+ * cluster size. */
+int ref_cluster_move_at(const double *pivot, int axis, int seed_id) {
+  double u[3] = {0.0, 0.0, 0.0};
+  u[axis] = 1.0;
+  int n = part_info_get().NN;
+  int *pocket = malloc(sizeof(int) * (size_t)n);
+  for (int i = 0; i < n; i++) pocket[i] = -1;
+  int count = 0, size = 1;
+  cluster_move_part(seed_id, pivot[0], pivot[1], pivot[2], u[0], u[1], u[2]);
+  pocket_add(seed_id, pocket, &count);
+  while (count > 0) {
+    int id = pocket[rng_get_int(count)];
+    cluster_move_part(id, pivot[0], pivot[1], pivot[2], u[0], u[1], u[2]);
+    pocket_del(id, pocket, &count);
+    pocket_add(id, pocket, &count);
+    size++;
+  }
+  free(pocket);
+  return size;
+}
 
 /* Run part_move() once per entry with scripted draws: ids[k] is returned by
  * rng_get_int and raw[3k..3k+2] by the three rng_get_double calls.
