@@ -77,7 +77,7 @@ struct hsmc_ctx {
   Scratch cl_queue, cl_mark, cl_ctr, cl_out;
   unsigned long long cluster_seq = 0;  // cluster moves drawn from the stream so far
   uint32_t cl_epoch = 0;               // epoch of the last move (marks hold older ones)
-  int cl_grid = 0;
+  int cl_grid = -1;  // -1 not chosen yet, 0 the one-block shared-memory kernel
 };
 
 // ----------------------------------------------------------------- helpers
@@ -871,9 +871,8 @@ int hsmc_gpu_ql(hsmc_ctx *ctx, int l, double rc, double *ql_mean, double *per_pa
   return HSMC_OK;
 }
 
-// Geometric cluster moves (cluster.cu).  Each move is one cooperative
-// launch over the current layout, then the layout is rebuilt in place from
-// the moved positions.
+// Geometric cluster moves (cluster.cu): one cooperative launch makes the
+// moves one after the other and rebuilds the current layout after each.
 static int cluster_run(hsmc_ctx *ctx, int n_moves, const double *pivot, int axis, int seed_particle,
                        int64_t *sizes, double *drawn) {
   if (!ctx || n_moves < 0 || !ctx->uploaded || ctx->prm.pressure > 0) return HSMC_ERR_INVALID_ARG;
@@ -888,7 +887,7 @@ static int cluster_run(hsmc_ctx *ctx, int n_moves, const double *pivot, int axis
   HSMC_CUDA(ctx->cl_ctr.ensure(sizeof(uint32_t) * 4));
   const size_t per = sizeof(long long) + 5 * sizeof(double);
   HSMC_CUDA(ctx->cl_out.ensure(per * (size_t)n_moves));
-  if (ctx->cl_grid == 0) ctx->cl_grid = cluster_grid(ctx->n, ctx->num_sms);
+  if (ctx->cl_grid < 0) ctx->cl_grid = cluster_grid(ctx->n, ctx->hbox.ncell, ctx->num_sms);
   long long *d_size = (long long *)ctx->cl_out.ptr;
   double *d_drawn = (double *)(d_size + n_moves);
   HSMC_CUDA(cudaMemsetAsync(&ctx->sp.st->status, 0, sizeof(int), ctx->stream));
@@ -896,27 +895,28 @@ static int cluster_run(hsmc_ctx *ctx, int n_moves, const double *pivot, int axis
   job.queue = (int *)ctx->cl_queue.ptr;
   job.mark = (uint32_t *)ctx->cl_mark.ptr;
   job.ctr = (uint32_t *)ctx->cl_ctr.ptr;
-  job.cost = std::cos(M_PI);
   job.sint = std::sin(M_PI);
+  if (std::cos(M_PI) != -1.0) return HSMC_ERR_INVALID_ARG;  // the folded rotation assumes it
   if (pivot) {
     job.given = 1;
     for (int d = 0; d < 3; d++) job.pivot[d] = pivot[d];
     job.axis = axis;
     job.seed_id = seed_particle;
   }
-  for (int k = 0; k < n_moves; k++) {
-    if (++ctx->cl_epoch == 0) {  // marks of 2^32 moves ago could match again
-      HSMC_CUDA(cudaMemsetAsync(ctx->cl_mark.ptr, 0, sizeof(uint32_t) * n, ctx->stream));
-      ctx->cl_epoch = 1;
-    }
-    job.epoch = ctx->cl_epoch;
-    job.seq = ctx->cluster_seq + (unsigned long long)k;
-    job.size_out = d_size + k;
-    job.drawn = d_drawn + 5 * (size_t)k;
-    HSMC_CUDA(cudaMemsetAsync(job.ctr, 0, sizeof(uint32_t) * 4, ctx->stream));
-    HSMC_CUDA(launch_cluster(ctx->sp, job, ctx->cl_grid, ctx->stream));
-    rebuild_current_layout(ctx);
+  // epochs cl_epoch + 1 .. cl_epoch + n_moves; marks are cleared before the
+  // counter could come round to an epoch an old mark still holds
+  if ((unsigned long long)ctx->cl_epoch + (unsigned long long)n_moves > 0xFFFFFFFFull) {
+    HSMC_CUDA(cudaMemsetAsync(ctx->cl_mark.ptr, 0, sizeof(uint32_t) * n, ctx->stream));
+    ctx->cl_epoch = 0;
   }
+  job.epoch = ctx->cl_epoch + 1u;
+  job.seq = ctx->cluster_seq;
+  job.size_out = d_size;
+  job.drawn = d_drawn;
+  HSMC_CUDA(cudaMemsetAsync(job.ctr, 0, sizeof(uint32_t) * 4, ctx->stream));
+  HSMC_CUDA(launch_cluster(ctx->sp, job, n_moves, ctx->cl_grid, ctx->hbox.ncell, ctx->stream));
+  if (ctx->cl_grid == 0) rebuild_current_layout(ctx);  // the one-block kernel moved only the positions
+  else ctx->cl_epoch += (uint32_t)n_moves;
   if (!pivot) ctx->cluster_seq += (unsigned long long)n_moves;
   int e = check_kernels(ctx);
   if (e) return e;

@@ -85,22 +85,26 @@ void launch_advance_batch(const SysPtrs *reps, int n_reps, int n_sweeps, cudaStr
 void launch_pair_hist_batch(const SysPtrs *reps, int n_reps, int max_n, double bin, double rmax, int nbins,
                             unsigned long long *counts, cudaStream_t s);
 
-// cluster.cu: one geometric cluster move (cooperative launch of `grid`
-// blocks; ctr[0..3] must be zero at launch)
+// cluster.cu: n_moves geometric cluster moves in one cooperative launch of
+// `grid` blocks, each followed by a rebuild of the current layout
+// (ctr[3] must be zero at launch)
 struct ClusterJob {
   int *queue;                // n entries: the cluster, level by level
   uint32_t *mark;            // n words: epoch of the move that took each particle
   uint32_t *ctr;             // [0..2] particles found per level (rotating), [3] barrier arrivals
-  long long *size_out;       // the cluster's size
-  double *drawn;             // pivot x, y, z, axis, seed particle; or nullptr
-  double pivot[3];           // used when `given`
-  double cost, sint;         // cos(M_PI) and sin(M_PI) of the host libm
-  unsigned long long seq;    // index of the move in the context's stream
-  uint32_t epoch;            // nonzero, different from every mark left by earlier moves
+  long long *size_out;       // n_moves cluster sizes
+  double *drawn;             // 5 x n_moves: pivot x, y, z, axis, seed particle; or nullptr
+  double pivot[3];           // used when `given` (then n_moves = 1)
+  double sint;               // sin(M_PI) of the host libm (its cos(M_PI) is -1)
+  unsigned long long seq;    // index of the first move in the context's stream
+  uint32_t epoch;            // first move's epoch; epoch .. epoch + n_moves - 1 match no mark
   int axis, seed_id, given;
 };
-int cluster_grid(int n, int num_sms);
-cudaError_t launch_cluster(const SysPtrs &p, const ClusterJob &job, int grid, cudaStream_t s);
+// grid 0: the whole system fits one block's shared memory (k_cluster_small);
+// its launch leaves the cell layout to the caller
+int cluster_grid(int n, int ncell, int num_sms);
+cudaError_t launch_cluster(const SysPtrs &p, const ClusterJob &job, int n_moves, int grid, int ncell,
+                           cudaStream_t s);
 
 // observables.cu
 void launch_pair_hist(const SysPtrs &p, double bin, double rmax, int nbins, unsigned long long *counts,

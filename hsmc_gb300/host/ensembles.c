@@ -1,8 +1,8 @@
 /*
  * Ensemble drivers of the drop-in program: hs_nvt / run_nvt
- * (src/nvt.c:30-199), hs_npt / run_npt (src/npt.c:25-175) and the
- * displacement optimiser (src/optimizer.c:23-166), with the sweeps on the
- * device.  Sampling happens before the sweep of the same index, as in the
+ * (src/nvt.c:30-199), hs_npt / run_npt (src/npt.c:25-175), cluster_hs_nvt /
+ * cluster_run_nvt (src/cluster_nvt.c:31-218) and the displacement optimiser
+ * (src/optimizer.c:23-166), with the sweeps on the device.  Sampling happens before the sweep of the same index, as in the
  * reference; consecutive sweeps with nothing to sample between them go to
  * the device as one call.
  */
@@ -210,6 +210,77 @@ void host_nvt(host_run *r) {
     host_gpu_upload(r);
   }
   simulate(r, false);
+}
+
+/* n cluster sweeps of cluster_moves_sweep moves each (cluster_sweep_nvt,
+ * src/cluster_nvt.c:221-228); *last receives the size of the last cluster. */
+static void cluster_sweeps(host_run *r, int n, int *last) {
+  long long total = (long long)n * r->in.cluster_moves_sweep;
+  const long long chunk = 1 << 16;
+  int64_t *sizes = malloc(sizeof(int64_t) * (size_t)(total < chunk ? (total > 0 ? total : 1) : chunk));
+  while (total > 0) {
+    const int k = (int)(total < chunk ? total : chunk);
+    host_gpu_check(hsmc_gpu_cluster_moves(r->gpu, k, sizes, NULL), "cluster moves");
+    *last = (int)sizes[k - 1];
+    total -= k;
+  }
+  free(sizes);
+}
+
+static void cluster_block(host_run *r, bool prod, int offset, int *last) {
+  const host_input *in = &r->in;
+  if (in->output_int <= 0) {
+    printf("ERROR: the output interval (keyword out) must be positive\n");
+    exit(EXIT_FAILURE);
+  }
+  int n = prod ? in->sweep_stat : in->sweep_eq;
+  host_obs_state obs;
+  host_obs_begin(&obs);
+  int pending = 0;
+  for (int ii = offset; ii < n + offset; ii++) {
+    if (ii % in->output_int == 0 || sampling_due(in, ii, prod, false)) {
+      cluster_sweeps(r, pending, last);
+      pending = 0;
+    }
+    if (ii == offset) printf("Sweep number, cluster size\n ");
+    if (ii % in->output_int == 0) {
+      printf("%d %d\n", ii, *last);
+      fflush(stdout);
+    }
+    if (every(ii, in->restart_write)) host_write_restart(r, ii);
+    if (prod) {
+      if (every(ii, in->config_write)) host_write_config(r, ii);
+      if (every(ii, in->pressv_sample_int)) host_compute_pressv(r, &obs);
+      if (every(ii, in->presst_sample_int)) host_compute_presst(r, &obs);
+      if (every(ii, in->ql_sample_int)) host_compute_op(r, &obs);
+      if (every(ii, in->mu_sample_int)) host_compute_mu(r, &obs);
+      if (every(ii, in->rdf_sample_int)) host_compute_rdf(r, &obs, ii);
+    }
+    pending++;
+  }
+  cluster_sweeps(r, pending, last);
+}
+
+void host_cluster(host_run *r) {
+  start_system(r);
+  double t0 = wall_seconds();
+  host_reset_counters(r);
+  /* local sweeps so that a perfect crystal is not rotated */
+  host_sweeps(r, r->in.cluster_init_step, false);
+  int last = 0;
+  printf("---------------------------------------------------\n");
+  printf("Equilibration...\n");
+  cluster_block(r, false, 0, &last);
+  printf("Equilibration completed.\n");
+  printf("---------------------------------------------------\n");
+  printf("Production...\n");
+  cluster_block(r, true, r->in.sweep_eq, &last);
+  printf("Production completed.\n");
+  printf("Elapsed time: %f seconds\n", wall_seconds() - t0);
+  hsmc_gpu_destroy(r->gpu);
+  r->gpu = NULL;
+  free(r->conf);
+  r->conf = NULL;
 }
 
 void host_npt(host_run *r) {

@@ -118,5 +118,6 @@ void host_write_config(host_run *r, int sweep);
 /* ensembles.c */
 void host_nvt(host_run *r);
 void host_npt(host_run *r);
+void host_cluster(host_run *r);
 
 #endif

@@ -1,8 +1,9 @@
 /*
  * hsmc: the reference's command line (src/exec.c:28-145) over the GB300
  * engine.  -i/--input IN_FILE (default in.dat), -e/--example, -o/--output
- * OUT_FILE; dispatch on the input: NpT when npt > 0, else NVT.  Cavity and
- * cluster ensembles are not part of this engine and are refused.
+ * OUT_FILE; dispatch on the input as the reference does: NpT when npt > 0,
+ * else cavity sampling when cavity > 0 (refused: not part of this engine),
+ * else cluster moves when cluster is set, else NVT.
  */
 #include <getopt.h>
 #include <stdbool.h>
@@ -56,9 +57,11 @@ int main(int argc, char **argv) {
     host_read_input(&run.in, input);
     if (run.in.press > 0) {
       host_npt(&run);
-    } else if (run.in.cavity_pcav > 0 || run.in.cluster_flag > 0) {
-      printf("ERROR: cavity and cluster-move simulations are not provided by this engine\n");
+    } else if (run.in.cavity_pcav > 0) {
+      printf("ERROR: cavity simulations are not provided by this engine\n");
       exit(EXIT_FAILURE);
+    } else if (run.in.cluster_flag > 0) {
+      host_cluster(&run);
     } else {
       host_nvt(&run);
     }

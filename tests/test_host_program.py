@@ -47,10 +47,11 @@ def test_malformed_input_matches_reference(hsmc_exe, tmp_path, name, text):
 
 
 _NUM = re.compile(r"[-+]?\d+\.\d+(e[-+]\d+)?|[-+]?\d+e[-+]\d+")
+_SWEEP_SIZE = re.compile(r"^(\s*\d+) \d+$")  # "sweep cluster-size" progress lines
 
 
 def _mask(line):
-    return _NUM.sub("#", line)
+    return _NUM.sub("#", _SWEEP_SIZE.sub(r"\1 #", line))
 
 
 def _read(path):
@@ -70,7 +71,7 @@ def _run(hsmc_exe, tmp_path, case):
 
 
 @pytest.mark.gpu
-@pytest.mark.parametrize("case", ["nvt_small", "npt_small"])
+@pytest.mark.parametrize("case", ["nvt_small", "npt_small", "cluster_small"])
 def test_run_matches_reference_files(hsmc_exe, tmp_path, case):
     out = _run(hsmc_exe, tmp_path, case)
     gold = os.path.join(GOLD, case)
