@@ -542,6 +542,79 @@ def run_npt(args):
     return 0
 
 
+def run_cluster(args):
+    """Geometric cluster moves (src/cluster_nvt.c): the reference's own
+    comparison, N = 256 at packing fractions 0.25 and 0.30 with cluster moves
+    only (cluster moves/s, and the virial pressure in 10 blocks against
+    Carnahan-Starling); and N = 256,000 at 0.25 (particles moved per second).
+    Times are host wall-clock around the synchronous library calls.  CPU
+    baseline: the oracle's pocket algorithm (the reference's, restated) on one
+    host core, on the same N = 256 system and on N = 32,000."""
+    import numpy as np
+    from hsmc_gb300 import HardSphereSystem
+    from hsmc_gb300.batch import carnahan_starling, contact_z
+
+    small = []
+    for k, eta in enumerate((0.25, 0.30)):
+        rho = 6.0 * eta / math.pi
+        g = HardSphereSystem(rho=rho, cells=4, dr_max=0.4, seed=500 + k)
+        g.sweep_nvt(1000)  # cluster_init_step: melt the lattice with local moves
+        g.cluster_moves(1000)
+        nb, bin_ = 5, 0.01
+        blocks, per_block, every = 10, 400, 5
+        z, t, moves, moved = [], 0.0, 0, 0
+        for _ in range(blocks):
+            cnt = np.zeros(nb)
+            for _ in range(per_block):
+                t0 = time.perf_counter()
+                sz = g.cluster_moves(every)
+                t += time.perf_counter() - t0
+                moves += every
+                moved += int(sz.sum())
+                cnt += g.compute_pressv_counts(bin_, 1.0 + nb * bin_, nb)
+            z.append(contact_z(cnt, per_block, g.n, rho, bin_))
+        z = np.array(z)
+        small.append({"packing_fraction": eta, "N": g.n, "cluster_moves_per_s": moves / t,
+                      "mean_cluster_size": moved / moves, "pressure": float(rho * z.mean()),
+                      "pressure_se": float(rho * z.std(ddof=1) / math.sqrt(blocks)),
+                      "pressure_cs": float(rho * carnahan_starling(rho)), "moves": moves})
+    rho = 6.0 * 0.25 / math.pi
+    g = HardSphereSystem(rho=rho, cells=40, dr_max=0.4, seed=77)
+    g.sweep_nvt(200)
+    g.cluster_moves(20)
+    t0 = time.perf_counter()
+    sz = g.cluster_moves(200)
+    t_big = time.perf_counter() - t0
+    line = {
+        "metric": "particles moved/s by cluster moves, N=256000 packing fraction 0.25",
+        "value": float(sz.sum()) / t_big, "unit": "particles/s", "n_gpus": 1, "higher_is_better": True,
+        "dtype": "f64", "data": "synthetic (FCC start melted by local sweeps)",
+        "config": {"workload": "geometric cluster moves only; N=256 at packing fractions 0.25 and 0.30 "
+                               "(the reference's own comparison), and N=256000 at 0.25",
+                   "timing": "host wall-clock around synchronous calls"},
+        "large": {"N": g.n, "cluster_moves_per_s": 200 / t_big, "mean_cluster_size": float(sz.mean())},
+        "small": small,
+    }
+    if not args.no_cpu_baseline:
+        from oracle.oracle import OracleSim
+
+        cpu = {}
+        for label, ncell, budget in (("N256", 4, 5.0), ("N32000", 20, 8.0)):
+            o = OracleSim(rho=rho, n_cells=ncell, seed=3, dr_max=0.4, neigh_dr=1.05)
+            o.sweeps_nvt(100)
+            t0, k, tot = time.perf_counter(), 0, 0
+            while time.perf_counter() - t0 < budget:
+                tot += int(o.cluster_moves(1)[0])
+                k += 1
+            dt = time.perf_counter() - t0
+            cpu[label] = {"cluster_moves_per_s": k / dt, "particles_per_s": tot / dt, "moves": k}
+        line["cpu_baseline"] = {"value": cpu["N32000"]["particles_per_s"], "unit": "particles/s", "cores": 1,
+                                "kind": "port", "sample": "oracle pocket algorithm, packing fraction 0.25: "
+                                "N=32000 (value) and N=256, about 5-8 s each", "detail": cpu}
+    print(json.dumps(line), flush=True)
+    return 0
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -549,7 +622,7 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
-    ap.add_argument("--workload", default="fluid", choices=["fluid", "replicas", "widom", "npt"])
+    ap.add_argument("--workload", default="fluid", choices=["fluid", "replicas", "widom", "npt", "cluster"])
     ap.add_argument("--replicas", type=int, default=512)
     ap.add_argument("--cell-edge", default="0",
                     help='replicas: smallest device-cell edge, a number or "auto" (min(rho^-1/3, 1.4))')
@@ -567,6 +640,8 @@ def main():
         return run_widom(args)
     if args.workload == "npt":
         return run_npt(args)
+    if args.workload == "cluster":
+        return run_cluster(args)
     return run_gpu_arm(args)
 
 

@@ -272,12 +272,15 @@ __global__ void __launch_bounds__(512) k_cluster(SysPtrs p, ClusterJob job, int 
 }
 
 // ------------------------------------------------ small systems, one block
-// The whole system in shared memory: FP64 positions, a cell list by counting
-// sort (start offsets + ids), marks and the queue.  The same moves as
+// The whole system in shared memory: FP64 positions and their FP32 roundings
+// (the screen and the cell index read only these, so a level's FP64 work is
+// the image of each particle), a cell list by counting sort (start offsets +
+// ids), marks and the queue.  The same moves as
 // k_cluster (same draws, same set, same images), with shared-memory latency
 // instead of L2 round trips between the dependent steps of a level.
 struct SmallSm {
   double *x, *y, *z;
+  float *x32, *y32, *z32;
   uint32_t *mark, *start, *fill;
   uint16_t *ids, *queue;
   uint32_t *pc;  // [0..2] rotating level counters, [3] scan carry
@@ -288,7 +291,10 @@ __device__ __forceinline__ SmallSm small_sm(unsigned char *raw, int n, int ncell
   m.x = reinterpret_cast<double *>(raw);
   m.y = m.x + n;
   m.z = m.y + n;
-  m.mark = reinterpret_cast<uint32_t *>(m.z + n);
+  m.x32 = reinterpret_cast<float *>(m.z + n);
+  m.y32 = m.x32 + n;
+  m.z32 = m.y32 + n;
+  m.mark = reinterpret_cast<uint32_t *>(m.z32 + n);
   m.start = m.mark + n;
   m.fill = m.start + (ncell + 1);
   m.pc = m.fill + ncell;
@@ -297,12 +303,12 @@ __device__ __forceinline__ SmallSm small_sm(unsigned char *raw, int n, int ncell
   return m;
 }
 
-__device__ __forceinline__ int small_cell(const Box *bx, double x, double y, double z) {
+__device__ __forceinline__ int small_cell(const Box *bx, float x, float y, float z) {
   int c[3];
   float t;
-  axis_cell(__double2float_rn(x), 0.0f, bx->len32[0], bx->inv_w32[0], bx->nc[0], c[0], t);
-  axis_cell(__double2float_rn(y), 0.0f, bx->len32[1], bx->inv_w32[1], bx->nc[1], c[1], t);
-  axis_cell(__double2float_rn(z), 0.0f, bx->len32[2], bx->inv_w32[2], bx->nc[2], c[2], t);
+  axis_cell(x, 0.0f, bx->len32[0], bx->inv_w32[0], bx->nc[0], c[0], t);
+  axis_cell(y, 0.0f, bx->len32[1], bx->inv_w32[1], bx->nc[1], c[1], t);
+  axis_cell(z, 0.0f, bx->len32[2], bx->inv_w32[2], bx->nc[2], c[2], t);
   return c[0] + bx->nc[0] * (c[1] + bx->nc[1] * c[2]);
 }
 
@@ -311,7 +317,7 @@ __device__ void small_cells(const SmallSm &m, const Box *bx, int n, int ncell) {
   const int tid = (int)threadIdx.x, nt = (int)blockDim.x;
   for (int c = tid; c < ncell; c += nt) m.fill[c] = 0u;
   __syncthreads();
-  for (int i = tid; i < n; i += nt) atomicAdd(m.fill + small_cell(bx, m.x[i], m.y[i], m.z[i]), 1u);
+  for (int i = tid; i < n; i += nt) atomicAdd(m.fill + small_cell(bx, m.x32[i], m.y32[i], m.z32[i]), 1u);
   __syncthreads();
   // exclusive scan of fill into start: a contiguous chunk per thread, then
   // a block scan of the chunk sums
@@ -349,7 +355,7 @@ __device__ void small_cells(const SmallSm &m, const Box *bx, int n, int ncell) {
   for (int c = tid; c < ncell; c += nt) m.fill[c] = 0u;
   __syncthreads();
   for (int i = tid; i < n; i += nt) {
-    const int c = small_cell(bx, m.x[i], m.y[i], m.z[i]);
+    const int c = small_cell(bx, m.x32[i], m.y32[i], m.z32[i]);
     const uint32_t k = atomicAdd(m.fill + c, 1u);
     m.ids[m.start[c] + k] = (uint16_t)i;
   }
@@ -377,6 +383,9 @@ __global__ void __launch_bounds__(512) k_cluster_small(SysPtrs p, ClusterJob job
     m.x[i] = x;
     m.y[i] = y;
     m.z[i] = z;
+    m.x32[i] = __double2float_rn(x);
+    m.y32[i] = __double2float_rn(y);
+    m.z32[i] = __double2float_rn(z);
     m.mark[i] = 0u;
   }
   __syncthreads();
@@ -428,30 +437,32 @@ __global__ void __launch_bounds__(512) k_cluster_small(SysPtrs p, ClusterJob job
         px = wrap_once(px, len[0]);
         py = wrap_once(py, len[1]);
         pz = wrap_once(pz, len[2]);
+        const float px32 = __double2float_rn(px), py32 = __double2float_rn(py), pz32 = __double2float_rn(pz);
         __syncwarp();
         if (lane == 0) {
           m.x[i] = px;
           m.y[i] = py;
           m.z[i] = pz;
+          m.x32[i] = px32;
+          m.y32[i] = py32;
+          m.z32[i] = pz32;
         }
         if (lane < 27) {
           int ci[3];
           float t;
-          axis_cell(__double2float_rn(px), 0.0f, bx->len32[0], bx->inv_w32[0], nc0, ci[0], t);
-          axis_cell(__double2float_rn(py), 0.0f, bx->len32[1], bx->inv_w32[1], nc1, ci[1], t);
-          axis_cell(__double2float_rn(pz), 0.0f, bx->len32[2], bx->inv_w32[2], nc2, ci[2], t);
+          axis_cell(px32, 0.0f, bx->len32[0], bx->inv_w32[0], nc0, ci[0], t);
+          axis_cell(py32, 0.0f, bx->len32[1], bx->inv_w32[1], nc1, ci[1], t);
+          axis_cell(pz32, 0.0f, bx->len32[2], bx->inv_w32[2], nc2, ci[2], t);
           int cx = ci[0] + ox, cy = ci[1] + oy, cz = ci[2] + oz;
           cx = cx < 0 ? cx + nc0 : (cx >= nc0 ? cx - nc0 : cx);
           cy = cy < 0 ? cy + nc1 : (cy >= nc1 ? cy - nc1 : cy);
           cz = cz < 0 ? cz + nc2 : (cz >= nc2 ? cz - nc2 : cz);
           const int c = cx + nc0 * (cy + nc1 * cz);
           const uint32_t q1 = m.start[c + 1];
-          const float px32 = __double2float_rn(px), py32 = __double2float_rn(py), pz32 = __double2float_rn(pz);
           for (uint32_t q = m.start[c]; q < q1; q++) {
             const int j = m.ids[q];
             if (j == i || m.mark[j] == epoch) continue;
-            const float r2 = screen_r2(px32, py32, pz32, __double2float_rn(m.x[j]), __double2float_rn(m.y[j]),
-                                       __double2float_rn(m.z[j]), bx->len32);
+            const float r2 = screen_r2(px32, py32, pz32, m.x32[j], m.y32[j], m.z32[j], bx->len32);
             if (r2 > 1.0f + band) continue;
             // pocket_add: compute_dist(moved, other) < 1.0 (src/cluster_nvt.c:371-410), in
             // FP64 when the single-precision value is within the guard band of 1
@@ -484,7 +495,8 @@ __global__ void __launch_bounds__(512) k_cluster_small(SysPtrs p, ClusterJob job
 
 size_t cluster_small_smem(int n, int ncell) {
   if (n > 65535) return 0;
-  const size_t bytes = 32 * (size_t)n + 8 * (size_t)ncell + 4 + 16 + 2 * (size_t)n;
+  // x, y, z (FP64 and FP32), mark, ids, queue per particle; start, fill per cell
+  const size_t bytes = 44 * (size_t)n + 8 * (size_t)ncell + 4 + 16;
   return bytes <= 200 * 1024 ? bytes : 0;
 }
 
