@@ -27,6 +27,7 @@ STATUS_NAMES = {
     7: "HSMC_ERR_TIMEOUT",
     8: "HSMC_ERR_OUT_OF_BOX",
     9: "HSMC_ERR_OVERLAP",
+    10: "HSMC_ERR_CAVITY_RANGE",
 }
 
 
@@ -44,6 +45,9 @@ class HsmcParams(C.Structure):
         ("cell_capacity", C.c_int),
         ("lanes_per_cell", C.c_int),
         ("min_cell_edge", C.c_double),
+        ("cavity_pcav", C.c_double),
+        ("cavity_maxdr", C.c_double),
+        ("cavity_mindr", C.c_double),
         ("reserved", C.c_int * 4),
     ]
 
@@ -98,6 +102,9 @@ def load() -> C.CDLL:
     L.hsmc_gpu_get_schedule.argtypes = [_vp, _P(C.c_int), _P(C.c_int)]
     L.hsmc_gpu_hold_region.argtypes = [_vp, C.c_int]
     L.hsmc_gpu_cluster_moves.argtypes = [_vp, C.c_int, _vp, _vp]
+    L.hsmc_gpu_cavity_psi.argtypes = [_vp, _vp, C.c_int, _vp]
+    L.hsmc_gpu_cavity_trace.argtypes = [_vp, C.c_int64]
+    L.hsmc_gpu_cavity_trace_read.argtypes = [_vp, _vp, C.c_int64, _P(C.c_int64)]
     L.hsmc_gpu_cluster_move_at.argtypes = [_vp, _vp, C.c_int, C.c_int, _P(C.c_int64)]
     L.hsmc_gpu_last_timing.argtypes = [_vp, _P(C.c_double), _P(C.c_double), _P(C.c_int)]
     _lib = L

@@ -24,7 +24,7 @@ LIB = os.path.join(PKG, "libhsmc_gpu.so")
 BIN_DIR = os.path.join(PKG, "bin")
 EXE = os.path.join(BIN_DIR, "hsmc")
 
-CU_SOURCES = ["api.cu", "sweep.cu", "move_pass.cu", "observables.cu", "batch.cu", "lwidom.cu", "cluster.cu"]
+CU_SOURCES = ["api.cu", "sweep.cu", "move_pass.cu", "observables.cu", "batch.cu", "lwidom.cu", "cluster.cu", "cavity.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-Xcompiler", "-O2",
               "--expt-relaxed-constexpr", "-I" + os.path.join(ROOT, "include")]
@@ -49,6 +49,18 @@ def _headers() -> list[str]:
     return hs + [os.path.join(ROOT, "include", "hsmc_gpu.h")]
 
 
+C_SOURCES = ["cavity_coeffs.c"]  # host C (C99 complex arithmetic), compiled by gcc
+
+
+def _compile_c(src: str) -> str:
+    obj = os.path.join(OBJ, os.path.basename(src).replace(".c", "_c.o"))
+    if _newer(obj, [src] + _headers()):
+        return obj
+    subprocess.run(["gcc", "-O2", "-std=gnu99", "-ffp-contract=off", "-fPIC", "-Wall", "-c", src, "-o", obj],
+                   check=True)
+    return obj
+
+
 def _compile(src: str, verbose_ptxas: bool) -> str:
     obj = os.path.join(OBJ, os.path.basename(src).replace(".cu", ".o"))
     if _newer(obj, [src] + _headers()) and not verbose_ptxas:
@@ -68,8 +80,9 @@ def build_library(verbose_ptxas: bool = False) -> str:
     srcs = [os.path.join(CSRC, s) for s in CU_SOURCES]
     with cf.ThreadPoolExecutor(max_workers=len(srcs)) as ex:
         objs = list(ex.map(lambda s: _compile(s, verbose_ptxas), srcs))
+    objs += [_compile_c(os.path.join(CSRC, s)) for s in C_SOURCES]
     if not _newer(LIB, objs):
-        cmd = [nvcc()] + ARCH + ["-shared", "-o", LIB] + objs + ["-lcudart"]
+        cmd = [nvcc()] + ARCH + ["-shared", "-o", LIB] + objs + ["-lcudart", "-lm"]
         subprocess.run(cmd, check=True)
     return LIB
 

@@ -78,6 +78,10 @@ struct hsmc_ctx {
   unsigned long long cluster_seq = 0;  // cluster moves drawn from the stream so far
   uint32_t cl_epoch = 0;               // epoch of the last move (marks hold older ones)
   int cl_grid = -1;  // -1 not chosen yet, 0 the one-block shared-memory kernel
+  // cavity sampling: on when the context was created with cavity_pcav > 0
+  bool cavity = false;
+  Scratch cav_trace;
+  long long cav_trace_cap = 0;
 };
 
 // ----------------------------------------------------------------- helpers
@@ -118,6 +122,7 @@ static int status_to_code(int st) {
   if (st & ST_TRACE_FULL) return HSMC_ERR_INVALID_ARG;
   if (st & ST_BAD_CELL) return HSMC_ERR_CELL_OVERFLOW;
   if (st & (ST_FLOW_TIMEOUT | ST_CLUSTER_TIMEOUT)) return HSMC_ERR_TIMEOUT;
+  if (st & ST_CAVITY_RANGE) return HSMC_ERR_CAVITY_RANGE;
   return HSMC_OK;
 }
 
@@ -199,6 +204,7 @@ const char *hsmc_gpu_strerror(int status) {
     case HSMC_ERR_TIMEOUT: return "ERROR: device wait timed out";
     case HSMC_ERR_OUT_OF_BOX: return "ERROR: coordinate outside the simulation box";
     case HSMC_ERR_OVERLAP: return "Overlap in the initial configuration";
+    case HSMC_ERR_CAVITY_RANGE: return "Error, the cavities are too close or too far apart!";
     default: return "ERROR: unknown status";
   }
 }
@@ -213,6 +219,11 @@ int hsmc_gpu_create(const hsmc_params *prm, hsmc_ctx **out) {
     if (!(prm->dr_max < prm->box[d])) return HSMC_ERR_INVALID_ARG;
   // the device re-derives an NpT grid with the standard edge only
   if (!(prm->min_cell_edge >= 0.0) || (prm->min_cell_edge > 0.0 && prm->pressure > 0)) return HSMC_ERR_INVALID_ARG;
+  const bool cavity = prm->cavity_pcav > 0;
+  if (!(prm->cavity_pcav >= 0.0) || prm->cavity_pcav > 1.0) return HSMC_ERR_INVALID_ARG;
+  if (cavity && (prm->pressure > 0 || prm->n_particles < 3 || !(prm->cavity_mindr >= 0.0) ||
+                 !(prm->cavity_maxdr > prm->cavity_mindr)))
+    return HSMC_ERR_INVALID_ARG;
   int dev = 0;
   if (cudaGetDevice(&dev) != cudaSuccess) return HSMC_ERR_NO_DEVICE;
   cudaDeviceProp p{};
@@ -238,6 +249,8 @@ int hsmc_gpu_create(const hsmc_params *prm, hsmc_ctx **out) {
     if (prm->cell_capacity > 32) return HSMC_ERR_INVALID_ARG;
     cap = prm->cell_capacity <= 8 ? 8 : (prm->cell_capacity <= 16 ? 16 : 32);
   }
+  // the two cavities may overlap each other: one more sphere than geometry allows
+  if (cavity && cap < 16) cap = 16;
 
   prepare_move_pass();
   hsmc_ctx *ctx = new hsmc_ctx();
@@ -286,6 +299,14 @@ int hsmc_gpu_create(const hsmc_params *prm, hsmc_ctx **out) {
   s0.seed = prm->seed;
   s0.per_cell = prm->lattice_type == 1 ? 1 : 4;
   s0.flow_hold = -1;
+  if (cavity) {
+    s0.frozen = 2;
+    const long long k = std::llround((double)prm->n_particles * prm->cavity_pcav);
+    s0.cav_trials = (int)(k < 1 ? 1 : k);
+    s0.cav_min = prm->cavity_mindr;
+    s0.cav_max = prm->cavity_maxdr;
+    hsmc_cavity_coeffs(prm->rho > 0 ? prm->rho : rho, &s0.psi);
+  }
   for (int d = 0; d < 3; d++) {
     s0.cells[d] = prm->cells[d];
     s0.nc_alloc[d] = balloc.nc[d];
@@ -297,6 +318,7 @@ int hsmc_gpu_create(const hsmc_params *prm, hsmc_ctx **out) {
   if ((ce = cudaMalloc(&ctx->prog, sizeof(uint32_t) * (size_t)(sp.ncell_alloc / 8 + 1))) != cudaSuccess)
     return fail(ce);
   ctx->flow = false;  // one launch per pass unless hsmc_gpu_set_schedule or the autotuner picks the dataflow sweep
+  ctx->cavity = cavity;
   *out = ctx;
   return HSMC_OK;
 }
@@ -325,6 +347,7 @@ void hsmc_gpu_destroy(hsmc_ctx *ctx) {
   ctx->cl_mark.release();
   ctx->cl_ctr.release();
   ctx->cl_out.release();
+  ctx->cav_trace.release();
   if (ctx->ev_start) cudaEventDestroy(ctx->ev_start);
   if (ctx->ev_stop) cudaEventDestroy(ctx->ev_stop);
   for (cudaEvent_t e : ctx->ev_pass) cudaEventDestroy(e);
@@ -401,10 +424,18 @@ static cudaError_t enqueue_moves(hsmc_ctx *ctx, bool trace) {
   return cudaSuccess;
 }
 
+// The cavity stage of a sweep (cavity.cu), after its colour passes.
+static void enqueue_cavity(hsmc_ctx *ctx, long long offset) {
+  if (ctx->cavity)
+    launch_cavity(ctx->sp, offset, ctx->cav_trace_cap > 0 ? (uint32_t *)ctx->cav_trace.ptr : nullptr,
+                  ctx->cav_trace_cap, ctx->stream);
+}
+
 static cudaError_t enqueue_sweep(hsmc_ctx *ctx, long long offset, bool trace, bool npt) {
   launch_build(ctx->sp, offset, ctx->num_sms, ctx->stream);
   cudaError_t e = enqueue_moves(ctx, trace);
   if (npt) launch_volume_move(ctx->sp, offset, ctx->margin, ctx->stream);
+  enqueue_cavity(ctx, offset);
   return e;
 }
 
@@ -456,7 +487,7 @@ static int run_sweeps(hsmc_ctx *ctx, int n_sweeps, bool trace, bool npt, uint64_
   HSMC_CUDA(cudaMemsetAsync(&ctx->sp.st->status, 0, sizeof(int), ctx->stream));
   ctx->last_move_ms = 0.0;
   ctx->last_move_launches = 0;
-  bool direct = trace || ctx->profiling;
+  bool direct = trace || ctx->profiling || ctx->cav_trace_cap > 0;  // graphs hold no trace buffers
   if (!direct) {
     int e = ensure_graph(ctx, npt);
     if (e) return e;
@@ -495,11 +526,13 @@ static int run_sweeps(hsmc_ctx *ctx, int n_sweeps, bool trace, bool npt, uint64_
       }
     }
     if (npt) launch_volume_move(ctx->sp, s, ctx->margin, ctx->stream);
+    enqueue_cavity(ctx, s);
   }
   if (rest > 0) launch_advance(ctx->sp, rest, ctx->stream);
   HSMC_CUDA(cudaEventRecord(ctx->ev_stop, ctx->stream));
   ctx->sweep_base += (unsigned long long)n_sweeps;
-  if (npt && n_sweeps > 0) rebuild_current_layout(ctx);
+  // volume and cavity moves leave the last layout behind the positions
+  if ((npt || ctx->cavity) && n_sweeps > 0) rebuild_current_layout(ctx);
   int e = check_kernels(ctx);
   if (e) return e;
   float ms = 0.f;
@@ -522,10 +555,10 @@ static int run_sweeps(hsmc_ctx *ctx, int n_sweeps, bool trace, bool npt, uint64_
     HSMC_CUDA(cudaMemcpy(&ctx->hbox, ctx->sp.box, sizeof(Box), cudaMemcpyDeviceToHost));
   }
   if (counters) {
-    const uint64_t moves = (uint64_t)ctx->n * (uint64_t)n_sweeps;
+    const uint64_t moves = (uint64_t)ctx->n * (uint64_t)n_sweeps + s.cav_moves;
     counters[HSMC_CNT_MOVES] = moves;
-    counters[HSMC_CNT_ACCEPTED] = s.acc;
-    counters[HSMC_CNT_REJECTED] = moves - s.acc;
+    counters[HSMC_CNT_ACCEPTED] = s.acc + s.cav_acc;
+    counters[HSMC_CNT_REJECTED] = moves - s.acc - s.cav_acc;
     counters[HSMC_CNT_VOL_MOVES] = s.vol_moves;
     counters[HSMC_CNT_VOL_ACCEPTED] = s.vol_acc;
     counters[HSMC_CNT_VOL_REJECTED] = s.vol_moves - s.vol_acc;
@@ -930,6 +963,38 @@ static int cluster_run(hsmc_ctx *ctx, int n_moves, const double *pivot, int axis
   }
   if (drawn) HSMC_CUDA(cudaMemcpy(drawn, d_drawn, sizeof(double) * 5 * (size_t)n_moves, cudaMemcpyDeviceToHost));
   return HSMC_OK;
+}
+
+int hsmc_gpu_cavity_psi(hsmc_ctx *ctx, const double *x, int n, double *out) {
+  if (!ctx || n < 0 || (n > 0 && (!x || !out)) || !ctx->cavity) return HSMC_ERR_INVALID_ARG;
+  if (n == 0) return HSMC_OK;
+  HSMC_CUDA(ctx->qpos.ensure(sizeof(double) * 2 * (size_t)n));
+  double *d = (double *)ctx->qpos.ptr;
+  HSMC_CUDA(cudaMemcpyAsync(d, x, sizeof(double) * (size_t)n, cudaMemcpyHostToDevice, ctx->stream));
+  launch_cavity_psi(ctx->sp, d, n, d + n, ctx->stream);
+  HSMC_CUDA(cudaMemcpyAsync(out, d + n, sizeof(double) * (size_t)n, cudaMemcpyDeviceToHost, ctx->stream));
+  return check_kernels(ctx);
+}
+
+int hsmc_gpu_cavity_trace(hsmc_ctx *ctx, int64_t capacity) {
+  if (!ctx || capacity < 0 || !ctx->cavity) return HSMC_ERR_INVALID_ARG;
+  if (capacity > 0) HSMC_CUDA(ctx->cav_trace.ensure(32 * (size_t)capacity));
+  ctx->cav_trace_cap = capacity;
+  HSMC_CUDA(cudaMemsetAsync(&ctx->sp.st->cav_trace_count, 0, sizeof(unsigned long long), ctx->stream));
+  return check_kernels(ctx);
+}
+
+int hsmc_gpu_cavity_trace_read(hsmc_ctx *ctx, uint32_t *rec, int64_t capacity, int64_t *n_rec) {
+  if (!ctx || !n_rec || capacity < 0 || (capacity > 0 && !rec) || !ctx->cavity) return HSMC_ERR_INVALID_ARG;
+  unsigned long long count = 0;
+  HSMC_CUDA(cudaMemcpy(&count, &ctx->sp.st->cav_trace_count, sizeof(count), cudaMemcpyDeviceToHost));
+  long long k = (long long)count;
+  if (k > ctx->cav_trace_cap) k = ctx->cav_trace_cap;
+  if (k > capacity) k = capacity;
+  if (k > 0) HSMC_CUDA(cudaMemcpy(rec, ctx->cav_trace.ptr, 32 * (size_t)k, cudaMemcpyDeviceToHost));
+  *n_rec = k;
+  HSMC_CUDA(cudaMemsetAsync(&ctx->sp.st->cav_trace_count, 0, sizeof(unsigned long long), ctx->stream));
+  return check_kernels(ctx);
 }
 
 int hsmc_gpu_cluster_moves(hsmc_ctx *ctx, int n_moves, int64_t *sizes, double *drawn) {

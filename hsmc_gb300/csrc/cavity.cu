@@ -1,0 +1,178 @@
+// Cavity sampling (cavity_part_move / cavity_check_move, src/moves.c:254-396)
+// on the device: the cavity stage of each sweep of a cavity run.
+//
+// Particles 0 and 1 are the two cavities.  The colour passes leave them in
+// place (move_pass.cu, DevState::frozen); after the passes of a sweep one warp
+// makes the sweep's cavity trials one after the other, because each depends
+// on where the previous one left the pair:
+//   - a cavity (one bit of the draw) is displaced as in part_move;
+//   - the move is rejected when the new distance between the cavities leaves
+//     [cav_min, cav_max], or by the Metropolis test on the umbrella potential
+//     psi = ln y_GH against a uniform, or when the moved cavity overlaps a
+//     particle other than the cavities (lane k of the warp tests neighbour
+//     cell k of the 27, single precision outside the guard band, the
+//     reference's FP64 distance inside it).
+// The other particles do not move during the stage, so the sweep's cell
+// layout still holds them; the cavities' own entries in it are not used.
+#include "cellview.cuh"
+
+namespace hsmc {
+
+namespace {
+
+// psi(x) = lny_gh(x, pi rho / 6, 1) (src/analytic.c:34-54): the
+// Grundke-Henderson cubic inside the core, ln g_VW outside, with g_VW the
+// Percus-Yevick g at x / dW plus a damped oscillation (rdf_vw and rdf_py,
+// src/analytic.c:79-99, 143-170), in the reference's operation order.
+__device__ double cavity_psi(const hsmc_cavity_psi_coeffs &c, double x) {
+  if (x < 1.0) {
+    return __dadd_rn(__dadd_rn(__dadd_rn(c.ay[0], __dmul_rn(c.ay[1], x)), __dmul_rn(__dmul_rn(c.ay[2], x), x)),
+                     __dmul_rn(__dmul_rn(__dmul_rn(c.ay[3], x), x), x));
+  }
+  const double d = __dsub_rn(x, 1.0);
+  const double osc =
+      __dmul_rn(__dmul_rn(__ddiv_rn(c.AA, x), exp(__dmul_rn(-c.mu, d))), cos(__dmul_rn(c.mu, d)));
+  // Re sum_k a_k exp(t_k (x / dW - 1)), divided by x / dW
+  const double xh = __ddiv_rn(x, c.dW);
+  const double dh = __dsub_rn(xh, 1.0);
+  double re = 0.0;
+#pragma unroll
+  for (int k = 0; k < 3; k++) {
+    const double mag = exp(__dmul_rn(c.t_re[k], dh));
+    double sn, cs;
+    sincos(__dmul_rn(c.t_im[k], dh), &sn, &cs);
+    const double er = __dmul_rn(mag, cs), ei = __dmul_rn(mag, sn);
+    const double term = __dsub_rn(__dmul_rn(c.a_re[k], er), __dmul_rn(c.a_im[k], ei));
+    re = k == 0 ? term : __dadd_rn(re, term);
+  }
+  const double g_py = __ddiv_rn(re, xh);
+  return log(__dadd_rn(g_py, osc));
+}
+
+__global__ void k_cavity_psi(const DevState *st, const double *x, int n, double *out) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) out[i] = cavity_psi(st->psi, x[i]);
+}
+
+// The cavity trials of sweep sweep_base + offset (one warp).
+__global__ void __launch_bounds__(32) k_cavity(SysPtrs p, long long offset, uint32_t *trace, long long trace_cap) {
+  DevState *st = p.st;
+  const int trials = st->cav_trials;
+  const unsigned long long s = st->sweep_base + (unsigned long long)offset;
+  const unsigned long long seed = st->seed;
+  const CellView v = current_view(p);
+  const Box *bx = p.box;
+  double len[3], half[3];
+  for (int d = 0; d < 3; d++) {
+    len[d] = bx->len[d];
+    half[d] = bx->half[d];
+  }
+  const float band = bx->band;
+  const double dr = st->dr_max, cmin = st->cav_min, cmax = st->cav_max;
+  const int lane = (int)threadIdx.x;
+  const int ox = lane % 3 - 1, oy = (lane / 3) % 3 - 1, oz = lane / 9 - 1;
+  double cav[2][3];
+  for (int w = 0; w < 2; w++) load_xyz(p.pos, w, cav[w][0], cav[w][1], cav[w][2]);
+  unsigned long long done = 0, acc = 0;
+  for (int k = 0; k < trials; k++) {
+    const U32x4 r1 = draw4(seed, (uint32_t)k, 0u, s, TAG_CAVITY);
+    const U32x4 r2 = draw4(seed, (uint32_t)k, 1u, s, TAG_CAVITY);
+    const int w = (int)(r1.x >> 31);
+    // compute_dist(0, 1) before the move: it must lie in the allowed range
+    const double d_old = sqrt(ref_r2(cav[0][0], cav[0][1], cav[0][2], cav[1][0], cav[1][1], cav[1][2], len, half));
+    if (d_old < cmin || d_old > cmax) {
+      if (lane == 0) atomicOr(&st->status, ST_CAVITY_RANGE);
+      break;
+    }
+    const double en_old = cavity_psi(st->psi, d_old);
+    double nw[3];
+    nw[0] = propose_axis(cav[w][0], centred_offset(r1.y), dr, len[0]);
+    nw[1] = propose_axis(cav[w][1], centred_offset(r1.z), dr, len[1]);
+    nw[2] = propose_axis(cav[w][2], centred_offset(r1.w), dr, len[2]);
+    const double *c0 = w == 0 ? nw : cav[0];
+    const double *c1 = w == 1 ? nw : cav[1];
+    const double d_new = sqrt(ref_r2(c0[0], c0[1], c0[2], c1[0], c1[1], c1[2], len, half));
+    int decision;
+    if (d_new < cmin || d_new > cmax) {
+      decision = 1;
+    } else if (open_unit(r2.x) > exp(-(cavity_psi(st->psi, d_new) - en_old))) {
+      decision = 2;
+    } else {
+      bool ov = false;
+      if (lane < 27) {
+        int ci[3];
+        float t[3];
+        axis_cell(__double2float_rn(nw[0]), v.sh[0], v.L32[0], v.iw[0], v.nc[0], ci[0], t[0]);
+        axis_cell(__double2float_rn(nw[1]), v.sh[1], v.L32[1], v.iw[1], v.nc[1], ci[1], t[1]);
+        axis_cell(__double2float_rn(nw[2]), v.sh[2], v.L32[2], v.iw[2], v.nc[2], ci[2], t[2]);
+        int cx = ci[0] + ox, cy = ci[1] + oy, cz = ci[2] + oz;
+        cx = cx < 0 ? cx + v.nc[0] : (cx >= v.nc[0] ? cx - v.nc[0] : cx);
+        cy = cy < 0 ? cy + v.nc[1] : (cy >= v.nc[1] ? cy - v.nc[1] : cy);
+        cz = cz < 0 ? cz + v.nc[2] : (cz >= v.nc[2] ? cz - v.nc[2] : cz);
+        const int c = cx + v.nc[0] * (cy + v.nc[1] * cz);
+        const int m = v.cnt[c];
+        const int nq = m < v.cap ? m : v.cap;
+        const Slot *sl = v.slot + (size_t)c * v.cap;
+        for (int q = 0; q < nq && !ov; q++) {
+          const Slot o = sl[q];
+          if (o.id < 2) continue;  // the cavities do not overlap each other
+          const float r2f = approx_r2(t[0], t[1], t[2], o, v.L32);
+          if (r2f > 1.0f + band) continue;
+          if (r2f < 1.0f - band) {
+            ov = true;
+          } else {
+            double px, py, pz;
+            load_xyz(p.pos, o.id, px, py, pz);
+            ov = ref_r2(nw[0], nw[1], nw[2], px, py, pz, len, half) < 1.0;
+          }
+        }
+      }
+      decision = __any_sync(0xffffffffu, ov) ? 3 : 0;
+    }
+    if (decision == 0) {
+      for (int d = 0; d < 3; d++) cav[w][d] = nw[d];
+      if (lane == 0) {
+        double *q = p.pos + 4 * (size_t)w;
+        q[1] = nw[0];
+        q[2] = nw[1];
+        q[3] = nw[2];
+      }
+      acc++;
+    }
+    done++;
+    if (trace && lane == 0) {
+      const unsigned long long at = atomicAdd(&st->cav_trace_count, 1ull);
+      if (at < (unsigned long long)trace_cap) {
+        uint32_t *rec = trace + 8 * at;
+        rec[0] = (uint32_t)s;
+        rec[1] = (uint32_t)k;
+        rec[2] = (uint32_t)w;
+        rec[3] = r1.y;
+        rec[4] = r1.z;
+        rec[5] = r1.w;
+        rec[6] = r2.x;
+        rec[7] = (uint32_t)decision;
+      } else {
+        atomicOr(&st->status, ST_TRACE_FULL);
+      }
+    }
+    __syncwarp();
+  }
+  if (lane == 0) {
+    atomicAdd(&st->cav_moves, done);
+    atomicAdd(&st->cav_acc, acc);
+  }
+}
+
+}  // namespace
+
+void launch_cavity(const SysPtrs &p, long long sweep_offset, uint32_t *trace, long long trace_cap,
+                   cudaStream_t s) {
+  k_cavity<<<1, 32, 0, s>>>(p, sweep_offset, trace, trace_cap);
+}
+
+void launch_cavity_psi(const SysPtrs &p, const double *x, int n, double *out, cudaStream_t s) {
+  if (n > 0) k_cavity_psi<<<(n + 127) / 128, 128, 0, s>>>(p.st, x, n, out);
+}
+
+}  // namespace hsmc

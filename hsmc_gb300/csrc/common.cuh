@@ -6,6 +6,8 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include "cavity_coeffs.h"
+
 namespace hsmc {
 
 // ---------------------------------------------------------------- Philox
@@ -46,6 +48,7 @@ enum : uint32_t {
   TAG_WIDOM = 4u,
   TAG_VOLUME = 5u,
   TAG_CLUSTER = 7u,  // 6 is the learned Widom sampler's
+  TAG_CAVITY = 8u,
 };
 
 __host__ __device__ inline U32x4 draw4(uint64_t seed, uint32_t a, uint32_t b, uint64_t seq, uint32_t tag) {
@@ -181,6 +184,7 @@ enum : int {
   ST_BAD_CELL = 16,
   ST_FLOW_TIMEOUT = 32,     // a dataflow wait gave up (the sweep's result is invalid)
   ST_CLUSTER_TIMEOUT = 64,  // a cluster move's grid-wide wait gave up (its result is invalid)
+  ST_CAVITY_RANGE = 128,    // the cavities' distance was outside the allowed range before a cavity move
 };
 
 struct DevState {
@@ -193,8 +197,10 @@ struct DevState {
   unsigned long long trace_count;
   unsigned long long widom_ok;
   unsigned long long scan_mask[4];  // thermodynamic-pressure overlap bits
+  unsigned long long cav_moves, cav_acc;  // cavity trials and acceptances
   double dr_max, dv_max, pressure;
   unsigned long long seed;
+  unsigned long long cav_trace_count;  // cavity-trial records since the last read
   int status;
   int pad;
   SweepParams params;
@@ -205,6 +211,12 @@ struct DevState {
   int cells[3], per_cell;
   int nc_alloc[3];
   int flow_hold;  // dataflow schedule: a region that does not publish (diagnostic), -1 for none
+  // cavity sampling: particles below `frozen` (the two cavities) are left in
+  // place by the colour passes and moved by k_cavity, cav_trials per sweep
+  int frozen;
+  int cav_trials;
+  double cav_min, cav_max;
+  hsmc_cavity_psi_coeffs psi;
 };
 
 // One particle in a cell: its grid coordinates t (single precision, from

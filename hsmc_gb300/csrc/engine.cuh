@@ -106,6 +106,11 @@ int cluster_grid(int n, int ncell, int num_sms);
 cudaError_t launch_cluster(const SysPtrs &p, const ClusterJob &job, int n_moves, int grid, int ncell,
                            cudaStream_t s);
 
+// cavity.cu: the cavity trials of sweep sweep_base + offset (trace: 8 words
+// per trial or nullptr), and psi at n distances
+void launch_cavity(const SysPtrs &p, long long sweep_offset, uint32_t *trace, long long trace_cap, cudaStream_t s);
+void launch_cavity_psi(const SysPtrs &p, const double *x, int n, double *out, cudaStream_t s);
+
 // observables.cu
 void launch_pair_hist(const SysPtrs &p, double bin, double rmax, int nbins, unsigned long long *counts,
                       int stencil[3], cudaStream_t s);

@@ -106,6 +106,7 @@ struct PassEnv {
   float L32[3], iw[3], sh[3];
   int nc[3];
   float lo, hi;
+  int frozen;  // particles below this id stay in place (the cavities of a cavity run)
   uint32_t rep;
   uint32_t *trace;
   unsigned long long trace_cap;
@@ -275,8 +276,11 @@ __device__ __forceinline__ void move_cell(const PassEnv &e, const PassSm &m, int
     axis_cell(__double2float_rn(ny), e.sh[1], e.L32[1], e.iw[1], nc[1], c1, uy);
     axis_cell(__double2float_rn(nz), e.sh[2], e.L32[2], e.iw[2], nc[2], c2, uz);
     const unsigned rc_before = t.rechecks;
+    const int moving_id = __float_as_int(m.own_t[js * GPB + gl].w);
     int decision;
-    if (c0 != ix || c1 != iy || c2 != iz) {
+    if (moving_id < e.frozen) {
+      decision = 4;  // a cavity: moved by the cavity stage, not here
+    } else if (c0 != ix || c1 != iy || c2 != iz) {
       decision = 2;  // the move would leave the active cell
     } else {
       bool ov = false;
@@ -368,7 +372,6 @@ __device__ __forceinline__ void move_cell(const PassEnv &e, const PassSm &m, int
       if (G > 1) ov = __ballot_sync(gmask, ov) != 0u;
       decision = ov ? 1 : 0;
     }
-    const int moving_id = __float_as_int(m.own_t[js * GPB + gl].w);
     if (decision == 0) {
       if (G > 1) __syncwarp(gmask);  // every lane has read this trial's records
       if (lane == 0) {
@@ -456,6 +459,7 @@ __device__ __forceinline__ PassEnv pass_env(const SysPtrs &p, uint32_t rep, int 
   }
   e.lo = 1.0f - bx->band;
   e.hi = 1.0f + bx->band;
+  e.frozen = st->frozen;
   e.rep = rep;
   e.trace = p.trace;
   e.trace_cap = p.trace_cap;

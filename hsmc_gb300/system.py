@@ -50,6 +50,22 @@ def box_from_lattice(rho: float, cells, lattice_type: int = 2):
     return box, vol, cell_size
 
 
+def cavity_start(conf: np.ndarray, box, maxdr: float, mindr: float) -> np.ndarray:
+    """cavity_set_distance (src/cavity_nvt.c:172-186): particle 1 moved onto
+    particle 0, shifted along z by (maxdr + mindr) / 2 with one periodic wrap."""
+    conf = np.array(conf, dtype=np.float64, copy=True)
+    ave = (maxdr + mindr) / 2.0
+    conf[1, 1] = conf[0, 1]
+    conf[1, 2] = conf[0, 2]
+    z = conf[0, 3] + ave
+    if z > box[2]:
+        z -= box[2]
+    elif z < 0.0:
+        z += box[2]
+    conf[1, 3] = z
+    return conf
+
+
 def lattice_config(rho: float, cells, lattice_type: int = 2) -> np.ndarray:
     """part_init_sc / part_init_fcc (src/sim_info.c:120-156) as double[N][4]
     rows (id, x, y, z) in the reference's order."""
@@ -81,7 +97,7 @@ class HardSphereSystem:
 
     def __init__(self, rho: float, cells, lattice_type: int = 2, dr_max: float = 0.05, dv_max: float = 0.001,
                  pressure: float = 0.0, seed: int = 0, conf: np.ndarray | None = None, cell_capacity: int = 0,
-                 box=None, lanes_per_cell: int = 0, min_cell_edge: float = 0.0):
+                 box=None, lanes_per_cell: int = 0, min_cell_edge: float = 0.0, cavity=None):
         lib = _native.load()
         self._lib = lib
         if np.isscalar(cells):
@@ -97,6 +113,8 @@ class HardSphereSystem:
         self.vol = vol
         if conf is None:
             conf = lattice_config(rho, self.cells, lattice_type)
+            if cavity is not None:
+                conf = cavity_start(conf, self.box, cavity[1], cavity[2])
         conf = np.ascontiguousarray(conf, dtype=np.float64)
         self.n = conf.shape[0]
         p = _native.HsmcParams()
@@ -113,6 +131,9 @@ class HardSphereSystem:
         p.cell_capacity = cell_capacity
         p.lanes_per_cell = lanes_per_cell
         p.min_cell_edge = min_cell_edge
+        if cavity is not None:  # (p_cav, maxdr, mindr), the keyword "cavity" of the reference
+            p.cavity_pcav, p.cavity_maxdr, p.cavity_mindr = (float(v) for v in cavity)
+        self.cavity = cavity
         h = C.c_void_p()
         _check(lib.hsmc_gpu_create(C.byref(p), C.byref(h)), "hsmc_gpu_create")
         self._h = h
@@ -204,6 +225,35 @@ class HardSphereSystem:
         _check(self._lib.hsmc_gpu_cluster_move_at(self._h, piv.ctypes.data, int(axis), int(seed_particle),
                                                   C.byref(size)), "hsmc_gpu_cluster_move_at")
         return int(size.value)
+
+    def cavity_psi(self, x) -> np.ndarray:
+        """The umbrella potential psi(x) = ln y_GH(x) of a cavity run, as the
+        device evaluates it (cavity_interaction, src/moves.c:434-440)."""
+        x = np.ascontiguousarray(x, dtype=np.float64)
+        out = np.zeros_like(x)
+        _check(self._lib.hsmc_gpu_cavity_psi(self._h, x.ctypes.data, x.size, out.ctypes.data),
+               "hsmc_gpu_cavity_psi")
+        return out
+
+    def cavity_trace(self, capacity: int) -> None:
+        _check(self._lib.hsmc_gpu_cavity_trace(self._h, capacity), "hsmc_gpu_cavity_trace")
+        self._cav_cap = capacity
+
+    def cavity_trace_read(self) -> np.ndarray:
+        cap = max(getattr(self, "_cav_cap", 0), 1)
+        rec = np.zeros((cap, 8), dtype=np.uint32)
+        got = C.c_int64(0)
+        _check(self._lib.hsmc_gpu_cavity_trace_read(self._h, rec.ctypes.data, cap, C.byref(got)),
+               "hsmc_gpu_cavity_trace_read")
+        return rec[: got.value].copy()
+
+    def cavity_distance(self) -> float:
+        """compute_dist(0, 1) of the reference (src/moves.c:400-431)."""
+        c = self.download()
+        d = c[0, 1:] - c[1, 1:]
+        L = np.array(self.box)
+        d = np.where(d > L / 2, d - L, np.where(d < -L / 2, d + L, d))
+        return float(np.sqrt(d[0] * d[0] + d[1] * d[1] + d[2] * d[2]))
 
     def get_moves_counters(self) -> np.ndarray:
         return self._counters.copy()

@@ -40,7 +40,9 @@ enum hsmc_status {
   HSMC_ERR_BAD_BIN = 6,       /* a pair fell outside its histogram (r < 1: overlapping input) */
   HSMC_ERR_TIMEOUT = 7,       /* a bounded device wait gave up */
   HSMC_ERR_OUT_OF_BOX = 8,    /* a coordinate outside [0, L] on upload */
-  HSMC_ERR_OVERLAP = 9        /* the configuration contains an overlapping pair */
+  HSMC_ERR_OVERLAP = 9,       /* the configuration contains an overlapping pair */
+  HSMC_ERR_CAVITY_RANGE = 10  /* the cavities' distance left [cavity_mindr, cavity_maxdr]
+                                 before a cavity move (src/moves.c:288-297) */
 };
 
 typedef struct hsmc_ctx hsmc_ctx;
@@ -66,6 +68,10 @@ typedef struct {
                            margin).  Larger cells hold more spheres each; for a sparse fluid an
                            edge near rho^(-1/3) spreads the per-cell cost over about one sphere.
                            Part of the chain's definition, like the seed. */
+  double cavity_pcav;   /* cavity sampling (keyword "cavity", src/cavity_nvt.c): > 0 turns it on;
+                           NVT only.  Particles 0 and 1 are the cavities; see hsmc_gpu_sweeps */
+  double cavity_maxdr;  /* largest and smallest allowed distance between the cavities */
+  double cavity_mindr;
   int reserved[4];
 } hsmc_params;
 
@@ -169,6 +175,33 @@ int hsmc_gpu_rng_set_state(hsmc_ctx *ctx, const uint64_t state[4]);
 /* Reference message for a status code (the printf text the reference emits
  * before exit(EXIT_FAILURE)); never NULL. */
 const char *hsmc_gpu_strerror(int status);
+
+/* --------------------------------------------------------- cavity sampling
+ * Torrie-Patey cavity simulations (cavity_hs_nvt, cavity_part_move,
+ * cavity_check_move; src/cavity_nvt.c, src/moves.c:254-440).  A context
+ * created with cavity_pcav > 0 treats particles 0 and 1 as the cavities:
+ * they overlap nothing but each other's umbrella potential
+ * psi(r) = ln y_GH(r) (Grundke-Henderson over Verlet-Weis and Percus-Yevick,
+ * src/analytic.c:34-230, at packing fraction pi rho / 6), and every other
+ * particle treats them as hard spheres.  Each sweep of hsmc_gpu_sweeps is the
+ * checkerboard sweep of the other particles (a trial that picks a cavity
+ * leaves it in place) followed by round(N * cavity_pcav) cavity trials in
+ * sequence, each accepted with probability min(1, exp(-(psi(r') - psi(r))))
+ * when the new distance lies in [cavity_mindr, cavity_maxdr] and the moved
+ * cavity overlaps no other particle.  The uniforms are the context's
+ * counter-based stream; psi uses the device's FP64 exp, cos, sin and log.
+ * The move counters include the cavity trials.
+ *
+ * hsmc_gpu_cavity_psi evaluates psi at n distances on the device (the
+ * values the moves use).  hsmc_gpu_cavity_trace starts (capacity > 0) or
+ * stops (0) recording every cavity trial of the following sweeps, 8 words
+ * each: sweep (low 32 bits), trial, cavity, the three step draws, the
+ * acceptance draw, decision (0 accepted, 1 out of the distance range, 2
+ * rejected by the Metropolis test, 3 overlap); hsmc_gpu_cavity_trace_read
+ * copies the records out and clears them. */
+int hsmc_gpu_cavity_psi(hsmc_ctx *ctx, const double *x, int n, double *out);
+int hsmc_gpu_cavity_trace(hsmc_ctx *ctx, int64_t capacity);
+int hsmc_gpu_cavity_trace_read(hsmc_ctx *ctx, uint32_t *rec, int64_t capacity, int64_t *n_rec);
 
 /* ---------------------------------------------------------- cluster moves
  * Geometric cluster moves (cluster_move / cluster_move_part / pocket_add,

@@ -9,6 +9,7 @@
  */
 #include "hsmc_oracle.h"
 
+#include <complex.h>
 #include <math.h>
 #include <stdio.h>
 #include <stdlib.h>
@@ -57,6 +58,14 @@ typedef struct {
   size_t int_n, int_pos;
 } hso_script;
 
+/* Coefficients of the Grundke-Henderson cavity function over the
+ * Verlet-Weis g(r) and the Percus-Yevick solution (src/analytic.c:23-31). */
+typedef struct {
+  double ay0, ay1, ay2, ay3;
+  double AA, mu, etaW, dW;
+  double complex t0, t1, t2, a00, a01, a02;
+} hso_psi;
+
 struct hso_sim {
   /* input (src/read_input.h:4-71 subset) */
   double rho;
@@ -81,6 +90,9 @@ struct hso_sim {
   unsigned long long moves, acc, rej, vmoves, vacc, vrej;
   /* persistent observable state (file statics of the reference) */
   double pressv_rmax;
+  /* cavity sampling (src/read_input.c:82-86) and its potential */
+  double pcav, cav_min, cav_max;
+  hso_psi psi;
   int err;
 };
 
@@ -516,6 +528,241 @@ int hso_sweeps_npt(hso_sim *s, int n) {
       if (draw_int(s, s->n + 1) < s->n) particle_move(s);
       else volume_move(s);
     }
+  return s->err;
+}
+
+/* ------------------------------------------------------ cavity potential */
+
+/* coeff_py (src/analytic.c:174-230) */
+static void psi_coeff_py(hso_psi *c, double eta) {
+  double complex eta2 = eta * eta;
+  double complex ometa = 1.0 - eta, ometa2 = ometa * ometa;
+  double complex opeta_2 = 1.0 + eta / 2.0;
+  double complex op2eta = 1.0 + 2 * eta;
+  double complex ff = 3.0 + 3. * eta - eta2;
+  double complex eta2_ff2 = (eta2 / ff) * (eta2 / ff);
+  double complex tetaff = cpow(2 * eta * ff, 1. / 3.);
+  double complex yp = cpow(sqrt(1. + 2. * eta2_ff2) + 1., 1. / 3.);
+  double complex ym = -cpow(sqrt(1. + 2. * eta2_ff2) - 1., 1. / 3.);
+  double complex jj = cexp((2. / 3.) * M_PI * I);
+  double complex jj1 = jj;
+  double complex jjm1 = 1. / jj1;
+  double complex jj2 = jj * jj;
+  double complex jjm2 = 1. / jj2;
+  c->t0 = (-2 * eta + tetaff * (yp + ym)) / ometa;
+  c->t1 = (-2 * eta + tetaff * (yp * jj1 + ym * jjm1)) / ometa;
+  c->t2 = (-2 * eta + tetaff * (yp * jj2 + ym * jjm2)) / ometa;
+  double complex L0 = opeta_2 * c->t0 + op2eta;
+  double complex L1 = opeta_2 * c->t1 + op2eta;
+  double complex L2 = opeta_2 * c->t2 + op2eta;
+  double complex S10 = 3 * ometa2 * c->t0 * c->t0 + 12. * eta * ometa * c->t0 + 18. * eta2;
+  double complex S11 = 3 * ometa2 * c->t1 * c->t1 + 12. * eta * ometa * c->t1 + 18. * eta2;
+  double complex S12 = 3 * ometa2 * c->t2 * c->t2 + 12. * eta * ometa * c->t2 + 18. * eta2;
+  c->a00 = c->t0 * L0 / S10;
+  c->a01 = c->t1 * L1 / S11;
+  c->a02 = c->t2 * L2 / S12;
+}
+
+/* rdf_py (src/analytic.c:143-170) */
+static double psi_rdf_py(const hso_psi *c, double xx, double sigma) {
+  double complex xx_hs = xx / sigma;
+  if (creal(xx_hs) < 1.0) return 0.0;
+  double complex g1 = c->a00 * cexp(c->t0 * (xx_hs - 1)) + c->a01 * cexp(c->t1 * (xx_hs - 1)) +
+                      c->a02 * cexp(c->t2 * (xx_hs - 1));
+  return creal(g1) / creal(xx_hs);
+}
+
+/* coeff_vw (src/analytic.c:103-140) */
+static void psi_coeff_vw(hso_psi *c, double eta) {
+  double eta2 = eta * eta;
+  double eta3 = eta2 * eta, eta4 = eta2 * eta2;
+  double ometa = 1. - eta, ometa3 = ometa * ometa * ometa;
+  double ometa4 = ometa3 * ometa;
+  double zz_cs = (1 + eta + eta2 - eta3) / ometa3;
+  double mu_cs = ometa4 / (1 + 4. * eta + 4. * eta2 - 4. * eta3 + eta4);
+  c->dW = pow(1 - eta / 16., 1. / 3.);
+  double dW3 = c->dW * c->dW * c->dW, dW4 = dW3 * c->dW;
+  c->etaW = eta * dW3;
+  double op2etaW2 = (1 + 2 * c->etaW) * (1 + 2 * c->etaW);
+  double ometaW = 1. - c->etaW;
+  double ometaW3 = ometaW * ometaW * ometaW;
+  double ometaW4 = ometaW3 * ometaW;
+  double mu_py = ometaW4 / op2etaW2;
+  psi_coeff_py(c, c->etaW);
+  c->AA = (zz_cs - 1.0) / (4.0 * eta) - psi_rdf_py(c, 1.0, c->dW);
+  c->mu = 12 * c->AA * eta /
+          (mu_cs - mu_py +
+           (c->etaW * (27.0 * c->etaW * (1 + c->etaW) - 8.0 * c->dW * op2etaW2 +
+                       dW4 * (8.0 + 5.0 * c->etaW + 5.0 * c->etaW * c->etaW))) /
+               (dW4 * (-ometaW3)));
+}
+
+/* rdf_vw (src/analytic.c:79-99) */
+static double psi_rdf_vw(const hso_psi *c, double xx, double sigma) {
+  double xx_hs = xx / sigma;
+  if (xx_hs < 1.0) return 0.0;
+  double delta_g1 = (c->AA / xx_hs) * exp(-c->mu * (xx_hs - 1)) * cos(c->mu * (xx_hs - 1));
+  return psi_rdf_py(c, xx_hs, c->dW) + delta_g1;
+}
+
+/* coeff_gh (src/analytic.c:57-75) */
+static void psi_coeff_gh(hso_psi *c, double eta) {
+  psi_coeff_vw(c, eta);
+  double eta2 = eta * eta, eta3 = eta2 * eta;
+  double ometa = 1. - eta, ometa3 = ometa * ometa * ometa;
+  double ometaW = 1. - c->etaW, ometaW3 = ometaW * ometaW * ometaW;
+  double g1 = psi_rdf_py(c, 1.0, c->dW) + c->AA;
+  double dg1 = -(9. / 2.) * c->etaW * (1 + c->etaW) / ometaW3 - c->AA * (1 + c->mu);
+  c->ay0 = (8. * eta - 9. * eta2 + 3. * eta3) / ometa3;
+  c->ay1 = -3. * eta * (2. - eta) / ometa3;
+  c->ay2 = -(dg1 / g1) - 3. * c->ay0 - 2. * c->ay1 + 3. * log(g1);
+  c->ay3 = 1. / 3. * ((dg1 / g1) - c->ay1 - 2. * c->ay2);
+}
+
+/* lny_gh (src/analytic.c:34-54) with sigma = 1 */
+static double psi_lny(const hso_psi *c, double xx) {
+  double xx_hs = xx / 1.0;
+  if (xx_hs < 1.0) return c->ay0 + c->ay1 * xx_hs + c->ay2 * xx_hs * xx_hs + c->ay3 * xx_hs * xx_hs * xx_hs;
+  return log(psi_rdf_vw(c, xx, 1.0));
+}
+
+/* The cavity interaction psi(x) = ln y_GH(x) at packing fraction pi rho / 6
+ * (cavity_interaction, src/moves.c:434-440), for n distances. */
+void hso_cavity_psi(double rho, int n, const double *x, double *out) {
+  hso_psi c;
+  psi_coeff_gh(&c, M_PI * rho / 6.0);
+  for (int k = 0; k < n; k++) out[k] = psi_lny(&c, x[k]);
+}
+
+/* The coefficients in the order ay0..ay3, AA, mu, etaW, dW, then the real
+ * and imaginary parts of t0, t1, t2, a00, a01, a02 (20 doubles). */
+void hso_cavity_coeffs(double rho, double *out) {
+  hso_psi c;
+  psi_coeff_gh(&c, M_PI * rho / 6.0);
+  const double v[8] = {c.ay0, c.ay1, c.ay2, c.ay3, c.AA, c.mu, c.etaW, c.dW};
+  const double complex z[6] = {c.t0, c.t1, c.t2, c.a00, c.a01, c.a02};
+  for (int k = 0; k < 8; k++) out[k] = v[k];
+  for (int k = 0; k < 6; k++) {
+    out[8 + 2 * k] = creal(z[k]);
+    out[9 + 2 * k] = cimag(z[k]);
+  }
+}
+
+/* ---------------------------------------------------------- cavity moves */
+
+/* cavity_set_distance (src/cavity_nvt.c:172-186): cavity 1 on cavity 0,
+ * shifted along z by the middle of the allowed range. */
+int hso_cavity_setup(hso_sim *s, double pcav, double maxdr, double mindr) {
+  s->pcav = pcav;
+  s->cav_max = maxdr;
+  s->cav_min = mindr;
+  psi_coeff_gh(&s->psi, M_PI * s->rho / 6.0);
+  double ave = (maxdr + mindr) / 2.0;
+  s->conf[1][1] = s->conf[0][1];
+  s->conf[1][2] = s->conf[0][2];
+  s->conf[1][3] = s->conf[0][3] + ave;
+  if (s->conf[1][3] > s->lz) s->conf[1][3] -= s->lz;
+  else if (s->conf[1][3] < 0.0) s->conf[1][3] += s->lz;
+  return cell_rebuild(s);
+}
+
+/* cavity_check_move (src/moves.c:333-396) after the proposal; returns 0 to
+ * accept, 1 when the cavities leave the allowed range, 2 when the Metropolis
+ * test fails, 3 on an overlap.  u_acc < 0 draws the uniform. */
+static int cavity_decide(hso_sim *s, int id, int type, double en_old, double u_acc) {
+  if (type == 1) {
+    double d = pair_dist(s, s->conf[0], s->conf[1], 1.0);
+    if (d < s->cav_min || d > s->cav_max) return 1;
+    double boltz = exp(-(psi_lny(&s->psi, d) - en_old));
+    double r = u_acc < 0 ? draw_double(s) : u_acc;
+    if (r > boltz) return 2;
+  }
+  int c = cell_of_particle(s, id);
+  if (c < 0 || c >= s->num_tot) return 3;
+  const int *nb = s->neigh_mat + (size_t)c * 27;
+  for (int q = 0; q < 27; q++) {
+    const int *r = row(s, nb[q]);
+    for (int j = 1; j <= r[0]; j++) {
+      int other = r[j];
+      double d = pair_dist(s, s->conf[id], s->conf[other], 1.0);
+      if (type == 0 && other != id && d < 1.0) return 3;
+      if (type == 1 && other >= 2 && d < 1.0) return 3;
+    }
+  }
+  return 0;
+}
+
+/* cavity_part_move (src/moves.c:254-330) given the particle, its type and
+ * the three step factors t = u - 0.5; u_acc < 0 draws the uniform. */
+static int cavity_move_with(hso_sim *s, int id, int type, const double *t, double u_acc) {
+  double *p = s->conf[id];
+  double ox = p[1], oy = p[2], oz = p[3];
+  int c_old = cell_of_particle(s, id);
+  double en_old = 0.0;
+  if (type == 1) {
+    double d = pair_dist(s, s->conf[0], s->conf[1], 1.0);
+    if (d < s->cav_min || d > s->cav_max) {
+      s->err = HSO_ERR_ARG;
+      return -1;
+    }
+    en_old = psi_lny(&s->psi, d);
+  }
+  p[1] += t[0] * s->dr_max;
+  p[2] += t[1] * s->dr_max;
+  p[3] += t[2] * s->dr_max;
+  wrap_into_box(s, p);
+  int dec = cavity_decide(s, id, type, en_old, u_acc);
+  if (dec == 0) {
+    int c_new = cell_of_particle(s, id);
+    if (c_new != c_old) {
+      int e = cell_move(s, c_old, c_new, id);
+      if (e) s->err = e;
+    }
+    s->acc++;
+  } else {
+    p[1] = ox;
+    p[2] = oy;
+    p[3] = oz;
+    s->rej++;
+  }
+  s->moves++;
+  return dec;
+}
+
+/* cavity_sweep_nvt (src/cavity_nvt.c:161-169): N trials with the
+ * reference's draws. */
+int hso_cavity_sweeps(hso_sim *s, int n) {
+  for (int k = 0; k < n && !s->err; k++)
+    for (int i = 0; i < s->n && !s->err; i++) {
+      double r_type = draw_double(s);
+      int id, type;
+      if (r_type > s->pcav) {
+        id = draw_int(s, s->n - 2) + 2;
+        type = 0;
+      } else {
+        id = draw_int(s, 2);
+        type = 1;
+      }
+      double t[3];
+      for (int d = 0; d < 3; d++) t[d] = draw_double(s) - 0.5;
+      cavity_move_with(s, id, type, t, -1.0);
+    }
+  return s->err;
+}
+
+/* Cavity moves made by the device: cavity which[k] stepped by
+ * (2r - 2^32 + 1) * 2^-33 * dr_max per axis (r = raw[3k..3k+2]) and tested
+ * against the uniform (2 uacc[k] + 1) * 2^-33.  decision[k] as
+ * cavity_decide. */
+int hso_cavity_replay(hso_sim *s, int n, const int *which, const uint32_t *raw, const uint32_t *uacc,
+                      int *decision) {
+  for (int k = 0; k < n && !s->err; k++) {
+    if (which[k] < 0 || which[k] > 1) return HSO_ERR_ARG;
+    double t[3];
+    for (int d = 0; d < 3; d++) t[d] = ldexp(2.0 * (double)raw[3 * k + d] - 4294967295.0, -33);
+    double u = ldexp(2.0 * (double)uacc[k] + 1.0, -33);
+    decision[k] = cavity_move_with(s, which[k], 1, t, u);
+  }
   return s->err;
 }
 

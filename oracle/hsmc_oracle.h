@@ -51,6 +51,14 @@ void hso_reset_counters(hso_sim *s);
 
 int hso_replay_moves(hso_sim *s, int n, const int *ids, const uint32_t *raw, int *accepted);
 
+/* Cavity sampling (src/cavity_nvt.c, src/moves.c:254-440, src/analytic.c). */
+void hso_cavity_psi(double rho, int n, const double *x, double *out);
+void hso_cavity_coeffs(double rho, double *out20);
+int hso_cavity_setup(hso_sim *s, double pcav, double maxdr, double mindr);
+int hso_cavity_sweeps(hso_sim *s, int n);
+int hso_cavity_replay(hso_sim *s, int n, const int *which, const uint32_t *raw, const uint32_t *uacc,
+                      int *decision);
+
 /* Geometric cluster moves (src/cluster_nvt.c:221-431). */
 int hso_cluster_move_at(hso_sim *s, const double *pivot, int axis, int seed_id, int *size);
 int hso_cluster_moves(hso_sim *s, int n, int *sizes);

@@ -197,6 +197,11 @@ class OracleSim(_SimBase):
             L.hso_cell_of32.restype = C.c_uint32
             L.hso_cell_of32.argtypes = [C.c_float, C.c_float, C.c_float, C.c_float, C.c_int]
             L.hso_cluster_move_at.argtypes = [C.c_void_p, _dp, C.c_int, C.c_int, _i32p]
+            L.hso_cavity_psi.argtypes = [C.c_double, C.c_int, _dp, _dp]
+            L.hso_cavity_coeffs.argtypes = [C.c_double, _dp]
+            L.hso_cavity_setup.argtypes = [C.c_void_p, C.c_double, C.c_double, C.c_double]
+            L.hso_cavity_sweeps.argtypes = [C.c_void_p, C.c_int]
+            L.hso_cavity_replay.argtypes = [C.c_void_p, C.c_int, _i32p, _u32p, _u32p, _i32p]
             L.hso_cluster_moves.argtypes = [C.c_void_p, C.c_int, _i32p]
             cls._lib = L
         return cls._lib
@@ -326,6 +331,39 @@ class OracleSim(_SimBase):
             raise RuntimeError(f"oracle cluster move failed ({e})")
         return int(size[0])
 
+    def cavity_setup(self, pcav, maxdr=1.2, mindr=0.0):
+        e = self._lib.hso_cavity_setup(self._h, pcav, maxdr, mindr)
+        if e:
+            raise RuntimeError(f"oracle cavity setup failed ({e})")
+
+    def cavity_sweeps(self, n):
+        e = self._lib.hso_cavity_sweeps(self._h, n)
+        if e:
+            raise RuntimeError(f"oracle cavity sweeps failed ({e})")
+
+    def cavity_replay(self, which, raw, uacc):
+        which = np.ascontiguousarray(which, dtype=np.int32)
+        raw = np.ascontiguousarray(raw, dtype=np.uint32)
+        uacc = np.ascontiguousarray(uacc, dtype=np.uint32)
+        dec = np.zeros(which.size, dtype=np.int32)
+        e = self._lib.hso_cavity_replay(self._h, which.size, which, raw, uacc, dec)
+        if e:
+            raise RuntimeError(f"oracle cavity replay failed ({e})")
+        return dec
+
+    @classmethod
+    def cavity_psi(cls, rho, x):
+        x = np.ascontiguousarray(x, dtype=np.float64)
+        out = np.zeros_like(x)
+        cls.lib().hso_cavity_psi(rho, x.size, x, out)
+        return out
+
+    @classmethod
+    def cavity_coeffs(cls, rho):
+        out = np.zeros(20)
+        cls.lib().hso_cavity_coeffs(rho, out)
+        return out
+
     def cluster_moves(self, n):
         """n cluster moves with the reference's draws; their sizes."""
         sizes = np.zeros(n, dtype=np.int32)
@@ -416,6 +454,10 @@ class RefSim(_SimBase):
             L.ref_rng_uniform_int.argtypes = [C.c_ulong, C.c_ulong, C.c_int, _i32p]
             L.ref_cluster_moves.argtypes = [C.c_int, _i32p]
             L.ref_cluster_move_at.argtypes = [_dp, C.c_int, C.c_int]
+            L.ref_cavity_setup.argtypes = [C.c_double, C.c_double, C.c_double]
+            L.ref_cavity_sweeps.argtypes = [C.c_int]
+            L.ref_cavity_psi.argtypes = [C.c_int, _dp, _dp]
+            L.ref_cavity_replay.argtypes = [C.c_int, _i32p, _u32p, _u32p, _i32p, _i32p]
             cls._lib = L
         return cls._lib
 
@@ -482,6 +524,28 @@ class RefSim(_SimBase):
         sizes = np.zeros(n, dtype=np.int32)
         self._lib.ref_cluster_moves(n, sizes)
         return sizes
+
+    def cavity_setup(self, pcav, maxdr=1.2, mindr=0.0):
+        self._lib.ref_cavity_setup(pcav, maxdr, mindr)
+
+    def cavity_sweeps(self, n):
+        self._lib.ref_cavity_sweeps(n)
+
+    def cavity_replay(self, which, raw, uacc, draws_acc):
+        which = np.ascontiguousarray(which, dtype=np.int32)
+        acc = np.zeros(which.size, dtype=np.int32)
+        e = self._lib.ref_cavity_replay(which.size, which, np.ascontiguousarray(raw, dtype=np.uint32),
+                                        np.ascontiguousarray(uacc, dtype=np.uint32),
+                                        np.ascontiguousarray(draws_acc, dtype=np.int32), acc)
+        if e:
+            raise RuntimeError("reference cavity replay consumed an unexpected number of draws")
+        return acc
+
+    def cavity_psi_ref(self, x):
+        x = np.ascontiguousarray(x, dtype=np.float64)
+        out = np.zeros_like(x)
+        self._lib.ref_cavity_psi(x.size, x, out)
+        return out
 
     def cluster_move_at(self, pivot, axis, seed_id) -> int:
         return self._lib.ref_cluster_move_at(np.ascontiguousarray(pivot, dtype=np.float64), int(axis), int(seed_id))

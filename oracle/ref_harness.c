@@ -34,6 +34,7 @@
 #include "compute_widom_chem_pot.h"
 #include "compute_order_parameter.h"
 #include "cluster_nvt.h"
+#include "cavity_nvt.h"
 #include "gsl/gsl_rng.h"
 
 /* Globalised statics of the reference objects. */
@@ -132,6 +133,27 @@ void ref_counters(unsigned long *out) {
 
 void ref_reset_counters(void) { reset_moves_counters(); }
 
+/* Cavity sampling set up as cavity_hs_nvt does it (src/cavity_nvt.c:27-62):
+ * the keyword values, cavity_set_distance, the potential's coefficients
+ * (cavity_interaction(0.5, true)), then a fresh cell list. */
+void ref_cavity_setup(double pcav, double maxdr, double mindr) {
+  G_IN.cavity_pcav = pcav;
+  G_IN.cavity_maxdr = maxdr;
+  G_IN.cavity_mindr = mindr;
+  cavity_set_distance();
+  cavity_interaction(0.5, true);
+  cell_list_new();
+}
+
+void ref_cavity_sweeps(int n) {
+  for (int k = 0; k < n; k++) cavity_sweep_nvt();
+}
+
+/* cavity_interaction(x, false) for n distances (after ref_cavity_setup). */
+void ref_cavity_psi(int n, const double *x, double *out) {
+  for (int k = 0; k < n; k++) out[k] = cavity_interaction(x[k], false);
+}
+
 /* n calls of cluster_move() (src/cluster_nvt.c:232-310) with the generator;
  * sizes[k] receives the reference's cluster_size after call k. */
 void ref_cluster_moves(int n, int *sizes) {
@@ -206,6 +228,38 @@ int ref_replay_moves_offsets(int n, const int *ids, const unsigned int *raw, int
   hsmc_shim_script_off();
   r_num_max = saved;
   free(w);
+  return 0;
+}
+
+/* Cavity trials made by the device, through the reference's own
+ * cavity_part_move (src/moves.c:254-330): trial k moves cavity which[k]
+ * with the uniforms (2r + 1) / 2^33 of raw[3k..3k+2] and, when draws_acc[k]
+ * (the trial reached the Metropolis test), the acceptance uniform from
+ * uacc[k]; the particle-type draw is scripted to pick a cavity.
+ * accepted[k] receives 1 when the reference accepted the move. */
+int ref_cavity_replay(int n, const int *which, const unsigned int *raw, const unsigned int *uacc,
+                      const int *draws_acc, int *accepted) {
+  unsigned long saved = r_num_max;
+  r_num_max = 8589934592ul;
+  for (int k = 0; k < n; k++) {
+    unsigned long w[5];
+    size_t nw = 0;
+    w[nw++] = 1ul; /* r_type = 2^-33 <= cavity_pcav: a cavity move */
+    for (int d = 0; d < 3; d++) w[nw++] = 2ul * raw[3 * k + d] + 1ul;
+    if (draws_acc[k]) w[nw++] = 2ul * uacc[k] + 1ul;
+    hsmc_shim_script_int(which + k, 1);
+    hsmc_shim_script_raw(w, nw);
+    unsigned long before = acc_part_moves;
+    cavity_part_move();
+    accepted[k] = acc_part_moves != before;
+    if (hsmc_shim_script_left_raw() != 0) {
+      hsmc_shim_script_off();
+      r_num_max = saved;
+      return -1; /* the reference consumed fewer draws than scripted */
+    }
+  }
+  hsmc_shim_script_off();
+  r_num_max = saved;
   return 0;
 }
 
