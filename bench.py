@@ -542,6 +542,74 @@ def run_npt(args):
     return 0
 
 
+def run_cavity(args):
+    """Torrie-Patey cavity sampling (src/cavity_nvt.c) at the reference's own
+    published case: rho = 0.8, 1000 spheres (simple-cubic 10^3 start),
+    cavities allowed in [0, 1.2] (the keyword defaults), p_cav = 0.1, dr_max
+    tuned toward 40 %.  Reports trial moves/s (checkerboard trials plus the
+    sweeps' cavity trials) and ln y(r) from the sampled distances, unbiased
+    with psi, against the Grundke-Henderson psi itself.  CPU baseline: the
+    oracle's cavity sweeps (the reference's algorithm) on one host core."""
+    import numpy as np
+    from hsmc_gb300 import HardSphereSystem
+
+    rho, pcav = 0.8, 0.1
+    g = HardSphereSystem(rho=rho, cells=10, lattice_type=1, dr_max=0.1, seed=42, cavity=(pcav, 1.2, 0.0))
+    dr, acc = tune_dr(g, 0.1)
+    g.sweep_nvt(args.equil)
+    sweeps, per = args.sweeps, 8  # one distance sample per 8 sweeps (one CUDA graph launch)
+    d = np.empty(sweeps // per)
+    t, moves = 0.0, 0
+    for k in range(sweeps // per):
+        t0 = time.perf_counter()
+        c = g.sweep_nvt(per)
+        t += time.perf_counter() - t0
+        moves += int(c[0])
+        d[k] = g.cavity_distance()
+    edges = np.linspace(0.0, 1.2, 13)
+    h, _ = np.histogram(d, bins=edges)
+    r = 0.5 * (edges[1:] + edges[:-1])
+    psi = g.cavity_psi(r)
+    with np.errstate(divide="ignore"):
+        lny = np.log(h / (r * r)) + psi
+    ok = h > 0
+    shift = float(np.mean((lny - psi)[ok & (r > 0.5)]))  # fix the constant where the counts are large
+    # the same ensemble at N = 256,000 (40^3 FCC), p_cav = 1e-4: 26 cavity
+    # trials per sweep, where the checkerboard passes carry the sweep
+    gl = HardSphereSystem(rho=rho, cells=40, dr_max=dr, seed=43, cavity=(1e-4, 1.2, 0.0))
+    gl.sweep_nvt(48)
+    t0 = time.perf_counter()
+    cl = gl.sweep_nvt(400)
+    t_large = time.perf_counter() - t0
+    line = {
+        "metric": "trial moves/s, cavity sampling rho=0.8 N=1000", "value": moves / t, "unit": "trial moves/s",
+        "n_gpus": 1, "higher_is_better": True, "dtype": "f64", "data": "synthetic (simple-cubic start)",
+        "config": {"workload": "cavity sampling, rho 0.8, 10^3 simple-cubic start, cavities in [0, 1.2], "
+                               f"p_cav {pcav}, {sweeps} sweeps after {args.equil}, a distance sample every {per}",
+                   "dr_max": dr, "acceptance": acc, "timing": "host wall-clock around synchronous calls"},
+        "large": {"N": gl.n, "p_cav": 1e-4, "sweeps": 400, "trial_moves_per_s": float(cl[0]) / t_large,
+                  "cavity_distance": gl.cavity_distance()},
+        "lny": {"r": r.tolist(), "sampled": [float(v - shift) if o else None for v, o in zip(lny, ok)],
+                "grundke_henderson": psi.tolist(), "counts": h.tolist()},
+    }
+    if not args.no_cpu_baseline:
+        from oracle.oracle import OracleSim
+
+        o = OracleSim(rho=rho, n_cells=10, lattice_type=1, seed=3, dr_max=dr, neigh_dr=1.05, neigh_max_part=12)
+        o.cavity_setup(pcav, 1.2, 0.0)
+        o.cavity_sweeps(20)
+        o.reset_counters()
+        t0, k = time.perf_counter(), 0
+        while time.perf_counter() - t0 < 10.0:
+            o.cavity_sweeps(10)
+            k += 10
+        dt = time.perf_counter() - t0
+        line["cpu_baseline"] = {"value": float(o.counters()[0]) / dt, "unit": "trial moves/s", "cores": 1,
+                                "kind": "port", "sample": f"{k} oracle cavity sweeps of the same system, about 10 s"}
+    print(json.dumps(line), flush=True)
+    return 0
+
+
 def run_cluster(args):
     """Geometric cluster moves (src/cluster_nvt.c): the reference's own
     comparison, N = 256 at packing fractions 0.25 and 0.30 with cluster moves
@@ -622,7 +690,7 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
-    ap.add_argument("--workload", default="fluid", choices=["fluid", "replicas", "widom", "npt", "cluster"])
+    ap.add_argument("--workload", default="fluid", choices=["fluid", "replicas", "widom", "npt", "cluster", "cavity"])
     ap.add_argument("--replicas", type=int, default=512)
     ap.add_argument("--cell-edge", default="0",
                     help='replicas: smallest device-cell edge, a number or "auto" (min(rho^-1/3, 1.4))')
@@ -642,6 +710,8 @@ def main():
         return run_npt(args)
     if args.workload == "cluster":
         return run_cluster(args)
+    if args.workload == "cavity":
+        return run_cavity(args)
     return run_gpu_arm(args)
 
 

@@ -6,6 +6,7 @@
  * reference; consecutive sweeps with nothing to sample between them go to
  * the device as one call.
  */
+#include <math.h>
 #include <stdio.h>
 #include <stdlib.h>
 #include <string.h>
@@ -76,8 +77,10 @@ static void sample_acceptance(host_run *r, int sweeps, bool npt, double *acc_par
   if (acc_vol) *acc_vol = (double)r->counters[HSMC_CNT_VOL_ACCEPTED] / ((double)r->counters[HSMC_CNT_VOL_MOVES]);
 }
 
-/* opt_nvt (src/optimizer.c:23-64): secant search of dr_max. */
-static void opt_nvt(host_run *r) {
+/* opt_nvt (src/optimizer.c:23-64): secant search of dr_max; opt_cavity_nvt
+ * (src/optimizer.c:172-212) is the same search over cavity sweeps, printed
+ * with a space before the newline of its acceptance line. */
+static void opt_nvt_as(host_run *r, bool cavity) {
   host_input *in = &r->in;
   int per = in->opt_sweeps / in->opt_samples;
   double a1, a2, d1, d2;
@@ -105,9 +108,11 @@ static void opt_nvt(host_run *r) {
     d2 = in->dr_max;
   }
   printf("Optimal maximum displacement: %.8f\n", in->dr_max);
-  printf("Acceptance ratio: %.8f\n", a2);
+  printf(cavity ? "Acceptance ratio: %.8f \n" : "Acceptance ratio: %.8f\n", a2);
   printf("Maximum displacement optimization completed\n");
 }
+
+static void opt_nvt(host_run *r) { opt_nvt_as(r, false); }
 
 /* opt_npt (src/optimizer.c:83-148): secant search of dr_max and dv_max. */
 static void opt_npt(host_run *r) {
@@ -277,6 +282,143 @@ void host_cluster(host_run *r) {
   cluster_block(r, true, r->in.sweep_eq, &last);
   printf("Production completed.\n");
   printf("Elapsed time: %f seconds\n", wall_seconds() - t0);
+  hsmc_gpu_destroy(r->gpu);
+  r->gpu = NULL;
+  free(r->conf);
+  r->conf = NULL;
+}
+
+/* --------------------------------------------------------- cavity sampling */
+
+/* cavity_set_distance (src/cavity_nvt.c:172-186) on the host copy. */
+static void cavity_set_distance(host_run *r) {
+  double ave = (r->in.cavity_maxdr + r->in.cavity_mindr) / 2.0;
+  r->conf[1][1] = r->conf[0][1];
+  r->conf[1][2] = r->conf[0][2];
+  r->conf[1][3] = r->conf[0][3] + ave;
+  if (r->conf[1][3] > r->box.lz) r->conf[1][3] -= r->box.lz;
+  else if (r->conf[1][3] < 0.0) r->conf[1][3] += r->box.lz;
+}
+
+/* cavity_psi_output (src/cavity_nvt.c:191-212), with psi as the device
+ * evaluates it. */
+static void cavity_psi_output(host_run *r) {
+  FILE *fid = fopen("cavity_psi.dat", "w");
+  if (fid == NULL) {
+    perror("Error while creating the file for the cavity potential\n");
+    exit(EXIT_FAILURE);
+  }
+  fprintf(fid, "#########################################################\n");
+  fprintf(fid, "# Interaction potential  between the cavities \n");
+  fprintf(fid, "# Distance, potential\n");
+  fprintf(fid, "#########################################################\n");
+  int n_points = (int)((r->in.cavity_maxdr - r->in.cavity_mindr) / r->in.cavity_out_dr);
+  if (n_points > 0) {
+    double *x = malloc(sizeof(double) * (size_t)n_points), *psi = malloc(sizeof(double) * (size_t)n_points);
+    double xx = r->in.cavity_mindr;
+    for (int ii = 0; ii < n_points; ii++) {
+      x[ii] = xx;
+      xx += r->in.cavity_out_dr;
+    }
+    host_gpu_check(hsmc_gpu_cavity_psi(r->gpu, x, n_points, psi), "cavity psi");
+    for (int ii = 0; ii < n_points; ii++) fprintf(fid, "%.8e %.8e\n", x[ii], psi[ii]);
+    free(x);
+    free(psi);
+  }
+  fclose(fid);
+}
+
+/* cavity_dist_output (src/cavity_nvt.c:217-237): compute_dist(0, 1). */
+static void cavity_dist_output(host_run *r, bool init) {
+  host_gpu_download(r);
+  double l[3] = {r->box.lx, r->box.ly, r->box.lz}, s2 = 0.0;
+  double d[3];
+  for (int k = 0; k < 3; k++) {
+    d[k] = r->conf[0][1 + k] - r->conf[1][1 + k];
+    if (d[k] > l[k] / 2.0) d[k] -= l[k];
+    else if (d[k] < -l[k] / 2.0) d[k] += l[k];
+  }
+  s2 = d[0] * d[0] + d[1] * d[1] + d[2] * d[2];
+  FILE *fid = fopen("cavity_distance.dat", init ? "w" : "a");
+  if (fid == NULL) {
+    perror("Error while creating the file for the cavity distance\n");
+    exit(EXIT_FAILURE);
+  }
+  if (init) {
+    fprintf(fid, "#########################################################\n");
+    fprintf(fid, "# Distance between the cavities (each line is one sample)\n");
+    fprintf(fid, "#########################################################\n");
+  }
+  fprintf(fid, "%.8e\n", sqrt(s2));
+  fclose(fid);
+}
+
+/* cavity_run_nvt (src/cavity_nvt.c:101-158) */
+static void cavity_block(host_run *r, bool prod, int offset, bool *dist_init) {
+  const host_input *in = &r->in;
+  if (in->output_int <= 0) {
+    printf("ERROR: the output interval (keyword out) must be positive\n");
+    exit(EXIT_FAILURE);
+  }
+  int n = prod ? in->sweep_stat : in->sweep_eq;
+  int pending = 0;
+  for (int ii = offset; ii < n + offset; ii++) {
+    const bool dist = prod && every(ii, in->cavity_sample_int);
+    if (every(ii, in->restart_write) || (prod && every(ii, in->config_write)) || dist) {
+      host_sweeps(r, pending, false);
+      pending = 0;
+    }
+    if (ii == 0) printf("Sweep number\n");
+    if (ii % in->output_int == 0) {
+      printf("%d\n", ii);
+      fflush(stdout);
+    }
+    if (every(ii, in->restart_write)) host_write_restart(r, ii);
+    if (prod) {
+      if (every(ii, in->config_write)) host_write_config(r, ii);
+      if (dist) {
+        cavity_dist_output(r, *dist_init);
+        *dist_init = false;
+      }
+    }
+    pending++;
+  }
+  host_sweeps(r, pending, false);
+}
+
+void host_cavity(host_run *r) {
+  if (r->in.restart_read == 0) {
+    host_box_init(r, r->in.type, r->in.nx, r->in.ny, r->in.nz, r->in.rho);
+    host_part_alloc(r);
+    host_part_init(r);
+    cavity_set_distance(r);
+  } else {
+    host_read_restart(r, r->in.restart_name);
+  }
+  host_print_sim_info(r);
+  host_cells_init(r, true);
+  host_gpu_open(r);
+  host_gpu_upload(r);
+  cavity_psi_output(r);
+  if (r->in.opt_flag == 1) {
+    opt_nvt_as(r, true);
+    host_part_init(r);
+    cavity_set_distance(r);
+    host_cells_init(r, false);
+    host_gpu_upload(r);
+  }
+  double t0 = wall_seconds();
+  host_reset_counters(r);
+  bool dist_init = true;
+  printf("---------------------------------------------------\n");
+  printf("Equilibration...\n");
+  cavity_block(r, false, 0, &dist_init);
+  printf("Equilibration completed.\n");
+  printf("---------------------------------------------------\n");
+  printf("Production...\n");
+  cavity_block(r, true, r->in.sweep_eq, &dist_init);
+  printf("Production completed.\n");
+  print_summary(r, wall_seconds() - t0, false);
   hsmc_gpu_destroy(r->gpu);
   r->gpu = NULL;
   free(r->conf);

@@ -119,5 +119,6 @@ void host_write_config(host_run *r, int sweep);
 void host_nvt(host_run *r);
 void host_npt(host_run *r);
 void host_cluster(host_run *r);
+void host_cavity(host_run *r);
 
 #endif

@@ -2,8 +2,8 @@
  * hsmc: the reference's command line (src/exec.c:28-145) over the GB300
  * engine.  -i/--input IN_FILE (default in.dat), -e/--example, -o/--output
  * OUT_FILE; dispatch on the input as the reference does: NpT when npt > 0,
- * else cavity sampling when cavity > 0 (refused: not part of this engine),
- * else cluster moves when cluster is set, else NVT.
+ * else cavity sampling when cavity > 0, else cluster moves when cluster is
+ * set, else NVT.
  */
 #include <getopt.h>
 #include <stdbool.h>
@@ -58,8 +58,7 @@ int main(int argc, char **argv) {
     if (run.in.press > 0) {
       host_npt(&run);
     } else if (run.in.cavity_pcav > 0) {
-      printf("ERROR: cavity simulations are not provided by this engine\n");
-      exit(EXIT_FAILURE);
+      host_cavity(&run);
     } else if (run.in.cluster_flag > 0) {
       host_cluster(&run);
     } else {

@@ -137,6 +137,11 @@ void host_gpu_open(host_run *r) {
   p.dv_max = r->in.dv_max;
   p.pressure = r->in.press;
   p.seed = r->in.seed;
+  if (r->in.press <= 0 && r->in.cavity_pcav > 0) {
+    p.cavity_pcav = r->in.cavity_pcav;
+    p.cavity_maxdr = r->in.cavity_maxdr;
+    p.cavity_mindr = r->in.cavity_mindr;
+  }
   host_gpu_check(hsmc_gpu_create(&p, &r->gpu), "hsmc_gpu_create");
   if (r->have_rng) host_gpu_check(hsmc_gpu_rng_set_state(r->gpu, r->rng_host), "hsmc_gpu_rng_set_state");
 }

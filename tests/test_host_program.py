@@ -6,6 +6,7 @@ must match the reference byte for byte.  On a GPU: whole runs must produce
 the same files with the same headers, the same deterministic columns (bin
 centres, compression steps, sweep numbers, box and particle count) and the
 same stdout lines up to the numbers a Monte Carlo run draws."""
+import math
 import os
 import re
 import shutil
@@ -71,7 +72,7 @@ def _run(hsmc_exe, tmp_path, case):
 
 
 @pytest.mark.gpu
-@pytest.mark.parametrize("case", ["nvt_small", "npt_small", "cluster_small"])
+@pytest.mark.parametrize("case", ["nvt_small", "npt_small", "cluster_small", "cavity_small"])
 def test_run_matches_reference_files(hsmc_exe, tmp_path, case):
     out = _run(hsmc_exe, tmp_path, case)
     gold = os.path.join(GOLD, case)
@@ -105,6 +106,16 @@ def test_run_matches_reference_files(hsmc_exe, tmp_path, case):
                         assert a == b, f
                 else:
                     assert fa[0] == fb[0], f
+        if f == "cavity_psi.dat":  # the grid exactly; psi from the device's exp/cos/sin/log
+            for a, b in zip(ours_l, ref_l):
+                if b.startswith("#"):
+                    continue
+                fa, fb = a.split(), b.split()
+                assert fa[0] == fb[0]
+                assert math.isclose(float(fa[1]), float(fb[1]), rel_tol=1e-8)
+        if f == "cavity_distance.dat":
+            vals = [float(l) for l in ours_l if not l.startswith("#")]
+            assert all(0.3 <= v <= 0.7 for v in vals)
         if f.startswith("press_thermo"):
             vals = [float(l.split()[1]) for l in ours_l if not l.startswith("#") and len(l.split()) == 2]
             assert set(vals) <= {0.0, 1.0}
