@@ -642,7 +642,11 @@ def run_cluster(args):
                 cnt += g.compute_pressv_counts(bin_, 1.0 + nb * bin_, nb)
             z.append(contact_z(cnt, per_block, g.n, rho, bin_))
         z = np.array(z)
+        t0 = time.perf_counter()
+        g.cluster_moves(2000)
+        batched = 2000 / (time.perf_counter() - t0)
         small.append({"packing_fraction": eta, "N": g.n, "cluster_moves_per_s": moves / t,
+                      "cluster_moves_per_s_2000_per_call": batched,
                       "mean_cluster_size": moved / moves, "pressure": float(rho * z.mean()),
                       "pressure_se": float(rho * z.std(ddof=1) / math.sqrt(blocks)),
                       "pressure_cs": float(rho * carnahan_starling(rho)), "moves": moves})

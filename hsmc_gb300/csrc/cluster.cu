@@ -200,22 +200,44 @@ __global__ void __launch_bounds__(512) k_cluster(SysPtrs p, ClusterJob job, int 
     while (ncur > 0) {
       const long long next = base + ncur;
       uint32_t *push = job.ctr + (level + 1) % 3;
-      for (int k = wid; k < ncur; k += nw) {
+      // On a small grid, the level's images first, one thread per particle
+      // (a warp's FP64 sequence serves 32 particles; the SMs' FP64 pipes are
+      // the bottleneck there), then a meeting so every block sees them.  On
+      // a large grid the extra meeting costs more than it saves: each search
+      // warp computes its own particle's image.
+      const bool split = gridDim.x <= 4;
+      for (int k = (int)(blockIdx.x * blockDim.x + threadIdx.x); split && k < ncur;
+           k += (int)(gridDim.x * blockDim.x)) {
         const int i = __ldcg(job.queue + base + k);
-        // unchanged until this warp writes the image
         const double2 a0 = __ldcg(reinterpret_cast<const double2 *>(p.pos + 4 * (size_t)i));
         const double2 b0 = __ldcg(reinterpret_cast<const double2 *>(p.pos + 4 * (size_t)i + 2));
         double px, py, pz;
         reflect_axis(a0.y, b0.x, b0.y, piv, two_piv, axis, job.sint, px, py, pz);
-        px = wrap_once(px, len[0]);
-        py = wrap_once(py, len[1]);
-        pz = wrap_once(pz, len[2]);
-        __syncwarp();
-        if (lane == 0) {
-          double *q = p.pos + 4 * (size_t)i;
-          q[1] = px;
-          q[2] = py;
-          q[3] = pz;
+        double *q = p.pos + 4 * (size_t)i;
+        q[1] = wrap_once(px, len[0]);
+        q[2] = wrap_once(py, len[1]);
+        q[3] = wrap_once(pz, len[2]);
+      }
+      if (split && !grid_meet(job.ctr + 3, ++phase, status)) return;
+      // one warp per particle, lane k on neighbour cell k of its image; the
+      // level's particles are all marked, so no search reads their images
+      for (int k = wid; k < ncur; k += nw) {
+        const int i = __ldcg(job.queue + base + k);
+        const double2 a0 = __ldcg(reinterpret_cast<const double2 *>(p.pos + 4 * (size_t)i));
+        const double2 b0 = __ldcg(reinterpret_cast<const double2 *>(p.pos + 4 * (size_t)i + 2));
+        double px = a0.y, py = b0.x, pz = b0.y;
+        if (!split) {
+          reflect_axis(a0.y, b0.x, b0.y, piv, two_piv, axis, job.sint, px, py, pz);
+          px = wrap_once(px, len[0]);
+          py = wrap_once(py, len[1]);
+          pz = wrap_once(pz, len[2]);
+          __syncwarp();
+          if (lane == 0) {
+            double *q = p.pos + 4 * (size_t)i;
+            q[1] = px;
+            q[2] = py;
+            q[3] = pz;
+          }
         }
         if (lane < 27) {
           int ci[3];
@@ -430,23 +452,29 @@ __global__ void __launch_bounds__(512) k_cluster_small(SysPtrs p, ClusterJob job
     while (ncur > 0) {
       const int next = base + ncur;
       uint32_t *push = m.pc + (level + 1) % 3;
-      for (int k = wid; k < ncur; k += nw) {
+      // the level's images, one thread per particle: a warp's FP64 sequence
+      // serves 32 particles (the FP64 pipe is busy per warp instruction)
+      for (int k = tid; k < ncur; k += nt) {
         const int i = m.queue[base + k];
         double px, py, pz;
         reflect_axis(m.x[i], m.y[i], m.z[i], piv, two_piv, axis, job.sint, px, py, pz);
         px = wrap_once(px, len[0]);
         py = wrap_once(py, len[1]);
         pz = wrap_once(pz, len[2]);
-        const float px32 = __double2float_rn(px), py32 = __double2float_rn(py), pz32 = __double2float_rn(pz);
-        __syncwarp();
-        if (lane == 0) {
-          m.x[i] = px;
-          m.y[i] = py;
-          m.z[i] = pz;
-          m.x32[i] = px32;
-          m.y32[i] = py32;
-          m.z32[i] = pz32;
-        }
+        m.x[i] = px;
+        m.y[i] = py;
+        m.z[i] = pz;
+        m.x32[i] = __double2float_rn(px);
+        m.y32[i] = __double2float_rn(py);
+        m.z32[i] = __double2float_rn(pz);
+      }
+      __syncthreads();
+      // then one warp per particle, lane k on neighbour cell k of its image;
+      // the level's particles are all marked, so no search reads their images
+      for (int k = wid; k < ncur; k += nw) {
+        const int i = m.queue[base + k];
+        const double px = m.x[i], py = m.y[i], pz = m.z[i];
+        const float px32 = m.x32[i], py32 = m.y32[i], pz32 = m.z32[i];
         if (lane < 27) {
           int ci[3];
           float t;
