@@ -78,6 +78,10 @@ struct hsmc_ctx {
   unsigned long long cluster_seq = 0;  // cluster moves drawn from the stream so far
   uint32_t cl_epoch = 0;               // epoch of the last move (marks hold older ones)
   int cl_grid = -1;  // -1 not chosen yet, 0 the one-block shared-memory kernel
+  // one-block schedule (sweep_small.cu): shared memory it needs (0: the
+  // system does not fit) and whether it is the schedule in use
+  size_t small_smem = 0;
+  bool small = false;
   // cavity sampling: on when the context was created with cavity_pcav > 0
   bool cavity = false;
   Scratch cav_trace;
@@ -319,6 +323,16 @@ int hsmc_gpu_create(const hsmc_params *prm, hsmc_ctx **out) {
     return fail(ce);
   ctx->flow = false;  // one launch per pass unless hsmc_gpu_set_schedule or the autotuner picks the dataflow sweep
   ctx->cavity = cavity;
+  // a system that fits one block's shared memory runs its NVT sweeps there
+  if (!cavity && prm->pressure <= 0) {
+    const size_t sm = sweep_small_smem(ctx->n, b.ncell);
+    if (sm > 0 && prepare_sweep_small(sm)) ctx->small_smem = sm;
+    cudaGetLastError();
+  }
+  // the default where it measured faster than one launch per pass: at most
+  // 64 active cells per pass (up to about 500 spheres); the autotuner tries
+  // it wherever it fits
+  ctx->small = ctx->small_smem > 0 && b.ncell / 8 <= 64;
   *out = ctx;
   return HSMC_OK;
 }
@@ -487,6 +501,36 @@ static int run_sweeps(hsmc_ctx *ctx, int n_sweeps, bool trace, bool npt, uint64_
   HSMC_CUDA(cudaMemsetAsync(&ctx->sp.st->status, 0, sizeof(int), ctx->stream));
   ctx->last_move_ms = 0.0;
   ctx->last_move_launches = 0;
+  if (ctx->small && !trace && !ctx->profiling && !npt) {
+    // every sweep in one launch, then the device layouts rebuilt for the
+    // last sweep (observables and the other schedules read them)
+    HSMC_CUDA(cudaEventRecord(ctx->ev_start, ctx->stream));
+    if (n_sweeps > 0) launch_sweep_small(ctx->sp, n_sweeps, ctx->small_smem, ctx->hbox.ncell / 8, ctx->stream);
+    HSMC_CUDA(cudaEventRecord(ctx->ev_stop, ctx->stream));
+    ctx->sweep_base += (unsigned long long)n_sweeps;
+    if (n_sweeps > 0) {
+      for (int l = 0; l < 2; l++)
+        HSMC_CUDA(cudaMemsetAsync(ctx->sp.cnt[l], 0, sizeof(int) * (size_t)ctx->sp.ncell_alloc, ctx->stream));
+      launch_build(ctx->sp, -1, ctx->num_sms, ctx->stream);
+      reset_progress(ctx);
+    }
+    int e = check_kernels(ctx);
+    if (e) return e;
+    float ms = 0.f;
+    HSMC_CUDA(cudaEventElapsedTime(&ms, ctx->ev_start, ctx->ev_stop));
+    ctx->last_total_ms = ms;
+    DevState s;
+    if ((e = read_state(ctx, s))) return e;
+    if (counters) {
+      const uint64_t moves = (uint64_t)ctx->n * (uint64_t)n_sweeps;
+      counters[HSMC_CNT_MOVES] = moves;
+      counters[HSMC_CNT_ACCEPTED] = s.acc;
+      counters[HSMC_CNT_REJECTED] = moves - s.acc;
+      counters[HSMC_CNT_VOL_MOVES] = counters[HSMC_CNT_VOL_ACCEPTED] = counters[HSMC_CNT_VOL_REJECTED] = 0;
+    }
+    if (s.status) return status_to_code(s.status);
+    return HSMC_OK;
+  }
   bool direct = trace || ctx->profiling || ctx->cav_trace_cap > 0;  // graphs hold no trace buffers
   if (!direct) {
     int e = ensure_graph(ctx, npt);
@@ -576,7 +620,13 @@ static void drop_graphs(hsmc_ctx *ctx) {
 // Lanes per cell and schedule; the grids follow.  Returns false when the
 // combination cannot run on this device.
 static bool apply_schedule(hsmc_ctx *ctx, int flow, int group) {
+  if (flow == 2) {  // one block: the lane mapping of the passes is kept for the other schedules
+    if (ctx->small_smem == 0) return false;
+    ctx->small = true;
+    return true;
+  }
   if (!move_pass_fits(group, ctx->sp.cap)) return false;
+  ctx->small = false;
   int fg = 0;
   if (flow) {
     int dev = 0, coop = 0;
@@ -602,11 +652,13 @@ int hsmc_gpu_autotune(hsmc_ctx *ctx, int sweeps_per_variant, int *lanes_out) {
   const bool npt = ctx->prm.pressure > 0;
   const int sweeps = ((sweeps_per_variant + kGraphSweeps - 1) / kGraphSweeps) * kGraphSweeps;
   ctx->profiling = false;  // time the production path: graphs of sweeps
-  int best_g = ctx->group, best_f = ctx->flow ? 1 : 0;
+  const int g0 = ctx->group;
+  int best_g = ctx->group, best_f = ctx->small ? 2 : (ctx->flow ? 1 : 0);
   double best_ms = 1e300;
-  for (int f = 1; f >= 0; f--)
+  for (int f = 2; f >= 0; f--)
     for (int v = 0; v < 4; v++) {
-      if (!apply_schedule(ctx, f, options[v])) continue;
+      if (f == 2 && (v > 0 || npt)) continue;  // one variant, NVT only
+      if (!apply_schedule(ctx, f, f == 2 ? ctx->group : options[v])) continue;
       int e = run_sweeps(ctx, sweeps, false, npt, nullptr);
       if (e) {
         ctx->profiling = was_profiling;
@@ -614,18 +666,23 @@ int hsmc_gpu_autotune(hsmc_ctx *ctx, int sweeps_per_variant, int *lanes_out) {
       }
       if (ctx->last_total_ms < best_ms) {
         best_ms = ctx->last_total_ms;
-        best_g = options[v];
+        best_g = f == 2 ? g0 : options[v];
         best_f = f;
       }
     }
   ctx->profiling = was_profiling;
-  apply_schedule(ctx, best_f, best_g);
+  if (best_f == 2) {
+    apply_schedule(ctx, 0, g0);  // the lane mapping the other schedules fall back on
+    ctx->small = true;
+  } else {
+    apply_schedule(ctx, best_f, best_g);
+  }
   if (lanes_out) *lanes_out = best_g;
   return HSMC_OK;
 }
 
 int hsmc_gpu_set_schedule(hsmc_ctx *ctx, int schedule, int lanes_per_cell) {
-  if (!ctx || (schedule != 0 && schedule != 1)) return HSMC_ERR_INVALID_ARG;
+  if (!ctx || schedule < 0 || schedule > 2) return HSMC_ERR_INVALID_ARG;
   const int g = lanes_per_cell == 0 ? ctx->group : lanes_per_cell;
   if (g != 1 && g != 2 && g != 4 && g != 8) return HSMC_ERR_INVALID_ARG;
   return apply_schedule(ctx, schedule, g) ? HSMC_OK : HSMC_ERR_INVALID_ARG;
@@ -641,7 +698,7 @@ int hsmc_gpu_hold_region(hsmc_ctx *ctx, int region) {
 
 int hsmc_gpu_get_schedule(hsmc_ctx *ctx, int *schedule, int *lanes_per_cell) {
   if (!ctx) return HSMC_ERR_INVALID_ARG;
-  if (schedule) *schedule = ctx->flow ? 1 : 0;
+  if (schedule) *schedule = ctx->small ? 2 : (ctx->flow ? 1 : 0);
   if (lanes_per_cell) *lanes_per_cell = ctx->group;
   return HSMC_OK;
 }

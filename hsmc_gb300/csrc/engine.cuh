@@ -106,6 +106,13 @@ int cluster_grid(int n, int ncell, int num_sms);
 cudaError_t launch_cluster(const SysPtrs &p, const ClusterJob &job, int n_moves, int grid, int ncell,
                            cudaStream_t s);
 
+// sweep_small.cu: every sweep of a call in one block with the system in
+// shared memory (0 bytes: the system does not fit); the same chain as the
+// pass-barrier schedule.  The launch leaves the device cell layouts stale.
+size_t sweep_small_smem(int n, int ncell);
+bool prepare_sweep_small(size_t smem);
+void launch_sweep_small(const SysPtrs &p, int n_sweeps, size_t smem, int n_active, cudaStream_t s);
+
 // cavity.cu: the cavity trials of sweep sweep_base + offset (trace: 8 words
 // per trial or nullptr), and psi at n distances
 void launch_cavity(const SysPtrs &p, long long sweep_offset, uint32_t *trace, long long trace_cap, cudaStream_t s);

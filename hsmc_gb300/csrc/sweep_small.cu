@@ -1,0 +1,284 @@
+// Whole checkerboard sweeps of a small system in one block (the "one block"
+// schedule).  The eight launches per sweep of the pass-barrier schedule cost
+// more than the work for a few thousand spheres: launch gaps dominate a
+// sweep of N = 256 to 4000.  Here one launch runs every sweep of a call with
+// the system in shared memory: FP64 positions, their grid coordinates, and a
+// cell list by counting sort (ids ascending within a cell), rebuilt on each
+// sweep's shifted grid; colour passes are separated by block barriers.
+//
+// The chain is the pass-barrier schedule's bit for bit: the same grid
+// shift and colour order per sweep (k_build), the same Philox counters per
+// cell and trial, the particle of rank floor(u n) by id, the same FP64
+// proposal and confinement test, and overlap decisions that are the
+// reference's FP64 test (single precision decides only outside the guard
+// band).  A group of G lanes owns one active cell of a pass, lane k
+// screening neighbour cells k, k + G, ... of the 27 (G from 4 to 32, so that
+// the groups cover the active cells); the cell's neighbours are of other
+// colours, so no other group writes what it reads.
+#include "engine.cuh"
+
+namespace hsmc {
+
+namespace {
+
+struct SmallSweepSm {
+  double *x, *y, *z;   // N positions
+  float *tx, *ty, *tz; // N grid coordinates on the current sweep's grid
+  uint32_t *fill;      // ncell counts, then scatter cursors
+  uint16_t *start;     // ncell + 1 offsets into ids
+  uint16_t *ids;       // N particle ids by cell, ascending within a cell
+};
+
+__device__ __forceinline__ SmallSweepSm small_sweep_sm(unsigned char *raw, int n, int ncell) {
+  SmallSweepSm m;
+  m.x = reinterpret_cast<double *>(raw);
+  m.y = m.x + n;
+  m.z = m.y + n;
+  m.tx = reinterpret_cast<float *>(m.z + n);
+  m.ty = m.tx + n;
+  m.tz = m.ty + n;
+  m.fill = reinterpret_cast<uint32_t *>(m.tz + n);
+  m.start = reinterpret_cast<uint16_t *>(m.fill + ncell);
+  m.ids = m.start + (ncell + 1);
+  return m;
+}
+
+// Exclusive scan of fill[0..ncell) into start (a contiguous chunk per
+// thread, then a block scan of the chunk sums).
+__device__ void scan_cells(const SmallSweepSm &m, int ncell, int n) {
+  const int tid = (int)threadIdx.x, nt = (int)blockDim.x;
+  const int per = (ncell + nt - 1) / nt;
+  const int c0 = tid * per, c1 = min(c0 + per, ncell);
+  uint32_t sum = 0;
+  for (int c = c0; c < c1; c++) sum += m.fill[c];
+  const int lane = tid & 31, w = tid >> 5;
+  uint32_t inc = sum;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    const uint32_t v = __shfl_up_sync(0xffffffffu, inc, o);
+    if (lane >= o) inc += v;
+  }
+  __shared__ uint32_t wsum[32];
+  if (lane == 31) wsum[w] = inc;
+  __syncthreads();
+  if (w == 0) {
+    uint32_t v = lane < (nt >> 5) ? wsum[lane] : 0u;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      const uint32_t u = __shfl_up_sync(0xffffffffu, v, o);
+      if (lane >= o) v += u;
+    }
+    wsum[lane] = v;
+  }
+  __syncthreads();
+  uint32_t run = (w ? wsum[w - 1] : 0u) + inc - sum;
+  for (int c = c0; c < c1; c++) {
+    m.start[c] = (uint16_t)run;
+    run += m.fill[c];
+  }
+  if (tid == nt - 1) m.start[ncell] = (uint16_t)n;
+  __syncthreads();
+}
+
+template <int G>
+__global__ void __launch_bounds__(1024) k_sweep_small(SysPtrs p, int n_sweeps) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  __shared__ float sh_s[3];
+  __shared__ int perm_s[8];
+  DevState *st = p.st;
+  const Box *bx = p.box;
+  const int n = p.n, ncell = bx->ncell, cap = p.cap;
+  const SmallSweepSm m = small_sweep_sm(smem_raw, n, ncell);
+  const int tid = (int)threadIdx.x, nt = (int)blockDim.x;
+  const int nc[3] = {bx->nc[0], bx->nc[1], bx->nc[2]};
+  double len[3], half[3];
+  float L32[3], iw[3];
+  for (int d = 0; d < 3; d++) {
+    len[d] = bx->len[d];
+    half[d] = bx->half[d];
+    L32[d] = bx->len32[d];
+    iw[d] = bx->inv_w32[d];
+  }
+  const float lo = 1.0f - bx->band, hi = 1.0f + bx->band;
+  const double dr = st->dr_max;
+  const unsigned long long seed = st->seed, s0 = st->sweep_base;
+  const int frozen = st->frozen;
+  for (int i = tid; i < n; i += nt) load_xyz(p.pos, i, m.x[i], m.y[i], m.z[i]);
+  unsigned acc = 0, rej_o = 0, rej_b = 0;
+  const int lane = tid % G, grp = tid / G, ngrp = nt / G;
+  const unsigned gmask = G == 32 ? 0xffffffffu : (((1u << G) - 1u) << ((tid & 31) & ~(G - 1)));
+  const int hx = nc[0] >> 1, hy = nc[1] >> 1, hz = nc[2] >> 1, n_active = hx * hy * hz;
+
+  for (int sw = 0; sw < n_sweeps; sw++) {
+    const unsigned long long s = s0 + (unsigned long long)sw;
+    // the sweep's grid shift and colour order, as k_build draws them
+    if (tid == 0) {
+      const U32x4 rs = draw4(seed, 0u, 0u, s, TAG_SHIFT);
+      sh_s[0] = __fmul_rn(__uint2float_rn(rs.x >> 8) * 5.9604644775390625e-08f, bx->w32[0]);
+      sh_s[1] = __fmul_rn(__uint2float_rn(rs.y >> 8) * 5.9604644775390625e-08f, bx->w32[1]);
+      sh_s[2] = __fmul_rn(__uint2float_rn(rs.z >> 8) * 5.9604644775390625e-08f, bx->w32[2]);
+      int perm[8] = {0, 1, 2, 3, 4, 5, 6, 7};
+      const U32x4 ra = draw4(seed, 0u, 0u, s, TAG_PERM), rb = draw4(seed, 1u, 0u, s, TAG_PERM);
+      const uint32_t r[7] = {ra.x, ra.y, ra.z, ra.w, rb.x, rb.y, rb.z};
+      for (int k = 7; k >= 1; k--) {  // Fisher-Yates
+        const int j = (int)__umulhi(r[7 - k], (unsigned)(k + 1));
+        const int tmp = perm[k];
+        perm[k] = perm[j];
+        perm[j] = tmp;
+      }
+      for (int k = 0; k < 8; k++) perm_s[k] = perm[k];
+    }
+    for (int c = tid; c < ncell; c += nt) m.fill[c] = 0u;
+    __syncthreads();
+    const float sh[3] = {sh_s[0], sh_s[1], sh_s[2]};
+    // cells of the shifted grid: counting sort
+    for (int i = tid; i < n; i += nt) {
+      int cx, cy, cz;
+      axis_cell(__double2float_rn(m.x[i]), sh[0], L32[0], iw[0], nc[0], cx, m.tx[i]);
+      axis_cell(__double2float_rn(m.y[i]), sh[1], L32[1], iw[1], nc[1], cy, m.ty[i]);
+      axis_cell(__double2float_rn(m.z[i]), sh[2], L32[2], iw[2], nc[2], cz, m.tz[i]);
+      atomicAdd(m.fill + cx + nc[0] * (cy + nc[1] * cz), 1u);
+    }
+    __syncthreads();
+    for (int c = tid; c < ncell; c += nt)
+      if (m.fill[c] > (uint32_t)cap) atomicOr(&st->status, ST_CELL_OVERFLOW);
+    scan_cells(m, ncell, n);
+    for (int c = tid; c < ncell; c += nt) m.fill[c] = 0u;
+    __syncthreads();
+    for (int i = tid; i < n; i += nt) {
+      int cx, cy, cz;
+      float t;
+      axis_cell(__double2float_rn(m.x[i]), sh[0], L32[0], iw[0], nc[0], cx, t);
+      axis_cell(__double2float_rn(m.y[i]), sh[1], L32[1], iw[1], nc[1], cy, t);
+      axis_cell(__double2float_rn(m.z[i]), sh[2], L32[2], iw[2], nc[2], cz, t);
+      const int c = cx + nc[0] * (cy + nc[1] * cz);
+      m.ids[m.start[c] + atomicAdd(m.fill + c, 1u)] = (uint16_t)i;
+    }
+    __syncthreads();
+    for (int c = tid; c < ncell; c += nt) {  // ids ascending within each cell
+      const int b = m.start[c], e = m.start[c + 1];
+      for (int a = b + 1; a < e; a++) {
+        const uint16_t v = m.ids[a];
+        int q = a - 1;
+        while (q >= b && m.ids[q] > v) {
+          m.ids[q + 1] = m.ids[q];
+          q--;
+        }
+        m.ids[q + 1] = v;
+      }
+    }
+    __syncthreads();
+
+    for (int pass = 0; pass < 8; pass++) {
+      const int colour = perm_s[pass];
+      const unsigned long long seq = s * 8ull + (unsigned long long)pass;
+      for (int ac = grp; ac < n_active; ac += ngrp) {
+        const int ax = ac % hx, ayz = ac / hx, ay = ayz % hy, az = ayz / hy;
+        const int ix = 2 * ax + (colour & 1), iy = 2 * ay + ((colour >> 1) & 1), iz = 2 * az + ((colour >> 2) & 1);
+        const int c = ix + nc[0] * (iy + nc[1] * iz);
+        const int b = m.start[c], cn = m.start[c + 1] - b;
+        if (cn == 0 || cn > cap) continue;  // an overfull cell was flagged above
+        for (int trial = 0; trial < cn; trial++) {
+          // every lane of the group computes the same draw and proposal
+          const U32x4 r = draw4(seed, (uint32_t)trial, (uint32_t)c, seq, TAG_MOVE);
+          const int id = m.ids[b + (int)__umulhi(r.x, (unsigned)cn)];
+          if (id < frozen) continue;  // a cavity: moved by the cavity stage
+          const double nx = propose_axis(m.x[id], centred_offset(r.y), dr, len[0]);
+          const double ny = propose_axis(m.y[id], centred_offset(r.z), dr, len[1]);
+          const double nz = propose_axis(m.z[id], centred_offset(r.w), dr, len[2]);
+          int c0, c1, c2;
+          float ux, uy, uz;
+          axis_cell(__double2float_rn(nx), sh[0], L32[0], iw[0], nc[0], c0, ux);
+          axis_cell(__double2float_rn(ny), sh[1], L32[1], iw[1], nc[1], c1, uy);
+          axis_cell(__double2float_rn(nz), sh[2], L32[2], iw[2], nc[2], c2, uz);
+          if (c0 != ix || c1 != iy || c2 != iz) {
+            if (lane == 0) rej_b++;  // the move would leave the active cell
+            continue;
+          }
+          bool ov = false;
+          for (int o = lane; o < 27 && !ov; o += G) {
+            const int ox = o % 3 - 1, oy = (o / 3) % 3 - 1, oz = o / 9 - 1;
+            int jx = ix + ox, jy = iy + oy, jz = iz + oz;
+            float imx = 0.f, imy = 0.f, imz = 0.f;
+            if (jx < 0) { jx += nc[0]; imx = -L32[0]; } else if (jx >= nc[0]) { jx -= nc[0]; imx = L32[0]; }
+            if (jy < 0) { jy += nc[1]; imy = -L32[1]; } else if (jy >= nc[1]) { jy -= nc[1]; imy = L32[1]; }
+            if (jz < 0) { jz += nc[2]; imz = -L32[2]; } else if (jz >= nc[2]) { jz -= nc[2]; imz = L32[2]; }
+            const int nb = jx + nc[0] * (jy + nc[1] * jz);
+            const int qe = m.start[nb + 1];
+            for (int q = m.start[nb]; q < qe && !ov; q++) {
+              const int j = m.ids[q];
+              if (j == id) continue;
+              const float dx = ux - __fadd_rn(m.tx[j], imx), dy = uy - __fadd_rn(m.ty[j], imy),
+                          dz = uz - __fadd_rn(m.tz[j], imz);
+              const float r2 = dx * dx + dy * dy + dz * dz;
+              if (r2 < lo) ov = true;
+              else if (r2 <= hi) ov = ref_r2(nx, ny, nz, m.x[j], m.y[j], m.z[j], len, half) < 1.0;
+            }
+          }
+          ov = G == 32 ? __any_sync(0xffffffffu, ov) : (__ballot_sync(gmask, ov) & gmask) != 0u;
+          if (ov) {
+            if (lane == 0) rej_o++;
+          } else {
+            if (lane == 0) {
+              m.x[id] = nx;
+              m.y[id] = ny;
+              m.z[id] = nz;
+              m.tx[id] = ux;
+              m.ty[id] = uy;
+              m.tz[id] = uz;
+              acc++;
+            }
+          }
+          __syncwarp(gmask);  // the move is visible to the group's next trial
+        }
+      }
+      __syncthreads();
+    }
+    if (sw == n_sweeps - 1 && tid == 0) {  // the last sweep's layout, as k_build leaves it
+      st->params.sweep = s;
+      for (int d = 0; d < 3; d++) st->params.shift32[d] = sh[d];
+      for (int k = 0; k < 8; k++) st->params.perm[k] = perm_s[k];
+    }
+  }
+  for (int i = tid; i < n; i += nt) {
+    double *q = p.pos + 4 * (size_t)i;
+    q[1] = m.x[i];
+    q[2] = m.y[i];
+    q[3] = m.z[i];
+  }
+  const unsigned long long a = warp_sum_u64(acc), o = warp_sum_u64(rej_o), bd = warp_sum_u64(rej_b);
+  if ((tid & 31) == 0) {
+    if (a) atomicAdd(&st->acc, a);
+    if (o) atomicAdd(&st->rej_overlap, o);
+    if (bd) atomicAdd(&st->rej_boundary, bd);
+  }
+  if (tid == 0) st->sweep_base = s0 + (unsigned long long)n_sweeps;
+}
+
+}  // namespace
+
+size_t sweep_small_smem(int n, int ncell) {
+  if (n > 65535 || ncell > 65534) return 0;
+  const size_t bytes = 38 * (size_t)n + 6 * (size_t)ncell + 16;
+  return bytes <= 200 * 1024 ? bytes : 0;
+}
+
+bool prepare_sweep_small(size_t smem) {
+  if (smem == 0) return false;
+  const int a = (int)smem;
+  return cudaFuncSetAttribute(k_sweep_small<4>, cudaFuncAttributeMaxDynamicSharedMemorySize, a) == cudaSuccess &&
+         cudaFuncSetAttribute(k_sweep_small<8>, cudaFuncAttributeMaxDynamicSharedMemorySize, a) == cudaSuccess &&
+         cudaFuncSetAttribute(k_sweep_small<16>, cudaFuncAttributeMaxDynamicSharedMemorySize, a) == cudaSuccess &&
+         cudaFuncSetAttribute(k_sweep_small<32>, cudaFuncAttributeMaxDynamicSharedMemorySize, a) == cudaSuccess;
+}
+
+// Lanes per cell: the widest group for which the 1024 threads still cover
+// every active cell of a pass at once, at least 4.
+void launch_sweep_small(const SysPtrs &p, int n_sweeps, size_t smem, int n_active, cudaStream_t s) {
+  if (n_active * 32 <= 1024) k_sweep_small<32><<<1, 1024, smem, s>>>(p, n_sweeps);
+  else if (n_active * 16 <= 1024) k_sweep_small<16><<<1, 1024, smem, s>>>(p, n_sweeps);
+  else if (n_active * 8 <= 1024) k_sweep_small<8><<<1, 1024, smem, s>>>(p, n_sweeps);
+  else k_sweep_small<4><<<1, 1024, smem, s>>>(p, n_sweeps);
+}
+
+}  // namespace hsmc

@@ -341,7 +341,8 @@ class HardSphereSystem:
         return lanes.value
 
     def set_schedule(self, schedule: int, lanes_per_cell: int = 0) -> None:
-        """0: one launch per colour pass; 1: dataflow sweep (same chain)."""
+        """0: one launch per colour pass; 1: dataflow sweep; 2: every sweep of
+        a call in one block (small NVT systems).  The same chain."""
         _check(self._lib.hsmc_gpu_set_schedule(self._h, schedule, lanes_per_cell), "hsmc_gpu_set_schedule")
 
     def get_schedule(self):

@@ -287,11 +287,15 @@ int hsmc_gpu_grid_info(hsmc_ctx *ctx, int nc[3], float len32[3], float inv_w32[3
 int hsmc_gpu_autotune(hsmc_ctx *ctx, int sweeps_per_variant, int *lanes_out);
 
 /* Schedule of the eight colour passes of a sweep: 0 = one launch per pass
- * with a kernel boundary between passes (the default); 1 = dataflow, all
- * eight passes in one cooperative launch where a cell waits only for the 26
- * cells around it to finish the previous pass.  Both give the same chain;
- * hsmc_gpu_autotune picks the faster.  lanes_per_cell 0 keeps the current
- * mapping. */
+ * with a kernel boundary between passes; 1 = dataflow, all eight passes in
+ * one cooperative launch where a cell waits only for the 26 cells around it
+ * to finish the previous pass; 2 = one block, every sweep of a call in one
+ * launch with the system in shared memory (NVT systems of up to a few
+ * thousand spheres; the default up to 64 active cells per pass, about 500
+ * spheres, where it is faster, else 0).  All give the same
+ * chain; hsmc_gpu_autotune picks the fastest.  lanes_per_cell 0 keeps the
+ * current mapping (schedule 2 has none).  Traced and profiled sweeps, NpT
+ * sweeps and cavity runs use schedule 0 or 1. */
 int hsmc_gpu_set_schedule(hsmc_ctx *ctx, int schedule, int lanes_per_cell);
 int hsmc_gpu_get_schedule(hsmc_ctx *ctx, int *schedule, int *lanes_per_cell);
 

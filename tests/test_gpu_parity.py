@@ -102,6 +102,7 @@ def test_chain_independent_of_lane_mapping(gpu_lib):
     finals = []
     for lanes in (1, 2, 4, 8):
         g = gpu_lib.HardSphereSystem(rho=0.8, cells=8, dr_max=0.15, seed=123, lanes_per_cell=lanes)
+        g.set_schedule(0)  # the pass-barrier launches, where the lane mapping applies
         c = g.sweep_nvt(37)
         finals.append((g.download(), c.copy()))
     for conf, c in finals[1:]:
@@ -212,6 +213,43 @@ def test_dataflow_schedule_is_the_pass_barrier_chain(gpu_lib, lanes):
         confs.append((s.download(), c))
     assert np.array_equal(confs[0][0], confs[1][0])
     assert np.array_equal(confs[0][1], confs[1][1])
+
+
+@pytest.mark.parametrize("rho,cells,lt,dr,seed,edge", [
+    (0.80, 8, 2, 0.15, 42, 0.0),   # N = 2048 fluid
+    (0.50, 10, 2, 0.30, 7, 0.0),   # N = 4000, the C1 density
+    (0.94, 5, 2, 0.06, 3, 0.0),    # dense crystal
+    (0.30, 6, 1, 0.40, 11, 1.6),   # 32-slot cells
+    (0.85, 4, 2, 0.12, 5, 0.0),    # N = 256, six cells per side
+])
+def test_one_block_schedule_is_the_pass_barrier_chain(gpu_lib, rho, cells, lt, dr, seed, edge):
+    """Every sweep of a call in one block with the system in shared memory
+    gives the chain of one launch per pass bit for bit, counters included,
+    and leaves observables and later sweeps of the other schedule unchanged."""
+    runs = []
+    for schedule in (0, 2):
+        s = gpu_lib.HardSphereSystem(rho=rho, cells=cells, lattice_type=lt, dr_max=dr, seed=seed,
+                                     min_cell_edge=edge)
+        s.set_schedule(schedule)
+        assert s.get_schedule()[0] == schedule
+        c1 = s.sweep_nvt(19)
+        c2 = s.sweep_nvt(8)
+        s.set_schedule(0)
+        c3 = s.sweep_nvt(3)
+        runs.append((s.download(), c1, c2, c3, s.compute_rdf_counts(0.02, 2.0, 50)))
+    for a, b in zip(runs[0], runs[1]):
+        assert np.array_equal(a, b)
+
+
+def test_one_block_schedule_is_the_default_for_small_systems(gpu_lib):
+    small = gpu_lib.HardSphereSystem(rho=0.85, cells=4, dr_max=0.12, seed=1)
+    assert small.get_schedule()[0] == 2
+    mid = gpu_lib.HardSphereSystem(rho=0.5, cells=10, dr_max=0.3, seed=1)  # fits, but one launch per pass is faster
+    assert mid.get_schedule()[0] == 0
+    big = gpu_lib.HardSphereSystem(rho=0.85, cells=20, dr_max=0.12, seed=1)
+    assert big.get_schedule()[0] == 0
+    npt = gpu_lib.HardSphereSystem(rho=0.85, cells=6, dr_max=0.12, dv_max=0.01, pressure=8.0, seed=1)
+    assert npt.get_schedule()[0] == 0
 
 
 def test_dataflow_schedule_npt_matches(gpu_lib):
