@@ -330,9 +330,9 @@ int hsmc_gpu_create(const hsmc_params *prm, hsmc_ctx **out) {
     cudaGetLastError();
   }
   // the default where it measured faster than one launch per pass: at most
-  // 64 active cells per pass (up to about 500 spheres); the autotuner tries
-  // it wherever it fits
-  ctx->small = ctx->small_smem > 0 && b.ncell / 8 <= 64;
+  // 128 active cells per pass (up to about 1000 spheres); the autotuner
+  // tries it wherever it fits
+  ctx->small = ctx->small_smem > 0 && b.ncell / 8 <= 128;
   *out = ctx;
   return HSMC_OK;
 }

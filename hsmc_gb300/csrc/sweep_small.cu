@@ -11,10 +11,13 @@
 // cell and trial, the particle of rank floor(u n) by id, the same FP64
 // proposal and confinement test, and overlap decisions that are the
 // reference's FP64 test (single precision decides only outside the guard
-// band).  A group of G lanes owns one active cell of a pass, lane k
-// screening neighbour cells k, k + G, ... of the 27 (G from 4 to 32, so that
-// the groups cover the active cells); the cell's neighbours are of other
-// colours, so no other group writes what it reads.
+// band).  A pass runs in rounds, round t making trial t of every active
+// cell that has one: one thread per cell draws and proposes (so one warp's
+// FP64 sequence serves 32 cells: GB300's FP64 pipe is busy per warp
+// instruction), then one warp per cell screens it, lane k on neighbour
+// cell k of the 27, and the cell's thread applies an accepted move at the
+// start of the next round.  A cell's trials stay in order; its neighbours
+// are of other colours, so no other cell writes what it reads.
 #include "engine.cuh"
 
 namespace hsmc {
@@ -22,24 +25,36 @@ namespace hsmc {
 namespace {
 
 struct SmallSweepSm {
-  double *x, *y, *z;   // N positions
-  float *tx, *ty, *tz; // N grid coordinates on the current sweep's grid
-  uint32_t *fill;      // ncell counts, then scatter cursors
-  uint16_t *start;     // ncell + 1 offsets into ids
-  uint16_t *ids;       // N particle ids by cell, ascending within a cell
+  double *x, *y, *z;     // N positions
+  double *px, *py, *pz;  // per active cell: this round's trial position
+  float *tx, *ty, *tz;   // N grid coordinates on the current sweep's grid
+  float *ux, *uy, *uz;   // per active cell: the trial's grid coordinates
+  uint32_t *fill;        // ncell counts, then scatter cursors
+  uint16_t *start;       // ncell + 1 offsets into ids
+  uint16_t *ids;         // N particle ids by cell, ascending within a cell
+  uint16_t *tid_;        // per active cell: the trial's particle
+  uint8_t *state;        // per active cell: 0 no trial to screen, 1 screen it, 2 overlap found
 };
 
-__device__ __forceinline__ SmallSweepSm small_sweep_sm(unsigned char *raw, int n, int ncell) {
+__device__ __forceinline__ SmallSweepSm small_sweep_sm(unsigned char *raw, int n, int ncell, int na) {
   SmallSweepSm m;
   m.x = reinterpret_cast<double *>(raw);
   m.y = m.x + n;
   m.z = m.y + n;
-  m.tx = reinterpret_cast<float *>(m.z + n);
+  m.px = m.z + n;
+  m.py = m.px + na;
+  m.pz = m.py + na;
+  m.tx = reinterpret_cast<float *>(m.pz + na);
   m.ty = m.tx + n;
   m.tz = m.ty + n;
-  m.fill = reinterpret_cast<uint32_t *>(m.tz + n);
+  m.ux = m.tz + n;
+  m.uy = m.ux + na;
+  m.uz = m.uy + na;
+  m.fill = reinterpret_cast<uint32_t *>(m.uz + na);
   m.start = reinterpret_cast<uint16_t *>(m.fill + ncell);
   m.ids = m.start + (ncell + 1);
+  m.tid_ = m.ids + n;
+  m.state = reinterpret_cast<uint8_t *>(m.tid_ + na);
   return m;
 }
 
@@ -80,7 +95,6 @@ __device__ void scan_cells(const SmallSweepSm &m, int ncell, int n) {
   __syncthreads();
 }
 
-template <int G>
 __global__ void __launch_bounds__(1024) k_sweep_small(SysPtrs p, int n_sweeps) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   __shared__ float sh_s[3];
@@ -88,7 +102,9 @@ __global__ void __launch_bounds__(1024) k_sweep_small(SysPtrs p, int n_sweeps) {
   DevState *st = p.st;
   const Box *bx = p.box;
   const int n = p.n, ncell = bx->ncell, cap = p.cap;
-  const SmallSweepSm m = small_sweep_sm(smem_raw, n, ncell);
+  const int n_active = (bx->nc[0] >> 1) * (bx->nc[1] >> 1) * (bx->nc[2] >> 1);
+  const SmallSweepSm m = small_sweep_sm(smem_raw, n, ncell, n_active);
+  __shared__ int max_cn[8];  // per colour: the most trials any of its cells makes
   const int tid = (int)threadIdx.x, nt = (int)blockDim.x;
   const int nc[3] = {bx->nc[0], bx->nc[1], bx->nc[2]};
   double len[3], half[3];
@@ -105,9 +121,8 @@ __global__ void __launch_bounds__(1024) k_sweep_small(SysPtrs p, int n_sweeps) {
   const int frozen = st->frozen;
   for (int i = tid; i < n; i += nt) load_xyz(p.pos, i, m.x[i], m.y[i], m.z[i]);
   unsigned acc = 0, rej_o = 0, rej_b = 0;
-  const int lane = tid % G, grp = tid / G, ngrp = nt / G;
-  const unsigned gmask = G == 32 ? 0xffffffffu : (((1u << G) - 1u) << ((tid & 31) & ~(G - 1)));
-  const int hx = nc[0] >> 1, hy = nc[1] >> 1, hz = nc[2] >> 1, n_active = hx * hy * hz;
+  const int lane = tid & 31, wid = tid >> 5, nw = nt >> 5;
+  const int hx = nc[0] >> 1, hy = nc[1] >> 1;
 
   for (int sw = 0; sw < n_sweeps; sw++) {
     const unsigned long long s = s0 + (unsigned long long)sw;
@@ -140,8 +155,17 @@ __global__ void __launch_bounds__(1024) k_sweep_small(SysPtrs p, int n_sweeps) {
       atomicAdd(m.fill + cx + nc[0] * (cy + nc[1] * cz), 1u);
     }
     __syncthreads();
-    for (int c = tid; c < ncell; c += nt)
-      if (m.fill[c] > (uint32_t)cap) atomicOr(&st->status, ST_CELL_OVERFLOW);
+    if (tid < 8) max_cn[tid] = 0;
+    __syncthreads();
+    for (int c = tid; c < ncell; c += nt) {
+      const uint32_t k = m.fill[c];
+      if (k > (uint32_t)cap) {
+        atomicOr(&st->status, ST_CELL_OVERFLOW);
+      } else if (k > 0) {
+        const int cx = c % nc[0], cyz = c / nc[0], cy = cyz % nc[1], cz = cyz / nc[1];
+        atomicMax(max_cn + cell_colour(cx, cy, cz), (int)k);
+      }
+    }
     scan_cells(m, ncell, n);
     for (int c = tid; c < ncell; c += nt) m.fill[c] = 0u;
     __syncthreads();
@@ -172,33 +196,80 @@ __global__ void __launch_bounds__(1024) k_sweep_small(SysPtrs p, int n_sweeps) {
     for (int pass = 0; pass < 8; pass++) {
       const int colour = perm_s[pass];
       const unsigned long long seq = s * 8ull + (unsigned long long)pass;
-      for (int ac = grp; ac < n_active; ac += ngrp) {
-        const int ax = ac % hx, ayz = ac / hx, ay = ayz % hy, az = ayz / hy;
-        const int ix = 2 * ax + (colour & 1), iy = 2 * ay + ((colour >> 1) & 1), iz = 2 * az + ((colour >> 2) & 1);
-        const int c = ix + nc[0] * (iy + nc[1] * iz);
-        const int b = m.start[c], cn = m.start[c + 1] - b;
-        if (cn == 0 || cn > cap) continue;  // an overfull cell was flagged above
-        for (int trial = 0; trial < cn; trial++) {
-          // every lane of the group computes the same draw and proposal
-          const U32x4 r = draw4(seed, (uint32_t)trial, (uint32_t)c, seq, TAG_MOVE);
-          const int id = m.ids[b + (int)__umulhi(r.x, (unsigned)cn)];
-          if (id < frozen) continue;  // a cavity: moved by the cavity stage
-          const double nx = propose_axis(m.x[id], centred_offset(r.y), dr, len[0]);
-          const double ny = propose_axis(m.y[id], centred_offset(r.z), dr, len[1]);
-          const double nz = propose_axis(m.z[id], centred_offset(r.w), dr, len[2]);
-          int c0, c1, c2;
-          float ux, uy, uz;
-          axis_cell(__double2float_rn(nx), sh[0], L32[0], iw[0], nc[0], c0, ux);
-          axis_cell(__double2float_rn(ny), sh[1], L32[1], iw[1], nc[1], c1, uy);
-          axis_cell(__double2float_rn(nz), sh[2], L32[2], iw[2], nc[2], c2, uz);
-          if (c0 != ix || c1 != iy || c2 != iz) {
-            if (lane == 0) rej_b++;  // the move would leave the active cell
-            continue;
+      // this thread's cell (n_active <= blockDim.x)
+      const bool own = tid < n_active;
+      int ix = 0, iy = 0, iz = 0, c = 0, b = 0, cn = 0;
+      if (own) {
+        const int ax = tid % hx, ayz = tid / hx, ay = ayz % hy, az = ayz / hy;
+        ix = 2 * ax + (colour & 1);
+        iy = 2 * ay + ((colour >> 1) & 1);
+        iz = 2 * az + ((colour >> 2) & 1);
+        c = ix + nc[0] * (iy + nc[1] * iz);
+        b = m.start[c];
+        cn = m.start[c + 1] - b;
+        if (cn > cap) cn = 0;  // an overfull cell was flagged above
+      }
+      const int rounds = max_cn[colour];
+      U32x4 r = draw4(seed, 0u, (uint32_t)c, seq, TAG_MOVE);  // round 0's draws
+      for (int round = 0; round <= rounds; round++) {
+        // the cell's thread: apply the previous round's accepted move, then
+        // draw and propose this round's trial
+        if (own) {
+          const int st_prev = round > 0 ? m.state[tid] : 0;
+          if (st_prev == 1) {
+            const int id = m.tid_[tid];
+            m.x[id] = m.px[tid];
+            m.y[id] = m.py[tid];
+            m.z[id] = m.pz[tid];
+            m.tx[id] = m.ux[tid];
+            m.ty[id] = m.uy[tid];
+            m.tz[id] = m.uz[tid];
+            acc++;
+          } else if (st_prev == 2) {
+            rej_o++;
           }
+          uint8_t state = 0;
+          if (round < cn) {
+            const int id = m.ids[b + (int)__umulhi(r.x, (unsigned)cn)];
+            if (id >= frozen) {  // a cavity is moved by the cavity stage
+              const double nx = propose_axis(m.x[id], centred_offset(r.y), dr, len[0]);
+              const double ny = propose_axis(m.y[id], centred_offset(r.z), dr, len[1]);
+              const double nz = propose_axis(m.z[id], centred_offset(r.w), dr, len[2]);
+              int c0, c1, c2;
+              float ux, uy, uz;
+              axis_cell(__double2float_rn(nx), sh[0], L32[0], iw[0], nc[0], c0, ux);
+              axis_cell(__double2float_rn(ny), sh[1], L32[1], iw[1], nc[1], c1, uy);
+              axis_cell(__double2float_rn(nz), sh[2], L32[2], iw[2], nc[2], c2, uz);
+              if (c0 != ix || c1 != iy || c2 != iz) {
+                rej_b++;  // the move would leave the active cell
+              } else {
+                m.px[tid] = nx;
+                m.py[tid] = ny;
+                m.pz[tid] = nz;
+                m.ux[tid] = ux;
+                m.uy[tid] = uy;
+                m.uz[tid] = uz;
+                m.tid_[tid] = (uint16_t)id;
+                state = 1;
+              }
+            }
+          }
+          m.state[tid] = state;
+          // the next round's draws, while the screening runs
+          if (round + 1 < cn) r = draw4(seed, (uint32_t)(round + 1), (uint32_t)c, seq, TAG_MOVE);
+        }
+        __syncthreads();
+        if (round == rounds) break;
+        // one warp per cell with a trial: lane k screens neighbour cell k
+        for (int ac = wid; ac < n_active; ac += nw) {
+          if (m.state[ac] != 1) continue;
+          const int ax = ac % hx, ayz = ac / hx, ay = ayz % hy, az = ayz / hy;
+          const int jx0 = 2 * ax + (colour & 1), jy0 = 2 * ay + ((colour >> 1) & 1), jz0 = 2 * az + ((colour >> 2) & 1);
+          const int id = m.tid_[ac];
+          const float ux = m.ux[ac], uy = m.uy[ac], uz = m.uz[ac];
           bool ov = false;
-          for (int o = lane; o < 27 && !ov; o += G) {
-            const int ox = o % 3 - 1, oy = (o / 3) % 3 - 1, oz = o / 9 - 1;
-            int jx = ix + ox, jy = iy + oy, jz = iz + oz;
+          if (lane < 27) {
+            int jx = jx0 + lane % 3 - 1, jy = jy0 + (lane / 3) % 3 - 1, jz = jz0 + lane / 9 - 1;
             float imx = 0.f, imy = 0.f, imz = 0.f;
             if (jx < 0) { jx += nc[0]; imx = -L32[0]; } else if (jx >= nc[0]) { jx -= nc[0]; imx = L32[0]; }
             if (jy < 0) { jy += nc[1]; imy = -L32[1]; } else if (jy >= nc[1]) { jy -= nc[1]; imy = L32[1]; }
@@ -212,25 +283,13 @@ __global__ void __launch_bounds__(1024) k_sweep_small(SysPtrs p, int n_sweeps) {
                           dz = uz - __fadd_rn(m.tz[j], imz);
               const float r2 = dx * dx + dy * dy + dz * dz;
               if (r2 < lo) ov = true;
-              else if (r2 <= hi) ov = ref_r2(nx, ny, nz, m.x[j], m.y[j], m.z[j], len, half) < 1.0;
+              else if (r2 <= hi)
+                ov = ref_r2(m.px[ac], m.py[ac], m.pz[ac], m.x[j], m.y[j], m.z[j], len, half) < 1.0;
             }
           }
-          ov = G == 32 ? __any_sync(0xffffffffu, ov) : (__ballot_sync(gmask, ov) & gmask) != 0u;
-          if (ov) {
-            if (lane == 0) rej_o++;
-          } else {
-            if (lane == 0) {
-              m.x[id] = nx;
-              m.y[id] = ny;
-              m.z[id] = nz;
-              m.tx[id] = ux;
-              m.ty[id] = uy;
-              m.tz[id] = uz;
-              acc++;
-            }
-          }
-          __syncwarp(gmask);  // the move is visible to the group's next trial
+          if (__any_sync(0xffffffffu, ov) && lane == 0) m.state[ac] = 2;
         }
+        __syncthreads();
       }
       __syncthreads();
     }
@@ -258,27 +317,22 @@ __global__ void __launch_bounds__(1024) k_sweep_small(SysPtrs p, int n_sweeps) {
 }  // namespace
 
 size_t sweep_small_smem(int n, int ncell) {
-  if (n > 65535 || ncell > 65534) return 0;
-  const size_t bytes = 38 * (size_t)n + 6 * (size_t)ncell + 16;
-  return bytes <= 200 * 1024 ? bytes : 0;
+  const int na = ncell / 8;  // active cells per pass (even counts per axis)
+  if (n > 65535 || ncell > 65534 || na > 1024) return 0;
+  // per particle: x, y, z, tx, ty, tz, id; per cell: count, offset; per
+  // active cell: trial position, grid coordinates, particle, state
+  const size_t bytes = 38 * (size_t)n + 6 * (size_t)ncell + 39 * (size_t)na + 32;
+  return bytes <= 224 * 1024 ? bytes : 0;  // of the 227 KB a block may have
 }
 
 bool prepare_sweep_small(size_t smem) {
-  if (smem == 0) return false;
-  const int a = (int)smem;
-  return cudaFuncSetAttribute(k_sweep_small<4>, cudaFuncAttributeMaxDynamicSharedMemorySize, a) == cudaSuccess &&
-         cudaFuncSetAttribute(k_sweep_small<8>, cudaFuncAttributeMaxDynamicSharedMemorySize, a) == cudaSuccess &&
-         cudaFuncSetAttribute(k_sweep_small<16>, cudaFuncAttributeMaxDynamicSharedMemorySize, a) == cudaSuccess &&
-         cudaFuncSetAttribute(k_sweep_small<32>, cudaFuncAttributeMaxDynamicSharedMemorySize, a) == cudaSuccess;
+  return smem > 0 && cudaFuncSetAttribute(k_sweep_small, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) ==
+                         cudaSuccess;
 }
 
-// Lanes per cell: the widest group for which the 1024 threads still cover
-// every active cell of a pass at once, at least 4.
 void launch_sweep_small(const SysPtrs &p, int n_sweeps, size_t smem, int n_active, cudaStream_t s) {
-  if (n_active * 32 <= 1024) k_sweep_small<32><<<1, 1024, smem, s>>>(p, n_sweeps);
-  else if (n_active * 16 <= 1024) k_sweep_small<16><<<1, 1024, smem, s>>>(p, n_sweeps);
-  else if (n_active * 8 <= 1024) k_sweep_small<8><<<1, 1024, smem, s>>>(p, n_sweeps);
-  else k_sweep_small<4><<<1, 1024, smem, s>>>(p, n_sweeps);
+  (void)n_active;
+  k_sweep_small<<<1, 1024, smem, s>>>(p, n_sweeps);
 }
 
 }  // namespace hsmc

@@ -291,8 +291,8 @@ int hsmc_gpu_autotune(hsmc_ctx *ctx, int sweeps_per_variant, int *lanes_out);
  * one cooperative launch where a cell waits only for the 26 cells around it
  * to finish the previous pass; 2 = one block, every sweep of a call in one
  * launch with the system in shared memory (NVT systems of up to a few
- * thousand spheres; the default up to 64 active cells per pass, about 500
- * spheres, where it is faster, else 0).  All give the same
+ * thousand spheres; the default up to 128 active cells per pass, about
+ * 1000 spheres, where it is faster, else 0).  All give the same
  * chain; hsmc_gpu_autotune picks the fastest.  lanes_per_cell 0 keeps the
  * current mapping (schedule 2 has none).  Traced and profiled sweeps, NpT
  * sweeps and cavity runs use schedule 0 or 1. */
