@@ -542,6 +542,47 @@ def run_npt(args):
     return 0
 
 
+def run_small(args):
+    """The reference's own run sizes (its README tables use N = 256 to
+    1000; the first benchmark configuration is N = 4000): NVT sweeps/s with
+    the default schedule of each size (one block up to about 1000 spheres,
+    one launch per pass above), through the C ABI, against the oracle's
+    sweeps (the reference's algorithm) on one host core."""
+    from hsmc_gb300 import HardSphereSystem
+    from oracle.oracle import OracleSim
+
+    cases = [(0.85, 4, 2), (0.50, 5, 2), (0.80, 10, 1), (0.50, 10, 2)]
+    out = []
+    for rho, cells, lt in cases:
+        g = HardSphereSystem(rho=rho, cells=cells, lattice_type=lt, dr_max=0.15, seed=5)
+        g.sweep_nvt(200)
+        k = 4000 if g.n < 1000 else 1600
+        t0 = time.perf_counter()
+        g.sweep_nvt(k)
+        dt = time.perf_counter() - t0
+        row = {"N": g.n, "rho": rho, "schedule": ["one launch per pass", "dataflow", "one block"][g.get_schedule()[0]],
+               "gpu_us_per_sweep": dt / k * 1e6, "gpu_moves_per_s": g.n * k / dt}
+        if not args.no_cpu_baseline:
+            o = OracleSim(rho=rho, n_cells=cells, lattice_type=lt, seed=3, dr_max=0.15, neigh_dr=1.05)
+            o.sweeps_nvt(20)
+            t0, kc = time.perf_counter(), 0
+            while time.perf_counter() - t0 < 3.0:
+                o.sweeps_nvt(10)
+                kc += 10
+            dtc = time.perf_counter() - t0
+            row.update({"cpu_us_per_sweep": dtc / kc * 1e6, "cpu_moves_per_s": o.n * kc / dtc,
+                        "gpu_over_cpu": (dtc / kc) / (dt / k)})
+        out.append(row)
+    line = {"metric": "NVT sweeps at the reference's own sizes", "value": out[0]["gpu_moves_per_s"],
+            "unit": "trial moves/s (N=256)", "n_gpus": 1, "higher_is_better": True, "dtype": "f64",
+            "data": "synthetic (lattice starts)",
+            "config": {"workload": "NVT sweeps, N = 256, 500, 1000, 4000, dr_max 0.15",
+                       "timing": "host wall-clock around synchronous calls; CPU: oracle port, one core"},
+            "sizes": out}
+    print(json.dumps(line), flush=True)
+    return 0
+
+
 def run_cavity(args):
     """Torrie-Patey cavity sampling (src/cavity_nvt.c) at the reference's own
     published case: rho = 0.8, 1000 spheres (simple-cubic 10^3 start),
@@ -694,7 +735,7 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
-    ap.add_argument("--workload", default="fluid", choices=["fluid", "replicas", "widom", "npt", "cluster", "cavity"])
+    ap.add_argument("--workload", default="fluid", choices=["fluid", "replicas", "widom", "npt", "cluster", "cavity", "small"])
     ap.add_argument("--replicas", type=int, default=512)
     ap.add_argument("--cell-edge", default="0",
                     help='replicas: smallest device-cell edge, a number or "auto" (min(rho^-1/3, 1.4))')
@@ -716,6 +757,8 @@ def main():
         return run_cluster(args)
     if args.workload == "cavity":
         return run_cavity(args)
+    if args.workload == "small":
+        return run_small(args)
     return run_gpu_arm(args)
 
 

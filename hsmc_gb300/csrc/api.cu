@@ -325,7 +325,7 @@ int hsmc_gpu_create(const hsmc_params *prm, hsmc_ctx **out) {
   ctx->cavity = cavity;
   // a system that fits one block's shared memory runs its NVT sweeps there
   if (!cavity && prm->pressure <= 0) {
-    const size_t sm = sweep_small_smem(ctx->n, b.ncell);
+    const size_t sm = sweep_small_smem(ctx->n, b.ncell, cap);
     if (sm > 0 && prepare_sweep_small(sm)) ctx->small_smem = sm;
     cudaGetLastError();
   }

@@ -109,7 +109,7 @@ cudaError_t launch_cluster(const SysPtrs &p, const ClusterJob &job, int n_moves,
 // sweep_small.cu: every sweep of a call in one block with the system in
 // shared memory (0 bytes: the system does not fit); the same chain as the
 // pass-barrier schedule.  The launch leaves the device cell layouts stale.
-size_t sweep_small_smem(int n, int ncell);
+size_t sweep_small_smem(int n, int ncell, int cap);
 bool prepare_sweep_small(size_t smem);
 void launch_sweep_small(const SysPtrs &p, int n_sweeps, size_t smem, int n_active, cudaStream_t s);
 

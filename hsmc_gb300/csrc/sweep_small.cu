@@ -34,10 +34,13 @@ struct SmallSweepSm {
   uint16_t *ids;         // N particle ids by cell, ascending within a cell
   uint16_t *tid_;        // per active cell: the trial's particle
   uint8_t *state;        // per active cell: 0 no trial to screen, 1 screen it, 2 overlap found
+  uint4 *draws;          // per active cell and trial (cap of them): the pass's Philox draws
 };
 
-__device__ __forceinline__ SmallSweepSm small_sweep_sm(unsigned char *raw, int n, int ncell, int na) {
+__device__ __forceinline__ SmallSweepSm small_sweep_sm(unsigned char *raw, int n, int ncell, int na, int cap) {
   SmallSweepSm m;
+  m.draws = reinterpret_cast<uint4 *>(raw);  // 16-byte aligned first
+  raw += 16 * (size_t)na * cap;
   m.x = reinterpret_cast<double *>(raw);
   m.y = m.x + n;
   m.z = m.y + n;
@@ -103,7 +106,7 @@ __global__ void __launch_bounds__(1024) k_sweep_small(SysPtrs p, int n_sweeps) {
   const Box *bx = p.box;
   const int n = p.n, ncell = bx->ncell, cap = p.cap;
   const int n_active = (bx->nc[0] >> 1) * (bx->nc[1] >> 1) * (bx->nc[2] >> 1);
-  const SmallSweepSm m = small_sweep_sm(smem_raw, n, ncell, n_active);
+  const SmallSweepSm m = small_sweep_sm(smem_raw, n, ncell, n_active, cap);
   __shared__ int max_cn[8];  // per colour: the most trials any of its cells makes
   const int tid = (int)threadIdx.x, nt = (int)blockDim.x;
   const int nc[3] = {bx->nc[0], bx->nc[1], bx->nc[2]};
@@ -210,7 +213,16 @@ __global__ void __launch_bounds__(1024) k_sweep_small(SysPtrs p, int n_sweeps) {
         if (cn > cap) cn = 0;  // an overfull cell was flagged above
       }
       const int rounds = max_cn[colour];
-      U32x4 r = draw4(seed, 0u, (uint32_t)c, seq, TAG_MOVE);  // round 0's draws
+      // every trial's draws of the pass at once, one thread per (cell,
+      // trial), off the rounds' critical path
+      for (int k = tid; k < n_active * rounds; k += nt) {
+        const int a = k % n_active, t = k / n_active;
+        const int ax = a % hx, ayz = a / hx, ay = ayz % hy, az = ayz / hy;
+        const int ca = (2 * ax + (colour & 1)) + nc[0] * ((2 * ay + ((colour >> 1) & 1)) + nc[1] * (2 * az + ((colour >> 2) & 1)));
+        const U32x4 d = draw4(seed, (uint32_t)t, (uint32_t)ca, seq, TAG_MOVE);
+        m.draws[a * cap + t] = make_uint4(d.x, d.y, d.z, d.w);
+      }
+      __syncthreads();
       for (int round = 0; round <= rounds; round++) {
         // the cell's thread: apply the previous round's accepted move, then
         // draw and propose this round's trial
@@ -230,6 +242,7 @@ __global__ void __launch_bounds__(1024) k_sweep_small(SysPtrs p, int n_sweeps) {
           }
           uint8_t state = 0;
           if (round < cn) {
+            const uint4 r = m.draws[tid * cap + round];
             const int id = m.ids[b + (int)__umulhi(r.x, (unsigned)cn)];
             if (id >= frozen) {  // a cavity is moved by the cavity stage
               const double nx = propose_axis(m.x[id], centred_offset(r.y), dr, len[0]);
@@ -255,8 +268,6 @@ __global__ void __launch_bounds__(1024) k_sweep_small(SysPtrs p, int n_sweeps) {
             }
           }
           m.state[tid] = state;
-          // the next round's draws, while the screening runs
-          if (round + 1 < cn) r = draw4(seed, (uint32_t)(round + 1), (uint32_t)c, seq, TAG_MOVE);
         }
         __syncthreads();
         if (round == rounds) break;
@@ -316,12 +327,13 @@ __global__ void __launch_bounds__(1024) k_sweep_small(SysPtrs p, int n_sweeps) {
 
 }  // namespace
 
-size_t sweep_small_smem(int n, int ncell) {
+size_t sweep_small_smem(int n, int ncell, int cap) {
   const int na = ncell / 8;  // active cells per pass (even counts per axis)
   if (n > 65535 || ncell > 65534 || na > 1024) return 0;
   // per particle: x, y, z, tx, ty, tz, id; per cell: count, offset; per
-  // active cell: trial position, grid coordinates, particle, state
-  const size_t bytes = 38 * (size_t)n + 6 * (size_t)ncell + 39 * (size_t)na + 32;
+  // active cell: trial position, grid coordinates, particle, state, and the
+  // draws of up to cap trials
+  const size_t bytes = 38 * (size_t)n + 6 * (size_t)ncell + 39 * (size_t)na + 16 * (size_t)na * cap + 32;
   return bytes <= 224 * 1024 ? bytes : 0;  // of the 227 KB a block may have
 }
 
