@@ -217,7 +217,7 @@ def test_dataflow_schedule_is_the_pass_barrier_chain(gpu_lib, lanes):
 
 @pytest.mark.parametrize("rho,cells,lt,dr,seed,edge", [
     (0.80, 8, 2, 0.15, 42, 0.0),   # N = 2048 fluid
-    (0.50, 8, 2, 0.30, 7, 0.0),    # N = 2048 at the C1 density
+    (0.50, 7, 2, 0.30, 7, 0.0),    # N = 1372 at the C1 density
     (0.94, 5, 2, 0.06, 3, 0.0),    # dense crystal
     (0.30, 6, 1, 0.40, 11, 1.6),   # 32-slot cells
     (0.85, 4, 2, 0.12, 5, 0.0),    # N = 256, six cells per side
