@@ -542,6 +542,104 @@ def run_npt(args):
     return 0
 
 
+# The reference's published state points (its README tables, N = 256): NVT
+# virial pressure by packing fraction, NpT packing fraction by pressure, and
+# Widom chemical potential by density, with the reference's own values.
+README_NVT = [(0.25, 1.468, "1.47(37)"), (0.30, 2.278, "2.28(47)"), (0.35, 3.480, "3.47(77)"),
+              (0.40, 5.291, "5.27(95)"), (0.45, 8.066, "8.0(14)")]
+README_NPT = [(1.472, "0.251(8)", 0.249), (2.280, "0.30(12)", 0.300), (3.471, "0.35(10)", 0.349),
+              (5.274, "0.40(12)", 0.399)]  # pressure, the reference's packing fraction, BHMJ's
+README_MU = [(0.1, 0.464, 62.0), (0.3, 1.754, 17.0), (0.5, 3.856, 2.2), (0.7, 6.656, 0.1)]
+
+
+def run_readme(args):
+    """The reference's own published tables rerun on the device at their
+    size (N = 256, FCC 4^3 starts): NVT virial pressure (32 replicas per
+    packing fraction in one batch, contact fit per replica), NpT packing
+    fraction (dr_max by the reference's optimiser; dv_max by a bounded
+    proportional rule toward 40 % volume acceptance, because the reference's
+    secant on dv_max can overshoot into a frozen box at N = 256), and the
+    Widom chemical potential; beside them the reference's values (its README),
+    BHMJ's packing fractions it quotes, and Carnahan-Starling."""
+    import numpy as np
+    from hsmc_gb300 import HardSphereSystem
+    from hsmc_gb300.batch import ReplicaBatch, carnahan_starling, contact_z
+
+    t_all = time.perf_counter()
+    per, reps = 32, 32
+    systems = [(6.0 * eta / math.pi, 4, 0.2, 7000 + 100 * k + r)
+               for k, (eta, _, _) in enumerate(README_NVT) for r in range(reps)]
+    b = ReplicaBatch(systems)
+    b.tune_steps(0.2, target=TARGET_ACC)
+    b.sweeps(2000)
+    nb, bin_ = 5, 0.01
+    samples, every = 2000, 10
+    cnt = np.zeros((len(systems), nb))
+    for _ in range(samples):
+        b.sweeps(every)
+        cnt += b.pressv_counts(bin_, 1.0 + nb * bin_, nb)
+    nvt = []
+    for k, (eta, p_cs, p_ref) in enumerate(README_NVT):
+        rho = 6.0 * eta / math.pi
+        z = np.array([contact_z(cnt[k * reps + r], samples, b.n[k * reps + r], rho, bin_) for r in range(reps)])
+        p = rho * z
+        nvt.append({"packing_fraction": eta, "pressure": float(p.mean()),
+                    "pressure_se": float(p.std(ddof=1) / math.sqrt(reps)), "reference": p_ref,
+                    "carnahan_starling": p_cs, "sweeps_per_replica": samples * every})
+    npt = []
+    for k, (pressure, eta_ref, eta_bhmj) in enumerate(README_NPT):
+        # the lattice start at the published density, as the reference's input
+        # files set rho, with a small first volume step
+        s = HardSphereSystem(rho=6.0 * eta_bhmj / math.pi, cells=4, dr_max=0.2, dv_max=0.01, pressure=pressure,
+                             seed=800 + k)
+        dr, acc, _, _ = opt_npt(s, TARGET_ACC, None)
+        dv, vacc = s.dv_max, 0.0
+        for _ in range(12):  # dv_max toward 40 % volume acceptance, a factor of at most 2 per step
+            c = s.sweep_npt(400).astype(float)
+            vacc = c[4] / c[3] if c[3] else 0.0
+            dv = float(np.clip(dv * np.clip(vacc / TARGET_ACC, 0.5, 2.0), 1e-4, 0.1))
+            s.set_step(dr, dv)
+        s.sweep_npt(4000)
+        etas = []
+        for _ in range(1600):
+            s.sweep_npt(25)
+            box = s.get_box()
+            etas.append(math.pi / 6.0 * s.n / (box[0] * box[1] * box[2]))
+        etas = np.array(etas)
+        blocks = etas.reshape(10, -1).mean(axis=1)
+        npt.append({"pressure": pressure, "packing_fraction": float(etas.mean()),
+                    "packing_fraction_se": float(blocks.std(ddof=1) / math.sqrt(len(blocks))),
+                    "reference": eta_ref, "bhmj": eta_bhmj, "dr_max": dr, "dv_max": dv, "volume_acceptance": vacc,
+                    "sweeps": 40000})
+    mu = []
+    for k, (rho, mu_ref, acc_ref) in enumerate(README_MU):
+        s = HardSphereSystem(rho=rho, cells=4, dr_max=0.3, seed=900 + k)
+        tune_dr(s, 0.3)
+        s.sweep_nvt(1000)
+        ok = tot = 0
+        vals = []
+        for _ in range(500):
+            s.sweep_nvt(20)
+            a = s.widom_insertion(20000)
+            ok += a
+            tot += 20000
+            vals.append(a / 20000)
+        vals = np.array(vals).reshape(20, -1).mean(axis=1)
+        beta_mu = -math.log(ok / tot)
+        se = float(np.std(-np.log(np.maximum(vals, 1e-300)), ddof=1) / math.sqrt(len(vals)))
+        mu.append({"density": rho, "beta_mu_ex": beta_mu, "beta_mu_ex_se": se, "reference": mu_ref,
+                   "accepted_percent": 100.0 * ok / tot, "reference_accepted_percent": acc_ref,
+                   "insertions": tot})
+    line = {"metric": "the reference's published tables at N=256", "value": time.perf_counter() - t_all,
+            "unit": "s (wall, all three tables)", "n_gpus": 1, "higher_is_better": False, "dtype": "f64",
+            "data": "synthetic (FCC 4^3 starts)",
+            "config": {"workload": "NVT pressure (5 packing fractions x 32 replicas x 20000 sweeps), NpT packing "
+                                   "fraction (4 pressures x 40000 sweeps), Widom (4 densities x 10^7 insertions)"},
+            "nvt": nvt, "npt": npt, "mu": mu}
+    print(json.dumps(line), flush=True)
+    return 0
+
+
 def run_small(args):
     """The reference's own run sizes (its README tables use N = 256 to
     1000; the first benchmark configuration is N = 4000): NVT sweeps/s with
@@ -735,7 +833,7 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
-    ap.add_argument("--workload", default="fluid", choices=["fluid", "replicas", "widom", "npt", "cluster", "cavity", "small"])
+    ap.add_argument("--workload", default="fluid", choices=["fluid", "replicas", "widom", "npt", "cluster", "cavity", "small", "readme"])
     ap.add_argument("--replicas", type=int, default=512)
     ap.add_argument("--cell-edge", default="0",
                     help='replicas: smallest device-cell edge, a number or "auto" (min(rho^-1/3, 1.4))')
@@ -759,6 +857,8 @@ def main():
         return run_cavity(args)
     if args.workload == "small":
         return run_small(args)
+    if args.workload == "readme":
+        return run_readme(args)
     return run_gpu_arm(args)
 
 
