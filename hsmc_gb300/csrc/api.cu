@@ -323,9 +323,10 @@ int hsmc_gpu_create(const hsmc_params *prm, hsmc_ctx **out) {
     return fail(ce);
   ctx->flow = false;  // one launch per pass unless hsmc_gpu_set_schedule or the autotuner picks the dataflow sweep
   ctx->cavity = cavity;
-  // a system that fits one block's shared memory runs its NVT sweeps there
-  if (!cavity && prm->pressure <= 0) {
-    const size_t sm = sweep_small_smem(ctx->n, b.ncell, cap);
+  // a system that fits one block's shared memory (at the largest grid its
+  // box may reach) runs its sweeps there
+  if (!cavity) {
+    const size_t sm = sweep_small_smem(ctx->n, balloc.ncell, cap);
     if (sm > 0 && prepare_sweep_small(sm)) ctx->small_smem = sm;
     cudaGetLastError();
   }
@@ -501,11 +502,11 @@ static int run_sweeps(hsmc_ctx *ctx, int n_sweeps, bool trace, bool npt, uint64_
   HSMC_CUDA(cudaMemsetAsync(&ctx->sp.st->status, 0, sizeof(int), ctx->stream));
   ctx->last_move_ms = 0.0;
   ctx->last_move_launches = 0;
-  if (ctx->small && !trace && !ctx->profiling && !npt) {
+  if (ctx->small && !trace && !ctx->profiling) {
     // every sweep in one launch, then the device layouts rebuilt for the
     // last sweep (observables and the other schedules read them)
     HSMC_CUDA(cudaEventRecord(ctx->ev_start, ctx->stream));
-    if (n_sweeps > 0) launch_sweep_small(ctx->sp, n_sweeps, ctx->small_smem, ctx->hbox.ncell / 8, ctx->stream);
+    if (n_sweeps > 0) launch_sweep_small(ctx->sp, n_sweeps, npt, ctx->margin, ctx->small_smem, ctx->stream);
     HSMC_CUDA(cudaEventRecord(ctx->ev_stop, ctx->stream));
     ctx->sweep_base += (unsigned long long)n_sweeps;
     if (n_sweeps > 0) {
@@ -521,12 +522,15 @@ static int run_sweeps(hsmc_ctx *ctx, int n_sweeps, bool trace, bool npt, uint64_
     ctx->last_total_ms = ms;
     DevState s;
     if ((e = read_state(ctx, s))) return e;
+    if (npt) HSMC_CUDA(cudaMemcpy(&ctx->hbox, ctx->sp.box, sizeof(Box), cudaMemcpyDeviceToHost));
     if (counters) {
       const uint64_t moves = (uint64_t)ctx->n * (uint64_t)n_sweeps;
       counters[HSMC_CNT_MOVES] = moves;
       counters[HSMC_CNT_ACCEPTED] = s.acc;
       counters[HSMC_CNT_REJECTED] = moves - s.acc;
-      counters[HSMC_CNT_VOL_MOVES] = counters[HSMC_CNT_VOL_ACCEPTED] = counters[HSMC_CNT_VOL_REJECTED] = 0;
+      counters[HSMC_CNT_VOL_MOVES] = s.vol_moves;
+      counters[HSMC_CNT_VOL_ACCEPTED] = s.vol_acc;
+      counters[HSMC_CNT_VOL_REJECTED] = s.vol_moves - s.vol_acc;
     }
     if (s.status) return status_to_code(s.status);
     return HSMC_OK;
@@ -657,7 +661,7 @@ int hsmc_gpu_autotune(hsmc_ctx *ctx, int sweeps_per_variant, int *lanes_out) {
   double best_ms = 1e300;
   for (int f = 2; f >= 0; f--)
     for (int v = 0; v < 4; v++) {
-      if (f == 2 && (v > 0 || npt)) continue;  // one variant, NVT only
+      if (f == 2 && v > 0) continue;  // one variant
       if (!apply_schedule(ctx, f, f == 2 ? ctx->group : options[v])) continue;
       int e = run_sweeps(ctx, sweeps, false, npt, nullptr);
       if (e) {

@@ -42,6 +42,52 @@ __device__ __forceinline__ int find_rep(const int *start, int n, int x) {
 __device__ __forceinline__ int *cnt_of(const SysPtrs &p, int layout) { return layout ? p.cnt[1] : p.cnt[0]; }
 __device__ __forceinline__ Slot *slot_of(const SysPtrs &p, int layout) { return layout ? p.slot[1] : p.slot[0]; }
 
+// vol_move (src/moves.c:83-153) in the reference's operation order, without
+// contraction, shared by the volume-move kernels (sweep.cu) and the
+// one-block sweep (sweep_small.cu) so that both make the same chain.
+// The proposal: ln V' = ln V + (u - 1/2) dv_max, ratio V'/V, sf = ratio^(1/3).
+__device__ __forceinline__ void vol_proposal(double vol, uint32_t r, double dv_max, double &vol_new, double &ratio,
+                                             double &sf) {
+  vol_new = exp(__dadd_rn(log(vol), __dmul_rn(centred_offset(r), dv_max)));
+  ratio = __ddiv_rn(vol_new, vol);
+  sf = pow(ratio, 1. / 3.);
+}
+
+// The acceptance bound exp(beta P (V - V') + (N + 1) ln(V'/V)).
+__device__ __forceinline__ double vol_boltz(double pressure, double vol, double vol_new, int n, double ratio) {
+  return exp(__dadd_rn(__dmul_rn(pressure, __dsub_rn(vol, vol_new)), __dmul_rn((double)(n + 1), log(ratio))));
+}
+
+// The box after an accepted volume move, rebuilt from the lattice counts
+// and the new density as sim_box_init does (src/moves.c:128-132,
+// src/sim_info.c:32-71), with the device grid re-derived for it (an even
+// count per axis, edge >= 1 + margin, at most the allocated count).
+// Returns false when the grid would have fewer than 4 cells per axis.
+__device__ __forceinline__ bool vol_rebuild_box(const DevState *st, int n, double vol_new, double margin, Box &bx) {
+  const double rho = n / vol_new;
+  const double cell_vol = st->per_cell / rho;
+  const double cell_size = pow(cell_vol, 1. / 3.);
+  double lmax = 0.0;
+  for (int d = 0; d < 3; d++) {
+    const double len = st->cells[d] * cell_size;
+    int nc = 2 * (int)floor(len / (2.0 * (1.0 + margin)));
+    if (nc > st->nc_alloc[d]) nc = st->nc_alloc[d];
+    if (nc < 4) return false;
+    bx.len[d] = len;
+    bx.half[d] = len / 2.0;
+    bx.len32[d] = (float)len;
+    bx.inv_w32[d] = (float)(nc / len);
+    bx.w32[d] = (float)(len / nc);
+    bx.nc[d] = nc;
+    lmax = len > lmax ? len : lmax;
+  }
+  bx.ncell = bx.nc[0] * bx.nc[1] * bx.nc[2];
+  bx.vol = st->cells[0] * st->cells[1] * st->cells[2] * cell_vol;
+  bx.rho = rho;
+  bx.band = (float)(5.9604644775390625e-08 * (48.0 * lmax + 16.0) + 1e-6);
+  return true;
+}
+
 // api.cu: what other parts of the library see of a context
 struct CtxView {
   SysPtrs sp;
@@ -107,11 +153,12 @@ cudaError_t launch_cluster(const SysPtrs &p, const ClusterJob &job, int n_moves,
                            cudaStream_t s);
 
 // sweep_small.cu: every sweep of a call in one block with the system in
-// shared memory (0 bytes: the system does not fit); the same chain as the
-// pass-barrier schedule.  The launch leaves the device cell layouts stale.
+// shared memory (0 bytes: the system does not fit; ncell the allocated
+// grid); the same chain as the pass-barrier schedule, with one volume move
+// per sweep when npt.  The launch leaves the device cell layouts stale.
 size_t sweep_small_smem(int n, int ncell, int cap);
 bool prepare_sweep_small(size_t smem);
-void launch_sweep_small(const SysPtrs &p, int n_sweeps, size_t smem, int n_active, cudaStream_t s);
+void launch_sweep_small(const SysPtrs &p, int n_sweeps, bool npt, double margin, size_t smem, cudaStream_t s);
 
 // cavity.cu: the cavity trials of sweep sweep_base + offset (trace: 8 words
 // per trial or nullptr), and psi at n distances

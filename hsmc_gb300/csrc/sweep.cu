@@ -105,11 +105,9 @@ __global__ void k_vol_propose(SysPtrs p, long long offset) {
   const Box *bx = p.box;
   const unsigned long long s = st->sweep_base + (unsigned long long)offset;
   const U32x4 r = draw4(st->seed, 0u, 0u, s, TAG_VOLUME);
-  const double vol = bx->vol;
-  const double log_new = log(vol) + centred_offset(r.x) * st->dv_max;
-  const double vol_new = exp(log_new);
-  const double ratio = vol_new / vol;
-  st->vol_sf = pow(ratio, 1. / 3.);
+  double vol_new, ratio, sf;
+  vol_proposal(bx->vol, r.x, st->dv_max, vol_new, ratio, sf);
+  st->vol_sf = sf;
   st->vol_new = vol_new;
   st->vol_ratio = ratio;
   st->vol_u_acc = open_unit(r.y);
@@ -183,32 +181,14 @@ __global__ void k_vol_decide(SysPtrs p, double margin) {
   DevState *st = p.st;
   Box *bx = p.box;
   if (st->vol_overlap) return;
-  const double boltz = exp(st->pressure * (bx->vol - st->vol_new) + (p.n + 1) * log(st->vol_ratio));
+  const double boltz = vol_boltz(st->pressure, bx->vol, st->vol_new, p.n, st->vol_ratio);
   if (st->vol_u_acc >= boltz) return;
-  const double rho = p.n / st->vol_new;
-  const double cell_vol = st->per_cell / rho;
-  const double cell_size = pow(cell_vol, 1. / 3.);
-  double lmax = 0.0;
-  for (int d = 0; d < 3; d++) {
-    const double len = st->cells[d] * cell_size;
-    int nc = 2 * (int)floor(len / (2.0 * (1.0 + margin)));
-    if (nc > st->nc_alloc[d]) nc = st->nc_alloc[d];
-    if (nc < 4) {
-      atomicOr(&st->status, ST_BAD_CELL);
-      return;
-    }
-    bx->len[d] = len;
-    bx->half[d] = len / 2.0;
-    bx->len32[d] = (float)len;
-    bx->inv_w32[d] = (float)(nc / len);
-    bx->w32[d] = (float)(len / nc);
-    bx->nc[d] = nc;
-    lmax = len > lmax ? len : lmax;
+  Box nb = *bx;
+  if (!vol_rebuild_box(st, p.n, st->vol_new, margin, nb)) {
+    atomicOr(&st->status, ST_BAD_CELL);
+    return;
   }
-  bx->ncell = bx->nc[0] * bx->nc[1] * bx->nc[2];
-  bx->vol = st->cells[0] * st->cells[1] * st->cells[2] * cell_vol;
-  bx->rho = rho;
-  bx->band = (float)(5.9604644775390625e-08 * (48.0 * lmax + 16.0) + 1e-6);
+  *bx = nb;
   st->vol_accept = 1;
   st->vol_acc += 1;
 }

@@ -18,6 +18,13 @@
 // cell k of the 27, and the cell's thread applies an accepted move at the
 // start of the next round.  A cell's trials stay in order; its neighbours
 // are of other colours, so no other cell writes what it reads.
+//
+// NpT sweeps add vol_move after the passes (src/moves.c:83-153): one thread
+// proposes, the block scans every particle's neighbourhood at the scaled
+// distances, one thread decides and rebuilds the box, and the block rescales
+// the positions; the box lives in shared memory for the launch.  The
+// arithmetic is engine.cuh's, shared with the volume-move kernels, so the
+// chain is the one of the eight-launch sweep followed by those kernels.
 #include "engine.cuh"
 
 namespace hsmc {
@@ -98,43 +105,58 @@ __device__ void scan_cells(const SmallSweepSm &m, int ncell, int n) {
   __syncthreads();
 }
 
-__global__ void __launch_bounds__(1024) k_sweep_small(SysPtrs p, int n_sweeps) {
+// A coordinate scaled by sf and wrapped once into [0, L] (src/moves.c:133-140).
+__device__ __forceinline__ double scale_wrap(double x, double sf, double len) {
+  double v = __dmul_rn(x, sf);
+  if (gt_pos(v, len)) v = __dsub_rn(v, len);
+  else if (lt_zero(v)) v = __dadd_rn(v, len);
+  return v;
+}
+
+__global__ void __launch_bounds__(1024) k_sweep_small(SysPtrs p, int n_sweeps, int npt, double margin) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   __shared__ float sh_s[3];
   __shared__ int perm_s[8];
+  __shared__ Box sb;         // the box, which a volume move may change
+  __shared__ double v_new, v_ratio, v_sf, v_u;
+  __shared__ int v_ov, v_acc;
   DevState *st = p.st;
-  const Box *bx = p.box;
-  const int n = p.n, ncell = bx->ncell, cap = p.cap;
-  const int n_active = (bx->nc[0] >> 1) * (bx->nc[1] >> 1) * (bx->nc[2] >> 1);
-  const SmallSweepSm m = small_sweep_sm(smem_raw, n, ncell, n_active, cap);
+  const int n = p.n, cap = p.cap;
+  // array sizes for the largest grid the context allocated (an NpT box can grow)
+  const SmallSweepSm m = small_sweep_sm(smem_raw, n, p.ncell_alloc, p.ncell_alloc / 8, cap);
   __shared__ int max_cn[8];  // per colour: the most trials any of its cells makes
   const int tid = (int)threadIdx.x, nt = (int)blockDim.x;
-  const int nc[3] = {bx->nc[0], bx->nc[1], bx->nc[2]};
-  double len[3], half[3];
-  float L32[3], iw[3];
-  for (int d = 0; d < 3; d++) {
-    len[d] = bx->len[d];
-    half[d] = bx->half[d];
-    L32[d] = bx->len32[d];
-    iw[d] = bx->inv_w32[d];
-  }
-  const float lo = 1.0f - bx->band, hi = 1.0f + bx->band;
+  if (tid == 0) sb = *p.box;
   const double dr = st->dr_max;
   const unsigned long long seed = st->seed, s0 = st->sweep_base;
   const int frozen = st->frozen;
   for (int i = tid; i < n; i += nt) load_xyz(p.pos, i, m.x[i], m.y[i], m.z[i]);
   unsigned acc = 0, rej_o = 0, rej_b = 0;
+  unsigned long long vmoves = 0, vacc = 0;
   const int lane = tid & 31, wid = tid >> 5, nw = nt >> 5;
-  const int hx = nc[0] >> 1, hy = nc[1] >> 1;
+  __syncthreads();
 
   for (int sw = 0; sw < n_sweeps; sw++) {
     const unsigned long long s = s0 + (unsigned long long)sw;
+    // this sweep's box and grid
+    const int nc[3] = {sb.nc[0], sb.nc[1], sb.nc[2]};
+    const int ncell = sb.ncell, hx = nc[0] >> 1, hy = nc[1] >> 1;
+    const int n_active = hx * hy * (nc[2] >> 1);
+    double len[3], half[3];
+    float L32[3], iw[3];
+    for (int d = 0; d < 3; d++) {
+      len[d] = sb.len[d];
+      half[d] = sb.half[d];
+      L32[d] = sb.len32[d];
+      iw[d] = sb.inv_w32[d];
+    }
+    const float lo = 1.0f - sb.band, hi = 1.0f + sb.band;
     // the sweep's grid shift and colour order, as k_build draws them
     if (tid == 0) {
       const U32x4 rs = draw4(seed, 0u, 0u, s, TAG_SHIFT);
-      sh_s[0] = __fmul_rn(__uint2float_rn(rs.x >> 8) * 5.9604644775390625e-08f, bx->w32[0]);
-      sh_s[1] = __fmul_rn(__uint2float_rn(rs.y >> 8) * 5.9604644775390625e-08f, bx->w32[1]);
-      sh_s[2] = __fmul_rn(__uint2float_rn(rs.z >> 8) * 5.9604644775390625e-08f, bx->w32[2]);
+      sh_s[0] = __fmul_rn(__uint2float_rn(rs.x >> 8) * 5.9604644775390625e-08f, sb.w32[0]);
+      sh_s[1] = __fmul_rn(__uint2float_rn(rs.y >> 8) * 5.9604644775390625e-08f, sb.w32[1]);
+      sh_s[2] = __fmul_rn(__uint2float_rn(rs.z >> 8) * 5.9604644775390625e-08f, sb.w32[2]);
       int perm[8] = {0, 1, 2, 3, 4, 5, 6, 7};
       const U32x4 ra = draw4(seed, 0u, 0u, s, TAG_PERM), rb = draw4(seed, 1u, 0u, s, TAG_PERM);
       const uint32_t r[7] = {ra.x, ra.y, ra.z, ra.w, rb.x, rb.y, rb.z};
@@ -304,6 +326,85 @@ __global__ void __launch_bounds__(1024) k_sweep_small(SysPtrs p, int n_sweeps) {
       }
       __syncthreads();
     }
+    if (npt) {
+      // vol_move: propose (one thread)
+      if (tid == 0) {
+        const U32x4 r = draw4(seed, 0u, 0u, s, TAG_VOLUME);
+        double vn, ra, sf;
+        vol_proposal(sb.vol, r.x, st->dv_max, vn, ra, sf);
+        v_new = vn;
+        v_ratio = ra;
+        v_sf = sf;
+        v_u = open_unit(r.y);
+        v_ov = 0;
+        v_acc = 0;
+        vmoves++;
+      }
+      __syncthreads();
+      const double sf = v_sf;
+      if (sf < 1.0) {  // a larger box cannot bring a pair closer
+        // check_overlap(i, sf, sf, sf) for every i (src/moves.c:104-112)
+        const float reach = (float)(1.0 / sf) + 1e-3f;
+        int k[3];
+        for (int d = 0; d < 3; d++) {
+          k[d] = (int)ceilf(reach * iw[d] * 1.0001f);
+          if (2 * k[d] + 1 > nc[d]) k[d] = -1;
+        }
+        for (int i = tid; i < n; i += nt) {
+          if (*(volatile int *)&v_ov) break;
+          int ci[3];
+          float xs[3];
+          axis_cell(__double2float_rn(m.x[i]), sh[0], L32[0], iw[0], nc[0], ci[0], xs[0]);
+          axis_cell(__double2float_rn(m.y[i]), sh[1], L32[1], iw[1], nc[1], ci[1], xs[1]);
+          axis_cell(__double2float_rn(m.z[i]), sh[2], L32[2], iw[2], nc[2], ci[2], xs[2]);
+          bool ov = false;
+          for (int a = (k[2] < 0 ? 0 : -k[2]); !ov && a <= (k[2] < 0 ? nc[2] - 1 : k[2]); a++) {
+            const int cz = k[2] < 0 ? a : (ci[2] + a + nc[2]) % nc[2];
+            for (int b2 = (k[1] < 0 ? 0 : -k[1]); !ov && b2 <= (k[1] < 0 ? nc[1] - 1 : k[1]); b2++) {
+              const int cy = k[1] < 0 ? b2 : (ci[1] + b2 + nc[1]) % nc[1];
+              for (int e = (k[0] < 0 ? 0 : -k[0]); !ov && e <= (k[0] < 0 ? nc[0] - 1 : k[0]); e++) {
+                const int cx = k[0] < 0 ? e : (ci[0] + e + nc[0]) % nc[0];
+                const int cc = cx + nc[0] * (cy + nc[1] * cz);
+                const int qe = m.start[cc + 1];
+                for (int q = m.start[cc]; q < qe && !ov; q++) {
+                  const int j = m.ids[q];
+                  if (j == i) continue;
+                  float dx = xs[0] - m.tx[j], dy = xs[1] - m.ty[j], dz = xs[2] - m.tz[j];
+                  dx -= L32[0] * rintf(dx / L32[0]);
+                  dy -= L32[1] * rintf(dy / L32[1]);
+                  dz -= L32[2] * rintf(dz / L32[2]);
+                  if (dx * dx + dy * dy + dz * dz > reach * reach) continue;
+                  if (ref_r2_scaled(m.x[i], m.y[i], m.z[i], m.x[j], m.y[j], m.z[j], len, sf) < 1.0) ov = true;
+                }
+              }
+            }
+          }
+          if (ov) atomicOr(&v_ov, 1);
+        }
+      }
+      __syncthreads();
+      // decide, and rebuild the box (one thread)
+      if (tid == 0 && !v_ov && v_u < vol_boltz(st->pressure, sb.vol, v_new, n, v_ratio)) {
+        Box nbx = sb;
+        if (vol_rebuild_box(st, n, v_new, margin, nbx)) {
+          sb = nbx;
+          v_acc = 1;
+          vacc++;
+        } else {
+          atomicOr(&st->status, ST_BAD_CELL);
+        }
+      }
+      __syncthreads();
+      if (v_acc) {  // positions scaled and wrapped into the new box (src/moves.c:133-140)
+        const double l0 = sb.len[0], l1 = sb.len[1], l2 = sb.len[2];
+        for (int i = tid; i < n; i += nt) {
+          m.x[i] = scale_wrap(m.x[i], sf, l0);
+          m.y[i] = scale_wrap(m.y[i], sf, l1);
+          m.z[i] = scale_wrap(m.z[i], sf, l2);
+        }
+      }
+      __syncthreads();
+    }
     if (sw == n_sweeps - 1 && tid == 0) {  // the last sweep's layout, as k_build leaves it
       st->params.sweep = s;
       for (int d = 0; d < 3; d++) st->params.shift32[d] = sh[d];
@@ -322,7 +423,14 @@ __global__ void __launch_bounds__(1024) k_sweep_small(SysPtrs p, int n_sweeps) {
     if (o) atomicAdd(&st->rej_overlap, o);
     if (bd) atomicAdd(&st->rej_boundary, bd);
   }
-  if (tid == 0) st->sweep_base = s0 + (unsigned long long)n_sweeps;
+  if (tid == 0) {
+    st->sweep_base = s0 + (unsigned long long)n_sweeps;
+    if (npt) {
+      *p.box = sb;
+      st->vol_moves += vmoves;
+      st->vol_acc += vacc;
+    }
+  }
 }
 
 }  // namespace
@@ -342,9 +450,8 @@ bool prepare_sweep_small(size_t smem) {
                          cudaSuccess;
 }
 
-void launch_sweep_small(const SysPtrs &p, int n_sweeps, size_t smem, int n_active, cudaStream_t s) {
-  (void)n_active;
-  k_sweep_small<<<1, 1024, smem, s>>>(p, n_sweeps);
+void launch_sweep_small(const SysPtrs &p, int n_sweeps, bool npt, double margin, size_t smem, cudaStream_t s) {
+  k_sweep_small<<<1, 1024, smem, s>>>(p, n_sweeps, npt ? 1 : 0, margin);
 }
 
 }  // namespace hsmc

@@ -290,12 +290,13 @@ int hsmc_gpu_autotune(hsmc_ctx *ctx, int sweeps_per_variant, int *lanes_out);
  * with a kernel boundary between passes; 1 = dataflow, all eight passes in
  * one cooperative launch where a cell waits only for the 26 cells around it
  * to finish the previous pass; 2 = one block, every sweep of a call in one
- * launch with the system in shared memory (NVT systems of up to a few
- * thousand spheres; the default up to 128 active cells per pass, about
- * 1000 spheres, where it is faster, else 0).  All give the same
+ * launch with the system in shared memory (systems of up to a few thousand
+ * spheres, NVT or NpT with its volume move per sweep; the default up to 128
+ * active cells per pass, about 1000 spheres, where it is faster, else 0).
+ * All give the same
  * chain; hsmc_gpu_autotune picks the fastest.  lanes_per_cell 0 keeps the
- * current mapping (schedule 2 has none).  Traced and profiled sweeps, NpT
- * sweeps and cavity runs use schedule 0 or 1. */
+ * current mapping (schedule 2 has none).  Traced and profiled sweeps and
+ * cavity runs use schedule 0 or 1. */
 int hsmc_gpu_set_schedule(hsmc_ctx *ctx, int schedule, int lanes_per_cell);
 int hsmc_gpu_get_schedule(hsmc_ctx *ctx, int *schedule, int *lanes_per_cell);
 

@@ -248,8 +248,31 @@ def test_one_block_schedule_is_the_default_for_small_systems(gpu_lib):
     assert mid.get_schedule()[0] == 0
     big = gpu_lib.HardSphereSystem(rho=0.85, cells=20, dr_max=0.12, seed=1)
     assert big.get_schedule()[0] == 0
-    npt = gpu_lib.HardSphereSystem(rho=0.85, cells=6, dr_max=0.12, dv_max=0.01, pressure=8.0, seed=1)
-    assert npt.get_schedule()[0] == 0
+    npt = gpu_lib.HardSphereSystem(rho=0.85, cells=4, dr_max=0.12, dv_max=0.01, pressure=8.0, seed=1)
+    assert npt.get_schedule()[0] == 2
+    cav = gpu_lib.HardSphereSystem(rho=0.85, cells=4, dr_max=0.12, seed=1, cavity=(0.1, 1.2, 0.0))
+    assert cav.get_schedule()[0] == 0  # the cavity stage runs between launches
+
+
+@pytest.mark.parametrize("rho,cells,P,dv,seed", [
+    (0.50, 4, 3.0, 0.01, 21),   # expands toward its pressure
+    (0.85, 4, 12.0, 0.004, 22), # dense
+    (0.60, 6, 5.0, 0.005, 23),  # N = 864
+])
+def test_one_block_npt_is_the_pass_barrier_chain(gpu_lib, rho, cells, P, dv, seed):
+    """NpT sweeps in one block (the volume move inside the launch) give the
+    chain of the eight launches plus the volume-move kernels bit for bit:
+    positions, box and counters."""
+    runs = []
+    for schedule in (0, 2):
+        s = gpu_lib.HardSphereSystem(rho=rho, cells=cells, dr_max=0.15, dv_max=dv, pressure=P, seed=seed)
+        s.set_schedule(schedule)
+        c1 = s.sweep_npt(40)
+        c2 = s.sweep_npt(9)
+        runs.append((s.download(), np.array(s.get_box()), c1, c2))
+    for a, b in zip(runs[0], runs[1]):
+        assert np.array_equal(a, b)
+    assert runs[0][2][4] > 0  # some volume moves were accepted
 
 
 def test_dataflow_schedule_npt_matches(gpu_lib):
