@@ -325,7 +325,7 @@ int hsmc_gpu_create(const hsmc_params *prm, hsmc_ctx **out) {
   ctx->cavity = cavity;
   // a system that fits one block's shared memory (at the largest grid its
   // box may reach) runs its sweeps there
-  if (!cavity) {
+  {
     const size_t sm = sweep_small_smem(ctx->n, balloc.ncell, cap);
     if (sm > 0 && prepare_sweep_small(sm)) ctx->small_smem = sm;
     cudaGetLastError();
@@ -502,11 +502,12 @@ static int run_sweeps(hsmc_ctx *ctx, int n_sweeps, bool trace, bool npt, uint64_
   HSMC_CUDA(cudaMemsetAsync(&ctx->sp.st->status, 0, sizeof(int), ctx->stream));
   ctx->last_move_ms = 0.0;
   ctx->last_move_launches = 0;
-  if (ctx->small && !trace && !ctx->profiling) {
+  if (ctx->small && !trace && !ctx->profiling && ctx->cav_trace_cap == 0) {
     // every sweep in one launch, then the device layouts rebuilt for the
     // last sweep (observables and the other schedules read them)
     HSMC_CUDA(cudaEventRecord(ctx->ev_start, ctx->stream));
-    if (n_sweeps > 0) launch_sweep_small(ctx->sp, n_sweeps, npt, ctx->margin, ctx->small_smem, ctx->stream);
+    if (n_sweeps > 0)
+      launch_sweep_small(ctx->sp, n_sweeps, npt, ctx->cavity, ctx->margin, ctx->small_smem, ctx->stream);
     HSMC_CUDA(cudaEventRecord(ctx->ev_stop, ctx->stream));
     ctx->sweep_base += (unsigned long long)n_sweeps;
     if (n_sweeps > 0) {
@@ -524,10 +525,10 @@ static int run_sweeps(hsmc_ctx *ctx, int n_sweeps, bool trace, bool npt, uint64_
     if ((e = read_state(ctx, s))) return e;
     if (npt) HSMC_CUDA(cudaMemcpy(&ctx->hbox, ctx->sp.box, sizeof(Box), cudaMemcpyDeviceToHost));
     if (counters) {
-      const uint64_t moves = (uint64_t)ctx->n * (uint64_t)n_sweeps;
+      const uint64_t moves = (uint64_t)ctx->n * (uint64_t)n_sweeps + s.cav_moves;
       counters[HSMC_CNT_MOVES] = moves;
-      counters[HSMC_CNT_ACCEPTED] = s.acc;
-      counters[HSMC_CNT_REJECTED] = moves - s.acc;
+      counters[HSMC_CNT_ACCEPTED] = s.acc + s.cav_acc;
+      counters[HSMC_CNT_REJECTED] = moves - s.acc - s.cav_acc;
       counters[HSMC_CNT_VOL_MOVES] = s.vol_moves;
       counters[HSMC_CNT_VOL_ACCEPTED] = s.vol_acc;
       counters[HSMC_CNT_VOL_REJECTED] = s.vol_moves - s.vol_acc;

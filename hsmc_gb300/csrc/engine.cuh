@@ -158,7 +158,8 @@ cudaError_t launch_cluster(const SysPtrs &p, const ClusterJob &job, int n_moves,
 // per sweep when npt.  The launch leaves the device cell layouts stale.
 size_t sweep_small_smem(int n, int ncell, int cap);
 bool prepare_sweep_small(size_t smem);
-void launch_sweep_small(const SysPtrs &p, int n_sweeps, bool npt, double margin, size_t smem, cudaStream_t s);
+void launch_sweep_small(const SysPtrs &p, int n_sweeps, bool npt, bool cavity, double margin, size_t smem,
+                        cudaStream_t s);
 
 // cavity.cu: the cavity trials of sweep sweep_base + offset (trace: 8 words
 // per trial or nullptr), and psi at n distances

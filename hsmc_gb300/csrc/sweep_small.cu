@@ -25,7 +25,9 @@
 // the positions; the box lives in shared memory for the launch.  The
 // arithmetic is engine.cuh's, shared with the volume-move kernels, so the
 // chain is the one of the eight-launch sweep followed by those kernels.
-#include "engine.cuh"
+// Cavity runs add their cavity stage after the passes, warp 0 making the
+// trials with cavity.cuh's loop against the shared-memory cell list.
+#include "cavity.cuh"
 
 namespace hsmc {
 
@@ -113,6 +115,7 @@ __device__ __forceinline__ double scale_wrap(double x, double sf, double len) {
   return v;
 }
 
+template <bool CAV>
 __global__ void __launch_bounds__(1024) k_sweep_small(SysPtrs p, int n_sweeps, int npt, double margin) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   __shared__ float sh_s[3];
@@ -130,9 +133,10 @@ __global__ void __launch_bounds__(1024) k_sweep_small(SysPtrs p, int n_sweeps, i
   const double dr = st->dr_max;
   const unsigned long long seed = st->seed, s0 = st->sweep_base;
   const int frozen = st->frozen;
+  const bool cavity = CAV && frozen == 2 && st->cav_trials > 0;
   for (int i = tid; i < n; i += nt) load_xyz(p.pos, i, m.x[i], m.y[i], m.z[i]);
   unsigned acc = 0, rej_o = 0, rej_b = 0;
-  unsigned long long vmoves = 0, vacc = 0;
+  unsigned long long vmoves = 0, vacc = 0, cdone = 0, cacc = 0;
   const int lane = tid & 31, wid = tid >> 5, nw = nt >> 5;
   __syncthreads();
 
@@ -326,6 +330,48 @@ __global__ void __launch_bounds__(1024) k_sweep_small(SysPtrs p, int n_sweeps, i
       }
       __syncthreads();
     }
+    if (CAV && cavity) {  // the sweep's cavity trials (cavity.cu's stage)
+      if (wid == 0) {
+        double cav[2][3] = {{m.x[0], m.y[0], m.z[0]}, {m.x[1], m.y[1], m.z[1]}};
+        const int ox = lane % 3 - 1, oy = (lane / 3) % 3 - 1, oz = lane / 9 - 1;
+        auto overlaps = [&](const double *nw) -> bool {
+          bool ov = false;
+          if (lane < 27) {
+            int ci[3];
+            float t[3];
+            axis_cell(__double2float_rn(nw[0]), sh[0], L32[0], iw[0], nc[0], ci[0], t[0]);
+            axis_cell(__double2float_rn(nw[1]), sh[1], L32[1], iw[1], nc[1], ci[1], t[1]);
+            axis_cell(__double2float_rn(nw[2]), sh[2], L32[2], iw[2], nc[2], ci[2], t[2]);
+            int jx = ci[0] + ox, jy = ci[1] + oy, jz = ci[2] + oz;
+            float imx = 0.f, imy = 0.f, imz = 0.f;
+            if (jx < 0) { jx += nc[0]; imx = -L32[0]; } else if (jx >= nc[0]) { jx -= nc[0]; imx = L32[0]; }
+            if (jy < 0) { jy += nc[1]; imy = -L32[1]; } else if (jy >= nc[1]) { jy -= nc[1]; imy = L32[1]; }
+            if (jz < 0) { jz += nc[2]; imz = -L32[2]; } else if (jz >= nc[2]) { jz -= nc[2]; imz = L32[2]; }
+            const int nb = jx + nc[0] * (jy + nc[1] * jz);
+            const int qe = m.start[nb + 1];
+            for (int q = m.start[nb]; q < qe && !ov; q++) {
+              const int j = m.ids[q];
+              if (j < 2) continue;  // the cavities do not overlap each other
+              const float dx = t[0] - __fadd_rn(m.tx[j], imx), dy = t[1] - __fadd_rn(m.ty[j], imy),
+                          dz = t[2] - __fadd_rn(m.tz[j], imz);
+              const float r2 = dx * dx + dy * dy + dz * dz;
+              if (r2 < lo) ov = true;
+              else if (r2 <= hi) ov = ref_r2(nw[0], nw[1], nw[2], m.x[j], m.y[j], m.z[j], len, half) < 1.0;
+            }
+          }
+          return __any_sync(0xffffffffu, ov);
+        };
+        auto accept = [&](int w, const double *nw) {
+          if (lane == 0) {
+            m.x[w] = nw[0];
+            m.y[w] = nw[1];
+            m.z[w] = nw[2];
+          }
+        };
+        cavity_trials(st, s, cav, len, half, overlaps, accept, nullptr, 0, nullptr, &st->status, cdone, cacc);
+      }
+      __syncthreads();
+    }
     if (npt) {
       // vol_move: propose (one thread)
       if (tid == 0) {
@@ -425,6 +471,10 @@ __global__ void __launch_bounds__(1024) k_sweep_small(SysPtrs p, int n_sweeps, i
   }
   if (tid == 0) {
     st->sweep_base = s0 + (unsigned long long)n_sweeps;
+    if (cavity) {
+      st->cav_moves += cdone;
+      st->cav_acc += cacc;
+    }
     if (npt) {
       *p.box = sb;
       st->vol_moves += vmoves;
@@ -446,12 +496,17 @@ size_t sweep_small_smem(int n, int ncell, int cap) {
 }
 
 bool prepare_sweep_small(size_t smem) {
-  return smem > 0 && cudaFuncSetAttribute(k_sweep_small, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) ==
-                         cudaSuccess;
+  return smem > 0 &&
+         cudaFuncSetAttribute(k_sweep_small<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) ==
+             cudaSuccess &&
+         cudaFuncSetAttribute(k_sweep_small<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) ==
+             cudaSuccess;
 }
 
-void launch_sweep_small(const SysPtrs &p, int n_sweeps, bool npt, double margin, size_t smem, cudaStream_t s) {
-  k_sweep_small<<<1, 1024, smem, s>>>(p, n_sweeps, npt ? 1 : 0, margin);
+void launch_sweep_small(const SysPtrs &p, int n_sweeps, bool npt, bool cavity, double margin, size_t smem,
+                        cudaStream_t s) {
+  if (cavity) k_sweep_small<true><<<1, 1024, smem, s>>>(p, n_sweeps, npt ? 1 : 0, margin);
+  else k_sweep_small<false><<<1, 1024, smem, s>>>(p, n_sweeps, npt ? 1 : 0, margin);
 }
 
 }  // namespace hsmc

@@ -295,8 +295,9 @@ int hsmc_gpu_autotune(hsmc_ctx *ctx, int sweeps_per_variant, int *lanes_out);
  * active cells per pass, about 1000 spheres, where it is faster, else 0).
  * All give the same
  * chain; hsmc_gpu_autotune picks the fastest.  lanes_per_cell 0 keeps the
- * current mapping (schedule 2 has none).  Traced and profiled sweeps and
- * cavity runs use schedule 0 or 1. */
+ * current mapping (schedule 2 has none; it also runs a cavity run's cavity
+ * stage).  Traced and profiled sweeps, and cavity runs recording their
+ * trials, use schedule 0 or 1. */
 int hsmc_gpu_set_schedule(hsmc_ctx *ctx, int schedule, int lanes_per_cell);
 int hsmc_gpu_get_schedule(hsmc_ctx *ctx, int *schedule, int *lanes_per_cell);
 

@@ -251,7 +251,28 @@ def test_one_block_schedule_is_the_default_for_small_systems(gpu_lib):
     npt = gpu_lib.HardSphereSystem(rho=0.85, cells=4, dr_max=0.12, dv_max=0.01, pressure=8.0, seed=1)
     assert npt.get_schedule()[0] == 2
     cav = gpu_lib.HardSphereSystem(rho=0.85, cells=4, dr_max=0.12, seed=1, cavity=(0.1, 1.2, 0.0))
-    assert cav.get_schedule()[0] == 0  # the cavity stage runs between launches
+    assert cav.get_schedule()[0] == 2
+
+
+@pytest.mark.parametrize("rho,cells,lt,pcav,maxdr,mindr,seed", [
+    (0.80, 10, 1, 0.10, 1.2, 0.0, 31),  # the reference's published cavity case, N = 1000
+    (0.50, 4, 2, 0.30, 1.1, 0.6, 32),
+    (0.40, 5, 2, 0.05, 0.7, 0.3, 33),
+])
+def test_one_block_cavity_is_the_pass_barrier_chain(gpu_lib, rho, cells, lt, pcav, maxdr, mindr, seed):
+    """Cavity sweeps in one block (the cavity stage inside the launch) give
+    the chain of the eight launches plus the cavity kernel bit for bit."""
+    runs = []
+    for schedule in (0, 2):
+        s = gpu_lib.HardSphereSystem(rho=rho, cells=cells, lattice_type=lt, dr_max=0.15, seed=seed,
+                                     cavity=(pcav, maxdr, mindr))
+        s.set_schedule(schedule)
+        c1 = s.sweep_nvt(25)
+        c2 = s.sweep_nvt(7)
+        runs.append((s.download(), c1, c2))
+    for a, b in zip(runs[0], runs[1]):
+        assert np.array_equal(a, b)
+    assert runs[0][1][0] > 25 * runs[0][0].shape[0]  # the counters include the cavity trials
 
 
 @pytest.mark.parametrize("rho,cells,P,dv,seed", [
