@@ -42,6 +42,10 @@ B_MOVE = 24.0 * (2.0 + 27.0 * RHO)  # algorithmic bytes per trial move
 # workload, from ncu captures of this bench command (cache-flushed replay, so
 # cold-cache upper bounds; in the timed graph the working set stays in L2).
 MOVE_DRAM_BYTES = {"k_move_pass": 31.65e6 + 256.0, "k_move_flow": None}
+# L2 sectors the SMs requested per launch (lts__t_sectors_srcunit_tex.sum x 32 B,
+# same captures): the working set is L2-resident, so this is the traffic the
+# timed launches actually move.
+MOVE_L2_BYTES = {"k_move_pass": 1476595 * 32.0, "k_move_flow": None}
 METRIC = "trial moves/s @N=256k rho=0.85"
 
 
@@ -300,6 +304,9 @@ def run_gpu_arm(args):
     per_sweep = 2 if schedule == 1 else 9  # build + move launches
     launches_per_step = SWEEPS_PER_STEP * per_sweep + math.ceil(SWEEPS_PER_STEP / 8)
     traffic = MOVE_DRAM_BYTES.get(kernel)
+    l2_bytes = MOVE_L2_BYTES.get(kernel)
+    l2 = None if l2_bytes is None else {"bytes_per_launch": l2_bytes, "gbs": l2_bytes / (kern_avg_ms * 1e-3) / 1e9,
+                                        "kind": "ncu lts__t_sectors_srcunit_tex.sum x 32 B per launch"}
     line = {
         "metric": METRIC, "value": value, "unit": "trial moves/s", "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": total_ms / args.steps, "higher_is_better": True,
@@ -315,7 +322,7 @@ def run_gpu_arm(args):
                      "frac": achieved / peak, "traffic": traffic,
                      "traffic_kind": "ncu dram__bytes_read.sum + dram__bytes_write.sum per launch, cold cache",
                      "kernel": kernel, "bytes_per_move": B_MOVE, "moves_per_launch": moves_per_launch,
-                     "avg_launch_ms": kern_avg_ms, "peak_kind": peak_kind},
+                     "avg_launch_ms": kern_avg_ms, "peak_kind": peak_kind, "l2": l2},
         "e2e": {"value": e2e_val, "unit": "trial moves/s", "h2d_bytes_per_step": N * 32,
                 "d2h_bytes_per_step": N * 32 + 6 * 8 + 4 * 8},
         "clocks": clk,
