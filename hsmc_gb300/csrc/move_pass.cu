@@ -487,6 +487,12 @@ __global__ void __launch_bounds__(128, PassSmem<G, CAP>::min_blocks)
     k_move_pass(SysPtrs p1, const SysPtrs *reps, const int *gstart, const int *rep_ids, int n_reps, int pass,
                 int *pool0, int *pool1, long long pool_cells) {
   static_assert(G == 1 || G == 2 || G == 4 || G == 8, "group size");
+  // Launched as a programmatic dependent of the previous pass (launch_gc),
+  // the blocks become resident while that pass drains and wait here until it
+  // has completed and its writes are visible; nothing is read before.  The
+  // next pass may then be scheduled (once every block of this one runs).
+  asm volatile("griddepcontrol.wait;\n" ::: "memory");
+  asm volatile("griddepcontrol.launch_dependents;\n" ::: "memory");
   extern __shared__ __align__(16) unsigned char smem_raw[];
   const PassSm m = pass_smem_ptrs<G, CAP>(smem_raw);
   const int tid = (int)threadIdx.x;
@@ -754,13 +760,30 @@ int move_pass_grid(int group, int cap, int ncell_alloc, int num_sms) {
   }
 }
 
+// A pass is a programmatic dependent launch: it may be scheduled before the
+// kernel ahead of it in the stream has finished, and waits for it inside
+// (griddepcontrol.wait), which hides the launch latency between passes.
 template <int G, int CAP>
 static void launch_gc(const SysPtrs &p, int pass, bool trace, int grid, cudaStream_t s) {
-  const size_t sm = pass_smem<G, CAP>();
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = dim3((unsigned)grid);
+  cfg.blockDim = dim3(128);
+  cfg.dynamicSmemBytes = pass_smem<G, CAP>();
+  cfg.stream = s;
+  cudaLaunchAttribute attr[1];
+  attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+  attr[0].val.programmaticStreamSerializationAllowed = 1;
+  cfg.attrs = attr;
+  cfg.numAttrs = 1;
+  const SysPtrs *no_reps = nullptr;
+  const int *no_ints = nullptr;
+  int *no_pool = nullptr;
   if (trace)
-    k_move_pass<G, CAP, true, false><<<grid, 128, sm, s>>>(p, nullptr, nullptr, nullptr, 0, pass, nullptr, nullptr, 0);
+    cudaLaunchKernelEx(&cfg, k_move_pass<G, CAP, true, false>, p, no_reps, no_ints, no_ints, 0, pass, no_pool, no_pool,
+                       0ll);
   else
-    k_move_pass<G, CAP, false, false><<<grid, 128, sm, s>>>(p, nullptr, nullptr, nullptr, 0, pass, nullptr, nullptr, 0);
+    cudaLaunchKernelEx(&cfg, k_move_pass<G, CAP, false, false>, p, no_reps, no_ints, no_ints, 0, pass, no_pool,
+                       no_pool, 0ll);
 }
 
 template <int G, int CAP>
