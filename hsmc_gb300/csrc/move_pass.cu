@@ -38,16 +38,25 @@ __constant__ unsigned char c_nbr[26] = {
 //   own_t   CAP x GPB float4: the cell's slots (grid coordinates, id)
 //   own_x/y/z  CAP x GPB double: their FP64 coordinates
 //   order   CAP x GPB byte: slot index of the particle of each id rank
+// The pool holds 4 CAP neighbour entries per group, plus one row (G more)
+// where that costs no resident block.  A cell whose neighbours hold more
+// than PC particles is screened straight from global memory, which is many
+// times slower and makes its warp the last of the pass: at 0.89 particles
+// per cell (rho = 0.85) 26 neighbour cells hold 23 on average, and more than
+// 32 about once per 30,000 occupied cells, more than 34 far more rarely.
 template <int G, int CAP>
 struct PassSmem {
-  static constexpr int GPB = 128 / G;  // groups per block
-  static constexpr int PC = 4 * CAP;   // pooled neighbour entries per group
-  static constexpr int PR = PC / G;    // pool rows
-  static constexpr size_t bytes =
-      (size_t)PR * 128 * 16 + (size_t)CAP * GPB * 16 + (size_t)3 * CAP * GPB * 8 + (size_t)CAP * GPB;
+  static constexpr int GPB = 128 / G;         // groups per block
   static constexpr size_t sm_bytes = 233472;  // shared memory of one SM
-  static constexpr int by_smem = (int)(sm_bytes / (bytes + 1024));
-  static constexpr int min_blocks = by_smem < 1 ? 1 : (by_smem > 8 ? 8 : by_smem);
+  static constexpr size_t fixed = (size_t)CAP * GPB * 16 + (size_t)3 * CAP * GPB * 8 + (size_t)CAP * GPB;
+  static constexpr int fit(int rows) {
+    const int b = (int)(sm_bytes / ((size_t)rows * 128 * 16 + fixed + 1024));
+    return b < 1 ? 1 : (b > 8 ? 8 : b);
+  }
+  static constexpr int PR = fit(4 * CAP / G + 1) == fit(4 * CAP / G) ? 4 * CAP / G + 1 : 4 * CAP / G;  // pool rows
+  static constexpr int PC = PR * G;  // pooled neighbour entries per group
+  static constexpr size_t bytes = (size_t)PR * 128 * 16 + fixed;
+  static constexpr int min_blocks = fit(PR);
 };
 
 // The slot copies bypass L1 (.cg): allocating them there measured 10 % slower
@@ -716,10 +725,18 @@ void prepare_move_pass() {
   allow_caps<8>();
 }
 
+template <int G>
+static size_t smem_for_g(int cap) {
+  return cap <= 8 ? PassSmem<G, 8>::bytes : (cap <= 16 ? PassSmem<G, 16>::bytes : PassSmem<G, 32>::bytes);
+}
+
 static size_t smem_for(int group, int cap) {
-  const int c = cap <= 8 ? 8 : (cap <= 16 ? 16 : 32);
-  // bytes grow as cap / group (PassSmem): evaluate the cap = 8 layout and scale
-  return PassSmem<1, 8>::bytes * (size_t)(c / 8) / (size_t)group;
+  switch (group) {
+    case 1: return smem_for_g<1>(cap);
+    case 2: return smem_for_g<2>(cap);
+    case 4: return smem_for_g<4>(cap);
+    default: return smem_for_g<8>(cap);
+  }
 }
 
 bool move_pass_fits(int group, int cap) {

@@ -62,10 +62,14 @@ def test_overlap_decisions_bit_exact(oracle_mod, gpu_lib, rho, n, seed, dr):
 
 @pytest.mark.parametrize("lanes", [1, 2, 4, 8])
 @pytest.mark.parametrize("rho,n,seed,dr,edge", [c + (0.0,) for c in CASES] +
-                         [(0.70, 10, 5, 0.2, 0.0), (0.40, 8, 9, 0.3, 1.2), (0.60, 8, 11, 0.25, 1.6)])
+                         [(0.70, 10, 5, 0.2, 0.0), (0.40, 8, 9, 0.3, 1.2), (0.60, 8, 11, 0.25, 1.6),
+                          (1.25, 6, 13, 0.05, 0.0)])
 def test_traced_sweeps_replay_bit_exact(oracle_mod, gpu_lib, rho, n, seed, dr, edge, lanes):
     """Every trial of a few sweeps replayed on the oracle; edge > 0 asks for
-    larger device cells (edges 1.23 and 1.88 here: capacity 16 and 32)."""
+    larger device cells (edges 1.23 and 1.88 here: capacity 16 and 32).  The
+    fcc crystal at rho = 1.25 (8 cells of edge 1.105 per axis, 1.7 spheres
+    per cell) overfills the shared-memory neighbour pool of most cells, so
+    their trials screen straight from global memory."""
     from oracle.philox import TAG_MOVE, draw4
 
     if edge > 1.41 and lanes == 1:
@@ -78,6 +82,17 @@ def test_traced_sweeps_replay_bit_exact(oracle_mod, gpu_lib, rho, n, seed, dr, e
     if edge:
         nc, _, _, _ = g.grid_info()
         assert all(g.box[d] / nc[d] >= edge for d in range(3))
+    if rho > 1.2:
+        # particles in the 26 neighbour cells of each cell (unshifted grid):
+        # beyond the 34 pool entries of two lanes per cell for most cells
+        nc, _, _, _ = g.grid_info()
+        w = np.array([g.box[d] / nc[d] for d in range(3)])
+        idx = np.floor(conf[:, 1:] / w).astype(int) % np.array(nc)
+        occ = np.zeros(tuple(nc))
+        np.add.at(occ, tuple(idx.T), 1)
+        around = sum(np.roll(occ, (dx, dy, dz), axis=(0, 1, 2))
+                     for dx in (-1, 0, 1) for dy in (-1, 0, 1) for dz in (-1, 0, 1)) - occ
+        assert np.mean(around > 34) > 0.5
     sweeps = 4
     rec, cnt = g.sweeps_traced(sweeps)
     assert len(rec) == o.n * sweeps
