@@ -275,14 +275,51 @@ __device__ __forceinline__ void move_cell(const PassEnv &e, const PassSm &m, int
     if (trial + 1 < n) r_next = draw4(e.seed, (e.rep << 8) | (uint32_t)(trial + 1), (uint32_t)c, e.seq, TAG_MOVE);
     const int s = (int)__umulhi(r.x, (unsigned)n);          // rank of the moving particle
     const int js = m.order[s * GPB + gl] & (CAP - 1);        // a slot index below CAP
-    const double nx = propose_axis(m.own_x[js * GPB + gl], centred_offset(r.y), e.dr, e.len[0]);
-    const double ny = propose_axis(m.own_y[js * GPB + gl], centred_offset(r.z), e.dr, e.len[1]);
-    const double nz = propose_axis(m.own_z[js * GPB + gl], centred_offset(r.w), e.dr, e.len[2]);
+    double nx, ny, nz;
     int c0, c1, c2;
     float ux, uy, uz;
-    axis_cell(__double2float_rn(nx), e.sh[0], e.L32[0], e.iw[0], nc[0], c0, ux);
-    axis_cell(__double2float_rn(ny), e.sh[1], e.L32[1], e.iw[1], nc[1], c1, uy);
-    axis_cell(__double2float_rn(nz), e.sh[2], e.L32[2], e.iw[2], nc[2], c2, uz);
+    if (G >= 2) {
+      // The FP64 work of the proposal is shared by the group's lanes: lane 0
+      // moves x, lane 1 y, both z, and they swap x and y.  The narrow FP64 pipe
+      // costs a warp instruction whatever the lanes it serves, and every warp
+      // of an SM reaches this point at about the same time, so this cuts the
+      // queue there by a third.  The periodic wrap is one add of -L or +L
+      // (v - L and v + (-L) are the same IEEE operation), issued only when a
+      // lane's proposal left the box.
+      const int a = lane & 1;
+      const double la = a ? e.len[1] : e.len[0];
+      double va = __dadd_rn(a ? m.own_y[js * GPB + gl] : m.own_x[js * GPB + gl],
+                            __dmul_rn(centred_offset(a ? r.z : r.y), e.dr));
+      double vz = __dadd_rn(m.own_z[js * GPB + gl], __dmul_rn(centred_offset(r.w), e.dr));
+      const bool oa = gt_pos(va, la), oz = gt_pos(vz, e.len[2]);
+      const bool wa = oa || lt_zero(va), wz = oz || lt_zero(vz);
+      if (__any_sync(gmask, wa || wz)) {
+        if (wa) va = __dadd_rn(va, oa ? -la : la);
+        if (wz) vz = __dadd_rn(vz, oz ? -e.len[2] : e.len[2]);
+      }
+      int ca;
+      float ua;
+      axis_cell(__double2float_rn(va), a ? e.sh[1] : e.sh[0], a ? e.L32[1] : e.L32[0], a ? e.iw[1] : e.iw[0],
+                a ? nc[1] : nc[0], ca, ua);
+      axis_cell(__double2float_rn(vz), e.sh[2], e.L32[2], e.iw[2], nc[2], c2, uz);
+      const double vb = __shfl_xor_sync(gmask, va, 1);
+      const float ub = __shfl_xor_sync(gmask, ua, 1);
+      const int cb = __shfl_xor_sync(gmask, ca, 1);
+      nx = a ? vb : va;
+      ny = a ? va : vb;
+      nz = vz;
+      ux = a ? ub : ua;
+      uy = a ? ua : ub;
+      c0 = a ? cb : ca;
+      c1 = a ? ca : cb;
+    } else {
+      nx = propose_axis(m.own_x[js * GPB + gl], centred_offset(r.y), e.dr, e.len[0]);
+      ny = propose_axis(m.own_y[js * GPB + gl], centred_offset(r.z), e.dr, e.len[1]);
+      nz = propose_axis(m.own_z[js * GPB + gl], centred_offset(r.w), e.dr, e.len[2]);
+      axis_cell(__double2float_rn(nx), e.sh[0], e.L32[0], e.iw[0], nc[0], c0, ux);
+      axis_cell(__double2float_rn(ny), e.sh[1], e.L32[1], e.iw[1], nc[1], c1, uy);
+      axis_cell(__double2float_rn(nz), e.sh[2], e.L32[2], e.iw[2], nc[2], c2, uz);
+    }
     const unsigned rc_before = t.rechecks;
     const int moving_id = __float_as_int(m.own_t[js * GPB + gl].w);
     int decision;
