@@ -278,7 +278,33 @@ __device__ __forceinline__ void move_cell(const PassEnv &e, const PassSm &m, int
     double nx, ny, nz;
     int c0, c1, c2;
     float ux, uy, uz;
-    if (G >= 2) {
+    if (G >= 4) {
+      // Lanes 0, 1 and 2 of each quad move x, y and z (lane 3 repeats z) in
+      // one round of the FP64 pipe, then every lane reads the three.
+      const int ax = (lane & 3) > 2 ? 2 : (lane & 3);
+      const double la = ax == 0 ? e.len[0] : (ax == 1 ? e.len[1] : e.len[2]);
+      const double xa = ax == 0 ? m.own_x[js * GPB + gl] : (ax == 1 ? m.own_y[js * GPB + gl] : m.own_z[js * GPB + gl]);
+      double va = __dadd_rn(xa, __dmul_rn(centred_offset(ax == 0 ? r.y : (ax == 1 ? r.z : r.w)), e.dr));
+      const bool oa = gt_pos(va, la);
+      const bool wa = oa || lt_zero(va);
+      if (__any_sync(gmask, wa)) {
+        if (wa) va = __dadd_rn(va, oa ? -la : la);
+      }
+      int ca;
+      float ua;
+      axis_cell(__double2float_rn(va), ax == 0 ? e.sh[0] : (ax == 1 ? e.sh[1] : e.sh[2]),
+                ax == 0 ? e.L32[0] : (ax == 1 ? e.L32[1] : e.L32[2]), ax == 0 ? e.iw[0] : (ax == 1 ? e.iw[1] : e.iw[2]),
+                ax == 0 ? nc[0] : (ax == 1 ? nc[1] : nc[2]), ca, ua);
+      nx = __shfl_sync(gmask, va, 0, 4);
+      ny = __shfl_sync(gmask, va, 1, 4);
+      nz = __shfl_sync(gmask, va, 2, 4);
+      ux = __shfl_sync(gmask, ua, 0, 4);
+      uy = __shfl_sync(gmask, ua, 1, 4);
+      uz = __shfl_sync(gmask, ua, 2, 4);
+      c0 = __shfl_sync(gmask, ca, 0, 4);
+      c1 = __shfl_sync(gmask, ca, 1, 4);
+      c2 = __shfl_sync(gmask, ca, 2, 4);
+    } else if (G >= 2) {
       // The FP64 work of the proposal is shared by the group's lanes: lane 0
       // moves x, lane 1 y, both z, and they swap x and y.  The narrow FP64 pipe
       // costs a warp instruction whatever the lanes it serves, and every warp
