@@ -41,11 +41,11 @@ B_MOVE = 24.0 * (2.0 + 27.0 * RHO)  # algorithmic bytes per trial move
 # DRAM bytes (read + write) of one launch of the move kernels on this
 # workload, from ncu captures of this bench command (cache-flushed replay, so
 # cold-cache upper bounds; in the timed graph the working set stays in L2).
-MOVE_DRAM_BYTES = {"k_move_pass": 31.65e6 + 256.0, "k_move_flow": None}
+MOVE_DRAM_BYTES = {"k_move_pass": 31664896.0, "k_move_flow": None}
 # L2 sectors the SMs requested per launch (lts__t_sectors_srcunit_tex.sum x 32 B,
 # same captures): the working set is L2-resident, so this is the traffic the
 # timed launches actually move.
-MOVE_L2_BYTES = {"k_move_pass": 1476595 * 32.0, "k_move_flow": None}
+MOVE_L2_BYTES = {"k_move_pass": 1476367 * 32.0, "k_move_flow": None}
 METRIC = "trial moves/s @N=256k rho=0.85"
 
 
