@@ -267,7 +267,19 @@ __device__ __forceinline__ void move_cell(const PassEnv &e, const PassSm &m, int
   if (!FLOW) cp_async_wait_all();
   if (G > 1) __syncwarp(gmask);
 
-  const int rows = (!direct && total > lane) ? (total - lane + G - 1) / G : 0;
+  // This lane's column holds `rows` entries; it is padded with far-away
+  // entries (never within the band of contact, never rechecked) up to a
+  // multiple of four rows where the pool has room, so the screen runs four
+  // candidates at a time without a serial remainder.
+  int rows = (!direct && total > lane) ? (total - lane + G - 1) / G : 0;
+  {
+    constexpr int PR = PassSmem<G, CAP>::PR;
+    const int rows4 = (rows + 3) & ~3;
+    if (rows4 <= PR) {
+      for (int w = rows; w < rows4; w++) m.pool[w * 128 + tid] = make_float4(1e30f, 1e30f, 1e30f, __int_as_float(-1));
+      rows = rows4;
+    }
+  }
   const float lo = e.lo, hi = e.hi;
   unsigned moved = 0;
   for (int trial = 0; trial < n; trial++) {
