@@ -123,12 +123,14 @@ __device__ bool cavity_trials(const DevState *st, unsigned long long s, double (
   const int lane = (int)(threadIdx.x & 31);
   const int trials = st->cav_trials;
   const unsigned long long seed = st->seed;
-  const double dr = st->dr_max, cmin = st->cav_min, cmax = st->cav_max;
+  const double dr = st->dr_max, r2lo = st->cav_r2min, r2hi = st->cav_r2max;
   const Psi32 c32 = psi32_coeffs(st->psi);
-  // the current distance and its psi (single precision always, FP64 when a
-  // decision has needed it), recomputed only when a move is accepted
-  double d_old = sqrt(ref_r2(cav[0][0], cav[0][1], cav[0][2], cav[1][0], cav[1][1], cav[1][2], len, half));
-  float en32_old = cavity_psi32(c32, (float)d_old, lane);
+  // the current squared distance and its psi (single precision always, FP64
+  // when a decision has needed it), recomputed only when a move is accepted.
+  // The range tests on the distance are exact tests on r2 (cav_r2min,
+  // cav_r2max), so the FP64 square root is taken only for an FP64 psi.
+  double r2_old = ref_r2(cav[0][0], cav[0][1], cav[0][2], cav[1][0], cav[1][1], cav[1][2], len, half);
+  float en32_old = cavity_psi32(c32, sqrtf(__double2float_rn(r2_old)), lane);
   double en_old = 0.0;
   bool have_old = false;
   U32x4 q1{0u, 0u, 0u, 0u};
@@ -144,7 +146,7 @@ __device__ bool cavity_trials(const DevState *st, unsigned long long s, double (
     const uint32_t r2x = __shfl_sync(0xffffffffu, q2, src);
     const int w = (int)(r1.x >> 31);
     // compute_dist(0, 1) before the move must lie in the allowed range
-    if (d_old < cmin || d_old > cmax) {
+    if (r2_old < r2lo || r2_old > r2hi) {
       if (lane == 0) atomicOr(status, ST_CAVITY_RANGE);
       return false;
     }
@@ -154,15 +156,15 @@ __device__ bool cavity_trials(const DevState *st, unsigned long long s, double (
     nw[2] = propose_axis(cav[w][2], centred_offset(r1.w), dr, len[2]);
     const double *c0 = w == 0 ? nw : cav[0];
     const double *c1 = w == 1 ? nw : cav[1];
-    const double d_new = sqrt(ref_r2(c0[0], c0[1], c0[2], c1[0], c1[1], c1[2], len, half));
+    const double r2_new = ref_r2(c0[0], c0[1], c0[2], c1[0], c1[1], c1[2], len, half);
     int decision = 1;  // the new distance leaves the allowed range
     double en_new = 0.0;
     float en32_new = 0.0f;
     bool have_new = false;
-    if (d_new >= cmin && d_new <= cmax) {
+    if (r2_new >= r2lo && r2_new <= r2hi) {
       // the reference's test u > exp(-(psi' - psi))
       const double u = open_unit(r2x);
-      en32_new = cavity_psi32(c32, (float)d_new, lane);
+      en32_new = cavity_psi32(c32, sqrtf(__double2float_rn(r2_new)), lane);
       const double b32 = (double)expf(-(en32_new - en32_old));
       if (u > b32 * (1.0 + 1e-3)) {
         decision = 2;
@@ -170,10 +172,10 @@ __device__ bool cavity_trials(const DevState *st, unsigned long long s, double (
         decision = 0;
       } else {
         if (!have_old) {
-          en_old = cavity_psi_warp(st->psi, d_old, lane);
+          en_old = cavity_psi_warp(st->psi, sqrt(r2_old), lane);
           have_old = true;
         }
-        en_new = cavity_psi_warp(st->psi, d_new, lane);
+        en_new = cavity_psi_warp(st->psi, sqrt(r2_new), lane);
         have_new = true;
         decision = u > exp(-(en_new - en_old)) ? 2 : 0;
       }
@@ -181,7 +183,7 @@ __device__ bool cavity_trials(const DevState *st, unsigned long long s, double (
     if (decision == 0 && overlaps(nw)) decision = 3;
     if (decision == 0) {
       for (int d = 0; d < 3; d++) cav[w][d] = nw[d];
-      d_old = d_new;
+      r2_old = r2_new;
       en32_old = en32_new;
       en_old = en_new;
       have_old = have_new;

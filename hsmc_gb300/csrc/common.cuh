@@ -216,6 +216,9 @@ struct DevState {
   int frozen;
   int cav_trials;
   double cav_min, cav_max;
+  // sqrt(r2) >= cav_min exactly when r2 >= cav_r2min, and sqrt(r2) <= cav_max
+  // exactly when r2 <= cav_r2max (sqrt is correctly rounded, so monotone)
+  double cav_r2min, cav_r2max;
   hsmc_cavity_psi_coeffs psi;
 };
 
