@@ -107,28 +107,6 @@ int hsmc::ctx_view(hsmc_ctx *ctx, CtxView *out) {
   return HSMC_OK;
 }
 
-// The cavity stage compares the distance sqrt(r2) between the cavities with
-// [cav_min, cav_max] (src/moves.c:293-297, 349).  sqrt is correctly
-// rounded here and on the device, hence monotone, so each comparison is one
-// with a fixed r2: the smallest r2 whose root reaches c, the largest whose
-// root stays within c.  Found by stepping from c * c one double at a time.
-static double r2_at_least(double c) {
-  if (!(c > 0.0)) return 0.0;  // every r2 >= 0 has a root >= 0
-  double x = c * c;
-  while (std::sqrt(x) < c) x = std::nextafter(x, INFINITY);
-  while (x > 0.0 && std::sqrt(std::nextafter(x, 0.0)) >= c) x = std::nextafter(x, 0.0);
-  return x;
-}
-
-static double r2_at_most(double c) {
-  if (!(c < INFINITY)) return INFINITY;
-  if (c < 0.0) return -1.0;  // no r2 >= 0 qualifies
-  double x = c * c;
-  while (std::sqrt(x) > c) x = std::nextafter(x, 0.0);
-  while (std::isfinite(x) && std::sqrt(std::nextafter(x, INFINITY)) <= c) x = std::nextafter(x, INFINITY);
-  return x;
-}
-
 static int cuda_status(cudaError_t e) {
   if (e == cudaSuccess) return HSMC_OK;
   fprintf(stderr, "hsmc_gpu: CUDA error %s\n", cudaGetErrorString(e));
@@ -331,8 +309,8 @@ int hsmc_gpu_create(const hsmc_params *prm, hsmc_ctx **out) {
     s0.cav_trials = (int)(k < 1 ? 1 : k);
     s0.cav_min = prm->cavity_mindr;
     s0.cav_max = prm->cavity_maxdr;
-    s0.cav_r2min = r2_at_least(prm->cavity_mindr);
-    s0.cav_r2max = r2_at_most(prm->cavity_maxdr);
+    s0.cav_r2min = hsmc_cavity_r2_at_least(prm->cavity_mindr);
+    s0.cav_r2max = hsmc_cavity_r2_at_most(prm->cavity_maxdr);
     hsmc_cavity_coeffs(prm->rho > 0 ? prm->rho : rho, &s0.psi);
   }
   for (int d = 0; d < 3; d++) {

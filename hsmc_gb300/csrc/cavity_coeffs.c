@@ -85,3 +85,22 @@ void hsmc_cavity_coeffs(double rho, hsmc_cavity_psi_coeffs *c) {
     c->a_im[k] = cimag(a[k]);
   }
 }
+
+/* The smallest r2 whose root reaches c, and the largest whose root stays
+ * within c: stepped to one double at a time from c * c. */
+double hsmc_cavity_r2_at_least(double c) {
+  if (!(c > 0.0)) return 0.0; /* every r2 >= 0 has a root >= 0 */
+  double x = c * c;
+  while (sqrt(x) < c) x = nextafter(x, INFINITY);
+  while (x > 0.0 && sqrt(nextafter(x, 0.0)) >= c) x = nextafter(x, 0.0);
+  return x;
+}
+
+double hsmc_cavity_r2_at_most(double c) {
+  if (!(c < INFINITY)) return INFINITY;
+  if (c < 0.0) return -1.0; /* no r2 >= 0 qualifies */
+  double x = c * c;
+  while (sqrt(x) > c) x = nextafter(x, 0.0);
+  while (isfinite(x) && sqrt(nextafter(x, INFINITY)) <= c) x = nextafter(x, INFINITY);
+  return x;
+}

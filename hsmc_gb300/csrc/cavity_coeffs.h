@@ -14,6 +14,12 @@ typedef struct {
 extern "C" {
 #endif
 void hsmc_cavity_coeffs(double rho, hsmc_cavity_psi_coeffs *c);
+/* The cavity distance sqrt(r2) is compared with [mindr, maxdr]
+ * (src/moves.c:293-297, 349).  sqrt is correctly rounded, hence monotone, so
+ * sqrt(r2) >= c exactly when r2 >= hsmc_cavity_r2_at_least(c), and
+ * sqrt(r2) <= c exactly when r2 <= hsmc_cavity_r2_at_most(c). */
+double hsmc_cavity_r2_at_least(double c);
+double hsmc_cavity_r2_at_most(double c);
 #ifdef __cplusplus
 }
 #endif

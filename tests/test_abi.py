@@ -42,3 +42,29 @@ def test_lattice_matches_reference(oracle_mod, gpu_lib, rho, n, lt):
     box, vol, _ = gpu_lib.box_from_lattice(rho, (n, n, n), lt)
     b = o.box()
     assert box == (b["lx"], b["ly"], b["lz"]) and vol == b["vol"]
+
+
+def test_cavity_range_thresholds_are_exact(gpu_lib):
+    """The cavity stage tests the distance range [mindr, maxdr] on r2 against
+    two host-computed thresholds; sqrt(r2) >= c must hold exactly when
+    r2 >= r2_at_least(c), and sqrt(r2) <= c exactly when r2 <= r2_at_most(c),
+    for every double near c * c (sqrt is correctly rounded in numpy, glibc
+    and CUDA alike)."""
+    lib = gpu_lib._native.load()
+    lo_f, hi_f = lib.hsmc_cavity_r2_at_least, lib.hsmc_cavity_r2_at_most
+    lo_f.restype = hi_f.restype = C.c_double
+    lo_f.argtypes = hi_f.argtypes = [C.c_double]
+    rng = np.random.default_rng(11)
+    cs = np.concatenate([[0.0, 0.3, 0.6, 0.7, 1.0, 1.1, 1.2, 1.5], rng.uniform(0.0, 3.0, 2000)])
+    steps = np.arange(-12, 13)
+    for c in cs:
+        lo, hi = lo_f(float(c)), hi_f(float(c))
+        x = np.float64(c) * np.float64(c)
+        near = np.array([x] * len(steps))
+        for i, k in enumerate(steps):
+            for _ in range(abs(int(k))):
+                near[i] = np.nextafter(near[i], np.inf if k > 0 else 0.0)
+        r = np.sqrt(near)
+        assert np.array_equal(r >= c, near >= lo), c
+        assert np.array_equal(r <= c, near <= hi), c
+    assert lo_f(0.0) == 0.0 and hi_f(float("inf")) == float("inf")
