@@ -14,9 +14,11 @@
 //   positions   the FP64 coordinates of the cell's particles, by cp.async,
 //               while the lanes rank the particles by id.
 // Then n trials (n = particles in the cell), each on the particle of rank
-// floor(u n) by id: FP64 proposal, confinement to the cell, single-precision
-// screen four candidates at a time, FP64 re-evaluation of any pair within the
-// guard band of contact.  Nothing per cell lives in local memory.
+// floor(u n) by id: FP64 proposal (its axes shared out over the group's
+// lanes), confinement to the cell, single-precision screen four candidates at
+// a time, FP64 re-evaluation of any pair within the guard band of contact.
+// Each pass is a programmatic dependent launch of the one before.  Nothing per
+// cell lives in local memory.
 #include <cooperative_groups.h>
 #include <cooperative_groups/reduce.h>
 
