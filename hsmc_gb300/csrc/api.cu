@@ -8,11 +8,13 @@
 // context's stream.
 #include <cuda_runtime.h>
 
+#include <atomic>
 #include <cmath>
 #include <cstddef>
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
+#include <mutex>
 #include <vector>
 
 #include "../../include/hsmc_gpu.h"
@@ -570,11 +572,12 @@ static int run_sweeps(hsmc_ctx *ctx, int n_sweeps, bool trace, bool npt, uint64_
       HSMC_CUDA(launch_move_flow(ctx->sp, ctx->prog, ctx->group, trace, ctx->flow_grid, ctx->stream));
       if (timing) HSMC_CUDA(cudaEventRecord(ctx->ev_pass[16 * s + 1], ctx->stream));
     } else {
-      for (int k = 0; k < 8; k++) {
-        if (timing) HSMC_CUDA(cudaEventRecord(ctx->ev_pass[16 * s + 2 * k], ctx->stream));
-        launch_move_pass(ctx->sp, k, ctx->group, trace, ctx->pass_grid, ctx->stream);
-        if (timing) HSMC_CUDA(cudaEventRecord(ctx->ev_pass[16 * s + 2 * k + 1], ctx->stream));
-      }
+      // timed as a whole: events between the passes would break the
+      // programmatic dependent launches that overlap one pass's tail with
+      // the next pass's start, so the eight passes are bracketed together
+      if (timing) HSMC_CUDA(cudaEventRecord(ctx->ev_pass[16 * s], ctx->stream));
+      for (int k = 0; k < 8; k++) launch_move_pass(ctx->sp, k, ctx->group, trace, ctx->pass_grid, ctx->stream);
+      if (timing) HSMC_CUDA(cudaEventRecord(ctx->ev_pass[16 * s + 1], ctx->stream));
     }
     if (npt) launch_volume_move(ctx->sp, s, ctx->margin, ctx->stream);
     enqueue_cavity(ctx, s);
@@ -591,12 +594,11 @@ static int run_sweeps(hsmc_ctx *ctx, int n_sweeps, bool trace, bool npt, uint64_
   ctx->last_total_ms = ms;
   if (timing) {
     double sum = 0.0;
-    for (int s = 0; s < rest; s++)
-      for (int k = 0; k < per_sweep; k++) {
-        float t = 0.f;
-        HSMC_CUDA(cudaEventElapsedTime(&t, ctx->ev_pass[16 * s + 2 * k], ctx->ev_pass[16 * s + 2 * k + 1]));
-        sum += t;
-      }
+    for (int s = 0; s < rest; s++) {
+      float t = 0.f;
+      HSMC_CUDA(cudaEventElapsedTime(&t, ctx->ev_pass[16 * s], ctx->ev_pass[16 * s + 1]));
+      sum += t;
+    }
     ctx->last_move_ms = sum;
     ctx->last_move_launches = per_sweep * rest;
   }
@@ -805,25 +807,35 @@ int hsmc_gpu_pressv(hsmc_ctx *ctx, double dr, double rmax, int nbins, uint64_t *
 // race on it.
 static __device__ __align__(256) unsigned long long g_rdf_noalloc_bins[HSMC_RDF_NOALLOC_MAX_BINS];
 
+// The address is looked up once per device.  Several contexts may be driven
+// from different host threads, so the first calls on a device can meet here:
+// the lookup runs under a mutex and the address is published with a release
+// store, which the unlocked fast path reads with an acquire load (a thread
+// never sees a non-null entry before the address it holds).
+static std::mutex g_noalloc_mu;
+static std::atomic<unsigned long long *> g_noalloc_addr[256];
+
 static unsigned long long *noalloc_bins_on(int device, int *status) {
-  static unsigned long long *addr[256] = {nullptr};
-  static bool ready[256] = {false};
   *status = HSMC_OK;
   if (device < 0 || device >= 256) {
     *status = HSMC_ERR_NO_DEVICE;
     return nullptr;
   }
-  if (!ready[device]) {
+  unsigned long long *a = g_noalloc_addr[device].load(std::memory_order_acquire);
+  if (a) return a;
+  std::lock_guard<std::mutex> lock(g_noalloc_mu);
+  a = g_noalloc_addr[device].load(std::memory_order_relaxed);
+  if (!a) {
     void *p = nullptr;
-    cudaError_t e = cudaGetSymbolAddress(&p, g_rdf_noalloc_bins);
-    if (e != cudaSuccess) {
-      *status = cuda_status(e);
+    const cudaError_t e = cudaGetSymbolAddress(&p, g_rdf_noalloc_bins);
+    if (e != cudaSuccess || p == nullptr) {
+      *status = cuda_status(e != cudaSuccess ? e : cudaErrorInvalidSymbol);
       return nullptr;
     }
-    addr[device] = (unsigned long long *)p;
-    ready[device] = true;
+    a = static_cast<unsigned long long *>(p);
+    g_noalloc_addr[device].store(a, std::memory_order_release);
   }
-  return addr[device];
+  return a;
 }
 
 int hsmc_gpu_rdf_noalloc(hsmc_ctx *ctx, double dr, double rmax, int nbins, uint64_t *counts) {
