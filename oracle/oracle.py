@@ -26,7 +26,11 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 ORACLE_SO = os.path.join(HERE, "liboracle.so")
 REF_SO = os.path.join(HERE, "_ref", "libhsmc_ref.so")
 REF_EXE = os.path.join(HERE, "_ref", "hsmc_ref")
-REF_SRC = "/root/reference/src"
+# The reference checkout: $HSMC_REFERENCE, else a directory named
+# "reference" beside this repository.  Only the oracle's build and the
+# fixture scripts read it; nothing that runs without it needs it.
+REF_ROOT = os.environ.get("HSMC_REFERENCE") or os.path.join(os.path.dirname(HERE), "..", "reference")
+REF_SRC = os.path.normpath(os.path.join(REF_ROOT, "src"))
 
 _dp = np.ctypeslib.ndpointer(dtype=np.float64, flags="C_CONTIGUOUS")
 _u32p = np.ctypeslib.ndpointer(dtype=np.uint32, flags="C_CONTIGUOUS")
@@ -44,7 +48,7 @@ def build_oracle(with_reference: bool | None = None) -> None:
         with_reference = os.path.isdir(REF_SRC)
     if with_reference:
         targets.append("ref")
-    subprocess.run(["make", "-s", "-C", HERE] + targets, check=True)
+    subprocess.run(["make", "-s", "-C", HERE, "REF_SRC=" + REF_SRC] + targets, check=True)
 
 
 def reference_available() -> bool:

@@ -22,7 +22,10 @@ import sys
 import types
 
 HERE = os.path.dirname(os.path.abspath(__file__))
-REF_PY = "/root/reference/python"
+sys.path.insert(0, os.path.dirname(os.path.dirname(HERE)))
+from oracle.oracle import REF_ROOT  # noqa: E402  ($HSMC_REFERENCE, else ../reference)
+
+REF_PY = os.path.normpath(os.path.join(REF_ROOT, "python"))
 OUT = os.path.join(HERE, "stat_ref")
 
 
