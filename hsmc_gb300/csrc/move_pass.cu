@@ -22,17 +22,11 @@
 #include <cooperative_groups.h>
 #include <cooperative_groups/reduce.h>
 
-#include "engine.cuh"
+#include "screen.cuh"
 
 namespace cg = cooperative_groups;
 
 namespace hsmc {
-
-// Neighbour offsets of the 26 cells around a cell, packed (dx+1) | (dy+1)<<2
-// | (dz+1)<<4, in the order x-major, the cell itself left out.
-__constant__ unsigned char c_nbr[26] = {
-    0x00, 0x10, 0x20, 0x04, 0x14, 0x24, 0x08, 0x18, 0x28, 0x01, 0x11, 0x21, 0x05,
-    0x25, 0x09, 0x19, 0x29, 0x02, 0x12, 0x22, 0x06, 0x16, 0x26, 0x0a, 0x1a, 0x2a};
 
 // Shared memory of one 128-thread block of k_move_pass<G, CAP>:
 //   pool    PR x 128 float4: neighbour entry e of group gl sits in row e / G,
@@ -78,34 +72,6 @@ __device__ __forceinline__ void cp_async8(void *dst, const void *src) {
 
 __device__ __forceinline__ void cp_async_wait_all() {
   asm volatile("cp.async.commit_group;\ncp.async.wait_group 0;\n" ::: "memory");
-}
-
-// Periodic image (a multiple of the box side) of neighbour `code` of cell
-// (ix, iy, iz) as seen from that cell.
-__device__ __forceinline__ void image_of(unsigned code, int ix, int iy, int iz, const int *nc, const float *L32,
-                                         float &imx, float &imy, float &imz) {
-  const int ox = (int)(code & 3u) - 1, oy = (int)((code >> 2) & 3u) - 1, oz = (int)(code >> 4) - 1;
-  imx = (ix + ox < 0) ? -L32[0] : (ix + ox >= nc[0] ? L32[0] : 0.f);
-  imy = (iy + oy < 0) ? -L32[1] : (iy + oy >= nc[1] ? L32[1] : 0.f);
-  imz = (iz + oz < 0) ? -L32[2] : (iz + oz >= nc[2] ? L32[2] : 0.f);
-}
-
-// Index of neighbour `code` of cell c = (ix, iy, iz): a linear offset for an
-// interior cell, periodic wrapping otherwise.
-__device__ __forceinline__ int neighbour_cell(unsigned code, int ix, int iy, int iz, int c, const int *nc,
-                                              bool interior) {
-  const int ox = (int)(code & 3u) - 1, oy = (int)((code >> 2) & 3u) - 1, oz = (int)(code >> 4) - 1;
-  if (interior) return c + ox + nc[0] * (oy + nc[1] * oz);
-  int x = ix + ox, y = iy + oy, z = iz + oz;
-  x += x < 0 ? nc[0] : (x >= nc[0] ? -nc[0] : 0);
-  y += y < 0 ? nc[1] : (y >= nc[1] ? -nc[1] : 0);
-  z += z < 0 ? nc[2] : (z >= nc[2] ? -nc[2] : 0);
-  return x + nc[0] * (y + nc[1] * z);
-}
-
-__device__ __forceinline__ float dist2(float ux, float uy, float uz, const float4 &q) {
-  const float dx = ux - q.x, dy = uy - q.y, dz = uz - q.z;
-  return dx * dx + dy * dy + dz * dz;
 }
 
 // Everything a pass needs that is fixed for the launch (or the pass).

@@ -9,7 +9,8 @@
 //                   (presst_compute_hist src/compute_press.c:243-273,
 //                   vol_move src/moves.c:104-112)
 //   k_widom         test-particle insertions (src/compute_widom_chem_pot.c:44-120)
-//   k_replay        check_overlap on given trial positions (src/moves.c:157-212)
+//   k_replay        check_overlap on given trial positions, screened as the move
+//                   pass screens a trial (src/moves.c:157-212)
 //   k_ql            Steinhardt q_l per particle (src/compute_order_parameter.c:99-229)
 // Every decision that the reference takes in FP64 is taken here in FP64 with
 // its operation order; single precision only discards pairs that are
@@ -17,6 +18,7 @@
 #include <cooperative_groups.h>
 
 #include "cellview.cuh"
+#include "screen.cuh"
 
 namespace cg = cooperative_groups;
 
@@ -185,16 +187,59 @@ void launch_widom(const SysPtrs &p, long long n, unsigned long long seq, const d
 }
 
 // ----------------------------------------------------------------- replay
+// check_overlap (src/moves.c:157-212) at given trial positions, screened
+// exactly as a move-pass trial is: the position's grid coordinates against
+// the slots of its cell and of the 26 cells around it (imaged across the
+// periodic faces), single precision outside the guard band of contact, the
+// reference's FP64 distance inside it (screen.cuh).  A replayed decision
+// therefore tests the band the move pass relies on, at any box size.
 __global__ void __launch_bounds__(256) k_replay(SysPtrs p, const int *ids, const double *pos_in, int n,
                                                 uint8_t *ov_out) {
   const CellView v = current_view(p);
   const Box *bx = p.box;
   const double len[3] = {bx->len[0], bx->len[1], bx->len[2]};
   const double half[3] = {bx->half[0], bx->half[1], bx->half[2]};
-  const Stencil s{{1, 1, 1}};
+  const float lo = 1.0f - bx->band, hi = 1.0f + bx->band;
   const int k = blockIdx.x * blockDim.x + threadIdx.x;
   if (k >= n) return;
-  ov_out[k] = point_overlaps(v, p, s, pos_in[3 * k], pos_in[3 * k + 1], pos_in[3 * k + 2], ids[k], len, half) ? 1 : 0;
+  const double x = pos_in[3 * k], y = pos_in[3 * k + 1], z = pos_in[3 * k + 2];
+  const int skip = ids[k];
+  int ix, iy, iz;
+  float ux, uy, uz;
+  axis_cell(__double2float_rn(x), v.sh[0], v.L32[0], v.iw[0], v.nc[0], ix, ux);
+  axis_cell(__double2float_rn(y), v.sh[1], v.L32[1], v.iw[1], v.nc[1], iy, uy);
+  axis_cell(__double2float_rn(z), v.sh[2], v.L32[2], v.iw[2], v.nc[2], iz, uz);
+  const int c = ix + v.nc[0] * (iy + v.nc[1] * iz);
+  bool ov = false;
+  auto screen = [&](const float4 &q) {
+    if (ov || __float_as_int(q.w) == skip) return;
+    const float r2 = dist2(ux, uy, uz, q);
+    if (r2 < lo) {
+      ov = true;
+    } else if (r2 <= hi) {
+      double ox, oy, oz;
+      load_xyz(p.pos, __float_as_int(q.w), ox, oy, oz);
+      ov = ref_r2(x, y, z, ox, oy, oz, len, half) < 1.0;
+    }
+  };
+  {
+    const int m = v.cnt[c];
+    const int nn = m < v.cap ? m : v.cap;
+    for (int q = 0; q < nn; q++) {
+      const Slot o = v.slot[(size_t)c * v.cap + q];
+      screen(make_float4(o.x, o.y, o.z, __int_as_float(o.id)));
+    }
+  }
+  for (int o26 = 0; o26 < 26 && !ov; o26++) {
+    const unsigned code = c_nbr[o26];
+    const int nb = neighbour_cell(code, ix, iy, iz, c, v.nc, false);
+    float imx, imy, imz;
+    image_of(code, ix, iy, iz, v.nc, v.L32, imx, imy, imz);
+    const int m = v.cnt[nb];
+    const int nn = m < v.cap ? m : v.cap;
+    for (int q = 0; q < nn; q++) screen(imaged_entry(v.slot[(size_t)nb * v.cap + q], imx, imy, imz));
+  }
+  ov_out[k] = ov ? 1 : 0;
 }
 
 void launch_overlap_replay(const SysPtrs &p, const int *ids, const double *pos_in, int n, uint8_t *ov_out,

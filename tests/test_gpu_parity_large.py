@@ -1,0 +1,115 @@
+"""Bit-exact decisions at the benchmarked geometries.
+
+The single-precision screen of the move pass decides a pair outside a guard
+band of contact whose width grows with the box side (single-precision
+coordinates lose absolute precision as |x| grows).  These tests check the
+decisions against the oracle (the reference's FP64 check_overlap and
+part_move, src/moves.c:27-80, 157-212, 400-431) where the coordinates are
+largest:
+
+  * the large NVT fluid: N = 256,000 (40^3 FCC) at rho = 0.85, L = 67.03;
+  * the NpT crystal's box: N = 1,048,576 (64^3 FCC) at rho = 1.04, L = 100.27.
+
+Two kinds of evidence, every call through the C ABI:
+  * adversarial trial positions: a particle moved toward its nearest
+    neighbour until their distance is within a few ulp of contact, or at
+    r^2 = 1 +- f * band with f on both sides of 1 (the pairs the single
+    precision screen decides alone, just outside the band), drawn mostly
+    near the box faces where coordinates are largest and images are added;
+    screened exactly as a move-pass trial (k_replay shares its screen);
+  * whole traced sweeps of the full systems replayed trial by trial by the
+    oracle: decisions and final configurations bit-identical.
+"""
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+C2 = dict(rho=0.85, cells=40, dr=0.13, melt=300)   # N = 256,000
+C5 = dict(rho=1.04, cells=64, dr=0.11, melt=20)    # N = 1,048,576
+
+
+def band_of(L):
+    return float(np.float32(2.0**-24 * (48.0 * L + 16.0) + 1e-6))
+
+
+def prepared(oracle_mod, gpu, cfg, seed):
+    g = gpu.HardSphereSystem(rho=cfg["rho"], cells=cfg["cells"], dr_max=cfg["dr"], seed=seed)
+    g.sweep_nvt(cfg["melt"])
+    conf = g.download()
+    o = oracle_mod.OracleSim(rho=cfg["rho"], n_cells=cfg["cells"], seed=seed, dr_max=cfg["dr"], neigh_dr=1.05,
+                             neigh_max_part=10)
+    o.set_config(conf)
+    return o, g, conf
+
+
+def adversarial_points(conf, L, band, rng, count):
+    """Trial positions of particle i at a chosen distance from its nearest
+    neighbour j: (kind 0) |r| = 1 + k 2^-52, k in [-4, 4]; (kind 1)
+    r^2 = 1 + s f band, s = +-1, f in [0.5, 2].  Three quarters of the
+    particles are taken with a coordinate within 1.5 of a box face."""
+    from scipy.spatial import cKDTree
+
+    x = conf[:, 1:].copy()
+    near_face = np.any((x < 1.5) | (x > L - 1.5), axis=1)
+    face_ids = np.flatnonzero(near_face)
+    n_face = (3 * count) // 4
+    ids = np.concatenate([rng.choice(face_ids, n_face), rng.integers(0, len(x), count - n_face)])
+    tree = cKDTree(np.mod(x, L), boxsize=L)
+    _, nn = tree.query(np.mod(x[ids], L), k=2)
+    j = nn[:, 1]
+    d = x[ids] - x[j]
+    d -= L * np.round(d / L)
+    r = np.linalg.norm(d, axis=1)
+    kind = rng.integers(0, 2, count)
+    k = rng.integers(-4, 5, count)
+    f = rng.uniform(0.5, 2.0, count)
+    s = np.where(rng.random(count) < 0.5, -1.0, 1.0)
+    target = np.where(kind == 0, 1.0 + k * 2.0**-52, np.sqrt(1.0 + s * f * band))
+    p = x[j] + d * (target / r)[:, None]
+    p = np.where(p >= L, p - L, np.where(p < 0.0, p + L, p))
+    return ids.astype(np.int32), p, kind, s * f
+
+
+@pytest.mark.parametrize("cfg", [C2, C5], ids=["N256k_L67", "N1M_L100"])
+def test_adversarial_screen_decisions_at_large_coordinates(oracle_mod, gpu_lib, cfg):
+    o, g, conf = prepared(oracle_mod, gpu_lib, cfg, seed=17)
+    L = o.box()["lx"]
+    assert abs(L - g.get_box()[0]) == 0.0
+    band = band_of(L)
+    rng = np.random.default_rng(5)
+    ids, pos, kind, sf = adversarial_points(conf, L, band, rng, 40000)
+    got = g.overlap_replay(ids, pos)
+    want = np.array([o.check_overlap_at(int(i), *p) for i, p in zip(ids, pos)], dtype=np.uint8)
+    mism = np.flatnonzero(got != want)
+    assert mism.size == 0, f"{mism.size} decisions differ, first at {ids[mism[0]]} {pos[mism[0]]}"
+    # both outcomes occur where the single-precision screen decides alone,
+    # just outside the band on either side, and in the FP64 recheck region
+    outside = (kind == 1) & (np.abs(sf) > 1.0)
+    assert want[outside & (sf < 0)].mean() > 0.99   # inside contact: overlap
+    assert want[outside & (sf > 0)].mean() < 0.9    # beyond contact: mostly free
+    assert 0 < want[kind == 0].sum() < (kind == 0).sum()
+    g.close()
+
+
+@pytest.mark.parametrize("cfg,sweeps", [(C2, 2), (C5, 1)], ids=["N256k_L67", "N1M_L100"])
+def test_traced_full_size_sweeps_replay_bit_exact(oracle_mod, gpu_lib, cfg, sweeps):
+    """Every trial of whole sweeps of the full system (512,000 trials at
+    N = 256,000; 1,048,576 at N = 1,048,576) replayed by the oracle."""
+    o, g, _ = prepared(oracle_mod, gpu_lib, cfg, seed=23)
+    rec, cnt = g.sweeps_traced(sweeps)
+    assert len(rec) == o.n * sweeps and cnt[0] == o.n * sweeps
+    rec = rec[np.lexsort((rec[:, 2], rec[:, 1], rec[:, 0]))]
+    nc, l32, iw, _ = g.grid_info()
+    shifts = rec[:, 8:11].copy().view(np.float32)
+    o.reset_counters()
+    dec = o.replay_checkerboard(rec[:, 3].astype(np.int32), rec[:, 4:7], rec[:, 1], shifts, nc, l32, iw)
+    assert not np.any(dec == 3), "a traced particle was not in its cell"
+    mism = np.flatnonzero(dec != rec[:, 7].astype(np.int32))
+    assert mism.size == 0, f"{mism.size} of {len(dec)} decisions differ"
+    assert np.array_equal(o.get_config(), g.download())
+    # the band was exercised: trials with at least one FP64 re-evaluation
+    rechecked = int(rec[:, 11].sum())
+    assert rechecked > 100, rechecked
+    assert cnt[1] == np.sum(dec == 0)
+    g.close()
