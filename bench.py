@@ -37,6 +37,14 @@ CELLS = 40
 N = 4 * CELLS**3
 SWEEPS_PER_STEP = 100
 TARGET_ACC = 0.40
+# dr_max of both arms: the reference's own chain (random particle, N moves
+# per sweep; the oracle) tuned toward 40 % acceptance on the equilibrated
+# fluid at rho = 0.85 (32,000 spheres melted for 1500 sweeps, then 600-sweep
+# samples per step size: 40.8 % at 0.160, 39.6 % at 0.165).  Both arms run
+# this step size from the lattice, so they sample the same state with the
+# same trial moves; the checkerboard's acceptance is lower by its
+# cell-boundary rejections.
+DR_MAX = 0.1635
 B_MOVE = 24.0 * (2.0 + 27.0 * RHO)  # algorithmic bytes per trial move
 # DRAM bytes (read + write) of one launch of the move kernels on this
 # workload, from ncu captures of this bench command (cache-flushed replay, so
@@ -46,6 +54,10 @@ MOVE_DRAM_BYTES = {"k_move_pass": 31664896.0, "k_move_flow": None}
 # same captures): the working set is L2-resident, so this is the traffic the
 # timed launches actually move.
 MOVE_L2_BYTES = {"k_move_pass": 1476367 * 32.0, "k_move_flow": None}
+# The configuration both arms report: the same state, chain parameters and start.
+CONFIG = {"workload": "NVT fluid N=256000 (40^3 FCC start) rho=0.85 cubic periodic, FP64 positions",
+          "n_particles": N, "rho": RHO, "dr_max": DR_MAX, "start": "FCC lattice, melted during the warm-up steps",
+          "l2": "flushed between timed steps on the GPU (256 MB write); the host arm has no device cache"}
 METRIC = "trial moves/s @N=256k rho=0.85"
 
 
@@ -127,22 +139,20 @@ def reduce_over_ranks(moves, total_ms, e2e_moves, e2e_s, world, device):
     return moves / (total_ms * 1e-3), e2e_moves / e2e_s, total_ms
 
 
-def tune_dr(sysm, dr0=0.12, sweeps=20, rounds=8):
+def tune_dr(sysm, dr0=0.12, sweeps=50, rounds=10, tol=0.005):
     """Secant search of dr_max toward the target acceptance, as the
-    reference's optimiser does (src/optimizer.c:23-64), after melting the
-    lattice start."""
+    reference's optimiser does (src/optimizer.c:23-64), on an already
+    equilibrated system (no lattice re-upload), with 50-sweep samples."""
     def acc(dr):
         sysm.set_step(dr)
         c = sysm.sweep_nvt(sweeps)
         return float(c[1]) / float(c[0])
 
-    sysm.set_step(dr0)
-    sysm.sweep_nvt(50)
     d1, a1 = dr0, acc(dr0)
     d2 = d1 * 2 if a1 > TARGET_ACC else d1 / 2
     a2 = acc(d2)
     for _ in range(rounds):
-        if a2 == a1:
+        if a2 == a1 or abs(a2 - TARGET_ACC) < tol:
             break
         d = d2 - (a2 - TARGET_ACC) * (d2 - d1) / (a2 - a1)
         d = min(max(abs(d), 1e-3), 1.0)
@@ -200,17 +210,19 @@ def run_reference_arm(args):
     if rank != 0:
         return 0
     procs = os.cpu_count() or 1
-    dr = 0.13  # tuned value for this state point (40% acceptance)
     sweeps_per_step = 1
-    rate, timed, wall = cpu_reference_throughput(dr, procs, sweeps_per_step, args.steps, args.warmup)
+    rate, timed, wall = cpu_reference_throughput(DR_MAX, procs, sweeps_per_step, args.steps, args.warmup)
     line = {
         "impl": "reference", "metric": METRIC, "value": rate, "unit": "trial moves/s", "n_gpus": args.gpus,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * timed / args.steps,
-        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-        "config": {"workload": "NVT fluid N=256000 (40^3 FCC) rho=0.85 cubic periodic, dr_max tuned to 40%",
-                   "step": f"{sweeps_per_step} sweep per system, one system per core", "systems": procs},
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+        "data": "synthetic (FCC lattice start, seeded random streams)",
+        "config": dict(CONFIG),
+        "step": f"{sweeps_per_step} sweep of each of {procs} independent systems (one per host core)",
         "cpu_baseline": {"value": rate, "unit": "trial moves/s", "cores": procs, "kind": "port",
-                         "sample": f"{procs} independent systems x {args.steps} timed sweeps (+{args.warmup} warm-up)"},
+                         "sample": f"{procs} independent systems x {args.steps} timed sweeps (+{args.warmup} "
+                                   f"warm-up), the reference algorithm restated in C (oracle/hsmc_oracle.c), "
+                                   f"pinned bit for bit to the reference build"},
         "e2e": {"value": rate, "unit": "trial moves/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line), flush=True)
@@ -234,13 +246,11 @@ def run_gpu_arm(args):
     dev = torch.cuda.current_device()
     import hsmc_gb300
 
-    sysm = hsmc_gb300.HardSphereSystem(rho=RHO, cells=CELLS, dr_max=0.12, seed=2026 + rank)
-    dr, acc = tune_dr(sysm)
+    sysm = hsmc_gb300.HardSphereSystem(rho=RHO, cells=CELLS, dr_max=DR_MAX, seed=2026 + rank)
     lanes = sysm.autotune(8)
     schedule, _ = sysm.get_schedule()  # 1: dataflow sweep (one launch), 0: one launch per colour pass
-    # The reference restarts from the lattice after optimising (src/nvt.c:58-62).
+    # the autotuner's sweeps are not part of the chain: restart from the lattice
     sysm.upload(hsmc_gb300.lattice_config(RHO, (CELLS,) * 3))
-    sysm.set_step(dr)
     flush = torch.empty(256 * 1024 * 1024, dtype=torch.uint8, device="cuda")  # > 129 MB L2
 
     for _ in range(args.warmup):
@@ -267,14 +277,17 @@ def run_gpu_arm(args):
     barrier()
     clk = clocks.stop()
 
-    # --- per-kernel timing of the dominant kernel (move pass), same workload
+    # --- the dominant kernel (move pass) on the same workload: one event
+    # pair around the eight passes of each sweep, which keeps the
+    # programmatic dependent launches between passes
     sysm.set_profiling(True)
-    kern_ms, kern_n = 0.0, 0
+    kern_ms, kern_n, prof_ms = 0.0, 0, 0.0
     for _ in range(max(1, args.steps // 4)):
         flush.fill_(1)
         torch.cuda.synchronize()
         sysm.sweep_nvt(SWEEPS_PER_STEP)
-        _, m, k = sysm.last_timing()
+        t, m, k = sysm.last_timing()
+        prof_ms += t
         kern_ms += m
         kern_n += k
     sysm.set_profiling(False)
@@ -295,13 +308,16 @@ def run_gpu_arm(args):
     value, e2e_val, total_ms = reduce_over_ranks(moves, total_ms, e2e_steps * SWEEPS_PER_STEP * N, e2e_s, world,
                                                  "cuda")
     peak, peak_kind = peaks()
+    ms_per_step = total_ms / args.steps
     # a dataflow launch makes a whole sweep (N trial moves); a colour pass
     # visits an eighth of the cells (N/8 trial moves on average)
     moves_per_launch = float(N) if schedule == 1 else N / 8.0
+    launches_per_sweep = 1 if schedule == 1 else 8
     kernel = "k_move_flow" if schedule == 1 else "k_move_pass"
     kern_avg_ms = kern_ms / kern_n if kern_n else float("nan")
     achieved = B_MOVE * moves_per_launch / (kern_avg_ms * 1e-3) / 1e9
-    per_sweep = 2 if schedule == 1 else 9  # build + move launches
+    move_ms_per_step = kern_avg_ms * launches_per_sweep * SWEEPS_PER_STEP
+    per_sweep = launches_per_sweep + 1  # build + move launches
     launches_per_step = SWEEPS_PER_STEP * per_sweep + math.ceil(SWEEPS_PER_STEP / 8)
     traffic = MOVE_DRAM_BYTES.get(kernel)
     l2_bytes = MOVE_L2_BYTES.get(kernel)
@@ -309,27 +325,34 @@ def run_gpu_arm(args):
                                         "kind": "ncu lts__t_sectors_srcunit_tex.sum x 32 B per launch"}
     line = {
         "metric": METRIC, "value": value, "unit": "trial moves/s", "n_gpus": world, "steps": args.steps,
-        "warmup": args.warmup, "ms_per_step": total_ms / args.steps, "higher_is_better": True,
+        "warmup": args.warmup, "ms_per_step": ms_per_step, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f64",
-        "data": "synthetic (FCC lattice start, seeded Philox streams)",
-        "config": {"workload": "NVT fluid N=256000 (40^3 FCC) rho=0.85 cubic periodic, FP64 positions, "
-                               "checkerboard sweeps", "n_particles": N, "rho": RHO,
-                   "sweeps_per_step": SWEEPS_PER_STEP, "dr_max": dr, "acceptance": acc_moves / max(moves, 1),
-                   "lanes_per_cell": lanes,
-                   "schedule": "dataflow (8 passes per launch)" if schedule == 1 else "one launch per pass",
-                   "l2": "flushed between steps (256 MB write)", "parallelism": f"replicas x{world}"},
+        "data": "synthetic (FCC lattice start, seeded random streams)",
+        "config": dict(CONFIG),
+        "step": f"{SWEEPS_PER_STEP} checkerboard sweeps of one system per GPU (each N trial moves), CUDA graphs "
+                f"of 8 sweeps",
+        "engine": {"lanes_per_cell": lanes,
+                   "schedule": "dataflow (8 passes per launch)" if schedule == 1 else "one launch per colour pass",
+                   "acceptance": acc_moves / max(moves, 1), "parallelism": f"replicas x{world}"},
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                      "frac": achieved / peak, "traffic": traffic,
                      "traffic_kind": "ncu dram__bytes_read.sum + dram__bytes_write.sum per launch, cold cache",
                      "kernel": kernel, "bytes_per_move": B_MOVE, "moves_per_launch": moves_per_launch,
-                     "avg_launch_ms": kern_avg_ms, "peak_kind": peak_kind, "l2": l2},
+                     "avg_launch_ms": kern_avg_ms,
+                     "avg_launch_kind": "CUDA events around the 8 passes of each sweep, summed over "
+                                        f"{kern_n // launches_per_sweep} sweeps / {kern_n} passes",
+                     "move_ms_per_step": move_ms_per_step,
+                     "move_share_of_step": move_ms_per_step / ms_per_step,
+                     "step_achieved": B_MOVE * N * SWEEPS_PER_STEP / (ms_per_step * 1e-3) / 1e9,
+                     "step_frac": B_MOVE * N * SWEEPS_PER_STEP / (ms_per_step * 1e-3) / 1e9 / peak,
+                     "peak_kind": peak_kind, "l2": l2},
         "e2e": {"value": e2e_val, "unit": "trial moves/s", "h2d_bytes_per_step": N * 32,
                 "d2h_bytes_per_step": N * 32 + 6 * 8 + 4 * 8},
         "clocks": clk,
         "gpu_launches": launches_per_step * args.steps,
     }
     if rank == 0 and not args.no_cpu_baseline:
-        line["cpu_baseline"] = cpu_baseline_sample(dr)
+        line["cpu_baseline"] = cpu_baseline_sample(DR_MAX)
     if rank == 0:
         print(json.dumps(line), flush=True)
     sysm.close()

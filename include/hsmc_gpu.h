@@ -311,8 +311,9 @@ int hsmc_gpu_hold_region(hsmc_ctx *ctx, int region);
 /* Timing of the last sweep call, from CUDA events on the context's stream:
  * total device time, and (only with profiling on) the summed time and count
  * of the move-pass kernel launches.  With profiling on, sweeps are launched
- * one kernel at a time with an event pair around each move pass instead of
- * as a CUDA graph. */
+ * one kernel at a time instead of as a CUDA graph, with one event pair around
+ * the eight move passes of each sweep (the passes keep their programmatic
+ * dependent launches); move_launches counts the passes so bracketed. */
 int hsmc_gpu_set_profiling(hsmc_ctx *ctx, int on);
 int hsmc_gpu_last_timing(hsmc_ctx *ctx, double *total_ms, double *move_kernel_ms, int *move_launches);
 
