@@ -23,6 +23,9 @@ def _bind(lib):
     lib.hsmc_batch_sweeps.argtypes = [vp, C.c_int, vp]
     lib.hsmc_batch_pressv.argtypes = [vp, C.c_double, C.c_double, C.c_int, vp]
     lib.hsmc_batch_last_timing.argtypes = [vp, P(C.c_double)]
+    lib.hsmc_batch_set_schedule.argtypes = [vp, C.c_int, C.c_int, C.c_int]
+    lib.hsmc_batch_get_schedule.argtypes = [vp, vp]
+    lib.hsmc_batch_autotune.argtypes = [vp, C.c_int, vp]
     lib._batch_bound = True
 
 
@@ -129,6 +132,25 @@ class ReplicaBatch:
         self.set_steps(d2)
         self.dr = d2
         return d2, a2
+
+    def set_schedule(self, schedule: int, cluster_blocks: int = 4, tile: int = 2) -> None:
+        """0: flat launches per colour pass (CUDA graphs of 8 sweeps); 1: every
+        sweep of a call in one persistent launch of thread-block clusters, one
+        cluster per bundle of replicas.  The same chain."""
+        _check(self._lib.hsmc_batch_set_schedule(self._h, schedule, cluster_blocks, tile),
+               "hsmc_batch_set_schedule")
+
+    def get_schedule(self):
+        out = np.zeros(3, dtype=np.int32)
+        _check(self._lib.hsmc_batch_get_schedule(self._h, out.ctypes.data), "hsmc_batch_get_schedule")
+        return tuple(int(x) for x in out)
+
+    def autotune(self, sweeps_per_variant: int = 16):
+        """Times both schedules and every cluster size and tile; keeps the
+        fastest and returns (schedule, cluster_blocks, tile)."""
+        out = np.zeros(3, dtype=np.int32)
+        _check(self._lib.hsmc_batch_autotune(self._h, sweeps_per_variant, out.ctypes.data), "hsmc_batch_autotune")
+        return tuple(int(x) for x in out)
 
     def last_timing(self):
         t = C.c_double()

@@ -24,7 +24,7 @@ LIB = os.path.join(PKG, "libhsmc_gpu.so")
 BIN_DIR = os.path.join(PKG, "bin")
 EXE = os.path.join(BIN_DIR, "hsmc")
 
-CU_SOURCES = ["api.cu", "sweep.cu", "move_pass.cu", "observables.cu", "batch.cu", "lwidom.cu", "cluster.cu", "cavity.cu", "sweep_small.cu"]
+CU_SOURCES = ["api.cu", "sweep.cu", "move_pass.cu", "observables.cu", "batch.cu", "lwidom.cu", "cluster.cu", "cavity.cu", "sweep_small.cu", "batch_persist.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-Xcompiler", "-O2",
               "--expt-relaxed-constexpr", "-I" + os.path.join(ROOT, "include")]

@@ -5,6 +5,7 @@
 // (blockIdx.y = replica).  Sweeps run as CUDA graphs.
 #include <cuda_runtime.h>
 
+#include <algorithm>
 #include <cstddef>
 #include <cstdio>
 #include <vector>
@@ -13,6 +14,16 @@
 #include "engine.cuh"
 
 using namespace hsmc;
+
+namespace hsmc {
+// batch_persist.cu
+int batch_persist_max_reps();
+int batch_persist_max_clusters(int cap, int cluster_blocks);
+cudaError_t prepare_batch_persist();
+cudaError_t launch_batch_persist(int cap, const SysPtrs *reps, const int *rep_ids, const int *nstart,
+                                 const int *gstart, const int *cstart, const int *bundle, int n_bundles,
+                                 int n_sweeps, int cluster_blocks, cudaStream_t s);
+}  // namespace hsmc
 
 namespace {
 
@@ -68,7 +79,36 @@ struct hsmc_batch {
   cudaGraphExec_t graph = nullptr;
   cudaEvent_t ev0 = nullptr, ev1 = nullptr;
   double last_ms = 0.0;
+  // schedule 1: every sweep of a call in one launch of thread-block
+  // clusters, one cluster per bundle of replicas (batch_persist.cu)
+  int schedule = 0;
+  int cluster_blocks = 4, tile = 2;
+  struct Bundles {
+    int cap = 8, n_bundles = 0;
+    SysPtrs *d_reps = nullptr;
+    int *d_ids = nullptr, *d_nstart = nullptr, *d_gstart = nullptr, *d_cstart = nullptr, *d_bundle = nullptr;
+  };
+  std::vector<Bundles> bundles;  // per cell capacity, for (bundled_cb, bundled_tile)
+  int bundled_cb = 0, bundled_tile = 0;
+  int persist_graph_sweeps = 0;
+  cudaGraphExec_t persist_graph = nullptr;  // one persistent launch per class, for persist_graph_sweeps
 };
+
+static void free_bundles(hsmc_batch *b) {
+  for (auto &q : b->bundles) {
+    cudaFree(q.d_reps);
+    cudaFree(q.d_ids);
+    cudaFree(q.d_nstart);
+    cudaFree(q.d_gstart);
+    cudaFree(q.d_cstart);
+    cudaFree(q.d_bundle);
+  }
+  b->bundles.clear();
+  b->bundled_cb = b->bundled_tile = 0;
+  if (b->persist_graph) cudaGraphExecDestroy(b->persist_graph);
+  b->persist_graph = nullptr;
+  b->persist_graph_sweeps = 0;
+}
 
 static int batch_check(hsmc_batch *b) {
   BATCH_CUDA(cudaGetLastError());
@@ -91,6 +131,7 @@ void hsmc_batch_destroy(hsmc_batch *b) {
   if (!b) return;
   if (b->stream) cudaStreamSynchronize(b->stream);
   if (b->graph) cudaGraphExecDestroy(b->graph);
+  free_bundles(b);
   cudaFree(b->d_reps);
   cudaFree(b->d_nstart);
   cudaFree(b->d_gstart);
@@ -322,11 +363,148 @@ static void enqueue_batch_sweep(hsmc_batch *b, long long offset) {
     }
 }
 
+// Packs the replicas of each cell capacity into bundles of at most `tile`
+// active cells per lane group of a cluster (first fit, largest replica
+// first, at most batch_persist_max_reps() replicas each; a larger replica is
+// a bundle of its own), orders the bundles largest first, so the clusters
+// that start first take the longest, and uploads the tables the persistent
+// kernel reads.
+static int build_bundles(hsmc_batch *b) {
+  if (!b->bundles.empty() && b->bundled_cb == b->cluster_blocks && b->bundled_tile == b->tile) return HSMC_OK;
+  free_bundles(b);
+  const int max_reps = batch_persist_max_reps();
+  for (int c : {8, 16, 32}) {
+    std::vector<int> ks;
+    for (int k = 0; k < b->reps; k++)
+      if (b->sp[k].cap == c) ks.push_back(k);
+    if (ks.empty()) continue;
+    const long long target = (long long)b->tile * b->cluster_blocks * (128 / (c / 4));
+    auto cells = [&](int k) { return (long long)b->hbox[k].ncell / 8; };
+    std::stable_sort(ks.begin(), ks.end(), [&](int x, int y) { return cells(x) > cells(y); });
+    std::vector<std::vector<int>> bun;
+    std::vector<long long> load;
+    for (int k : ks) {
+      size_t j = 0;
+      while (j < bun.size() && ((int)bun[j].size() >= max_reps || load[j] + cells(k) > target)) j++;
+      if (j == bun.size()) {
+        bun.emplace_back();
+        load.push_back(0);
+      }
+      bun[j].push_back(k);
+      load[j] += cells(k);
+    }
+    std::vector<size_t> order(bun.size());
+    for (size_t j = 0; j < order.size(); j++) order[j] = j;
+    std::stable_sort(order.begin(), order.end(), [&](size_t x, size_t y) { return load[x] > load[y]; });
+    std::vector<SysPtrs> sp;
+    std::vector<int> ids, ns(1, 0), gs(1, 0), cs(1, 0), bs(1, 0);
+    for (size_t j : order) {
+      for (int k : bun[j]) {
+        sp.push_back(b->sp[k]);
+        ids.push_back(k);
+        ns.push_back(ns.back() + b->sp[k].n);
+        gs.push_back(gs.back() + b->hbox[k].ncell / 8);
+        cs.push_back(cs.back() + b->hbox[k].ncell);
+      }
+      bs.push_back((int)sp.size());
+    }
+    hsmc_batch::Bundles q;
+    q.cap = c;
+    q.n_bundles = (int)bun.size();
+    const size_t nr = sp.size();
+    cudaError_t ce;
+    if ((ce = cudaMalloc(&q.d_reps, sizeof(SysPtrs) * nr)) || (ce = cudaMalloc(&q.d_ids, sizeof(int) * nr)) ||
+        (ce = cudaMalloc(&q.d_nstart, sizeof(int) * (nr + 1))) ||
+        (ce = cudaMalloc(&q.d_gstart, sizeof(int) * (nr + 1))) ||
+        (ce = cudaMalloc(&q.d_cstart, sizeof(int) * (nr + 1))) ||
+        (ce = cudaMalloc(&q.d_bundle, sizeof(int) * bs.size())) ||
+        (ce = cudaMemcpy(q.d_reps, sp.data(), sizeof(SysPtrs) * nr, cudaMemcpyHostToDevice)) ||
+        (ce = cudaMemcpy(q.d_ids, ids.data(), sizeof(int) * nr, cudaMemcpyHostToDevice)) ||
+        (ce = cudaMemcpy(q.d_nstart, ns.data(), sizeof(int) * (nr + 1), cudaMemcpyHostToDevice)) ||
+        (ce = cudaMemcpy(q.d_gstart, gs.data(), sizeof(int) * (nr + 1), cudaMemcpyHostToDevice)) ||
+        (ce = cudaMemcpy(q.d_cstart, cs.data(), sizeof(int) * (nr + 1), cudaMemcpyHostToDevice)) ||
+        (ce = cudaMemcpy(q.d_bundle, bs.data(), sizeof(int) * bs.size(), cudaMemcpyHostToDevice))) {
+      b->bundles.push_back(q);
+      free_bundles(b);
+      return cuda_fail(ce);
+    }
+    b->bundles.push_back(q);
+  }
+  b->bundled_cb = b->cluster_blocks;
+  b->bundled_tile = b->tile;
+  return HSMC_OK;
+}
+
+// The persistent schedule's launches for n_sweeps sweeps (one per cell
+// capacity), captured once into a CUDA graph and kept while n_sweeps and the
+// bundles stay the same.
+static int ensure_persist_graph(hsmc_batch *b, int n_sweeps) {
+  int e = build_bundles(b);
+  if (e) return e;
+  if (b->persist_graph && b->persist_graph_sweeps == n_sweeps) return HSMC_OK;
+  if (b->persist_graph) cudaGraphExecDestroy(b->persist_graph);
+  b->persist_graph = nullptr;
+  cudaGraph_t g = nullptr;
+  BATCH_CUDA(cudaStreamBeginCapture(b->stream, cudaStreamCaptureModeThreadLocal));
+  cudaError_t le = cudaSuccess;
+  for (const auto &q : b->bundles)
+    if (le == cudaSuccess)
+      le = launch_batch_persist(q.cap, q.d_reps, q.d_ids, q.d_nstart, q.d_gstart, q.d_cstart, q.d_bundle,
+                                q.n_bundles, n_sweeps, b->cluster_blocks, b->stream);
+  cudaError_t ce = cudaStreamEndCapture(b->stream, &g);
+  if (le != cudaSuccess || ce != cudaSuccess) {
+    if (g) cudaGraphDestroy(g);
+    return cuda_fail(le != cudaSuccess ? le : ce);
+  }
+  ce = cudaGraphInstantiate(&b->persist_graph, g, 0);
+  cudaGraphDestroy(g);
+  if (ce != cudaSuccess) {
+    b->persist_graph = nullptr;
+    return cuda_fail(ce);
+  }
+  b->persist_graph_sweeps = n_sweeps;
+  return HSMC_OK;
+}
+
+int hsmc_batch_set_schedule(hsmc_batch *b, int schedule, int cluster_blocks, int tile) {
+  if (!b || (schedule != 0 && schedule != 1)) return HSMC_ERR_INVALID_ARG;
+  if (schedule == 1) {
+    if ((cluster_blocks != 1 && cluster_blocks != 2 && cluster_blocks != 4 && cluster_blocks != 8) || tile < 1 ||
+        tile > 64)
+      return HSMC_ERR_INVALID_ARG;
+    int dev = 0, cl = 0;
+    BATCH_CUDA(cudaGetDevice(&dev));
+    BATCH_CUDA(cudaDeviceGetAttribute(&cl, cudaDevAttrClusterLaunch, dev));
+    if (!cl) return HSMC_ERR_INVALID_ARG;
+    BATCH_CUDA(prepare_batch_persist());
+    for (const auto &cls : b->classes)
+      if (batch_persist_max_clusters(cls.cap, cluster_blocks) <= 0) return HSMC_ERR_INVALID_ARG;
+    if (cluster_blocks != b->cluster_blocks || tile != b->tile) free_bundles(b);
+    b->cluster_blocks = cluster_blocks;
+    b->tile = tile;
+  }
+  b->schedule = schedule;
+  return HSMC_OK;
+}
+
+int hsmc_batch_get_schedule(hsmc_batch *b, int out[3]) {
+  if (!b || !out) return HSMC_ERR_INVALID_ARG;
+  out[0] = b->schedule;
+  out[1] = b->cluster_blocks;
+  out[2] = b->tile;
+  return HSMC_OK;
+}
+
 int hsmc_batch_sweeps(hsmc_batch *b, int n_sweeps, uint64_t *counters) {
   if (!b || n_sweeps < 0) return HSMC_ERR_INVALID_ARG;
   for (int k = 0; k < b->reps; k++)
     if (!b->uploaded[k]) return HSMC_ERR_INVALID_ARG;
-  if (!b->graph) {
+  const bool persist = b->schedule == 1 && n_sweeps > 0;
+  if (persist) {
+    int e = ensure_persist_graph(b, n_sweeps);
+    if (e) return e;
+  }
+  if (!persist && !b->graph) {
     cudaGraph_t g = nullptr;
     BATCH_CUDA(cudaStreamBeginCapture(b->stream, cudaStreamCaptureModeThreadLocal));
     for (int s = 0; s < kBatchGraphSweeps; s++) enqueue_batch_sweep(b, s);
@@ -345,14 +523,18 @@ int hsmc_batch_sweeps(hsmc_batch *b, int n_sweeps, uint64_t *counters) {
                                (size_t)b->reps, b->stream));
   BATCH_CUDA(cudaMemset2DAsync(&b->st[0].status, sizeof(DevState), 0, sizeof(int), (size_t)b->reps, b->stream));
   BATCH_CUDA(cudaEventRecord(b->ev0, b->stream));
-  int done = 0;
-  while (n_sweeps - done >= kBatchGraphSweeps) {
-    BATCH_CUDA(cudaGraphLaunch(b->graph, b->stream));
-    done += kBatchGraphSweeps;
+  if (persist) {
+    BATCH_CUDA(cudaGraphLaunch(b->persist_graph, b->stream));
+  } else {
+    int done = 0;
+    while (n_sweeps - done >= kBatchGraphSweeps) {
+      BATCH_CUDA(cudaGraphLaunch(b->graph, b->stream));
+      done += kBatchGraphSweeps;
+    }
+    const int rest = n_sweeps - done;
+    for (int s = 0; s < rest; s++) enqueue_batch_sweep(b, s);
+    if (rest > 0) launch_advance_batch(b->d_reps, b->reps, rest, b->stream);
   }
-  const int rest = n_sweeps - done;
-  for (int s = 0; s < rest; s++) enqueue_batch_sweep(b, s);
-  if (rest > 0) launch_advance_batch(b->d_reps, b->reps, rest, b->stream);
   BATCH_CUDA(cudaEventRecord(b->ev1, b->stream));
   int e = batch_check(b);
   if (e) return e;
@@ -372,6 +554,41 @@ int hsmc_batch_sweeps(hsmc_batch *b, int n_sweeps, uint64_t *counters) {
     }
   }
   return status;
+}
+
+// Times the flat schedule and the persistent one with every cluster size
+// (1, 2, 4, 8 blocks) and tile (1, 2, 4 active cells per lane group and
+// bundle), each over sweeps_per_variant sweeps after an untimed call of 8,
+// and keeps the fastest.  The chain is the same for all of them.
+int hsmc_batch_autotune(hsmc_batch *b, int sweeps_per_variant, int out[3]) {
+  if (!b || sweeps_per_variant <= 0) return HSMC_ERR_INVALID_ARG;
+  struct V {
+    int s, cb, tile;
+  };
+  std::vector<V> vs{{0, b->cluster_blocks, b->tile}};
+  for (int cb : {1, 2, 4, 8})
+    for (int tile : {1, 2, 4}) vs.push_back({1, cb, tile});
+  V best = vs[0];
+  double best_ms = 1e300;
+  for (const V &v : vs) {
+    if (hsmc_batch_set_schedule(b, v.s, v.cb, v.tile) != HSMC_OK) continue;
+    int e = hsmc_batch_sweeps(b, kBatchGraphSweeps, nullptr);
+    if (!e) e = hsmc_batch_sweeps(b, sweeps_per_variant, nullptr);
+    if (e) return e;
+    if (b->last_ms < best_ms) {
+      best_ms = b->last_ms;
+      best = v;
+    }
+  }
+  int e = hsmc_batch_set_schedule(b, best.s, best.cb, best.tile);
+  if (e) return e;
+  if (best.s == 0 && (b->cluster_blocks != best.cb || b->tile != best.tile)) {
+    // the flat launches won: keep the cluster shape the batch had before
+    free_bundles(b);
+    b->cluster_blocks = best.cb;
+    b->tile = best.tile;
+  }
+  return out ? hsmc_batch_get_schedule(b, out) : HSMC_OK;
 }
 
 int hsmc_batch_pressv(hsmc_batch *b, double dr, double rmax, int nbins, uint64_t *counts) {

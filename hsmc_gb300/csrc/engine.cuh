@@ -37,6 +37,30 @@ __device__ __forceinline__ int find_rep(const int *start, int n, int x) {
   return lo;
 }
 
+// The grid shift of sweep s of replica rep: a uniform point of one cell
+// (w = the cell edges), from 24-bit fractions of one Philox draw.
+__device__ __forceinline__ void sweep_shift(uint64_t seed, uint32_t rep, unsigned long long s, const float w[3],
+                                            float sh[3]) {
+  const U32x4 rs = draw4(seed, rep << 8, 0u, s, TAG_SHIFT);
+  sh[0] = __fmul_rn(__uint2float_rn(rs.x >> 8) * 5.9604644775390625e-08f, w[0]);
+  sh[1] = __fmul_rn(__uint2float_rn(rs.y >> 8) * 5.9604644775390625e-08f, w[1]);
+  sh[2] = __fmul_rn(__uint2float_rn(rs.z >> 8) * 5.9604644775390625e-08f, w[2]);
+}
+
+// The colour order of the eight passes of sweep s of replica rep: a
+// Fisher-Yates shuffle driven by seven Philox words.
+__device__ __forceinline__ void sweep_perm(uint64_t seed, uint32_t rep, unsigned long long s, int perm[8]) {
+  for (int k = 0; k < 8; k++) perm[k] = k;
+  const U32x4 ra = draw4(seed, rep << 8, 0u, s, TAG_PERM), rb = draw4(seed, (rep << 8) | 1u, 0u, s, TAG_PERM);
+  const uint32_t r[7] = {ra.x, ra.y, ra.z, ra.w, rb.x, rb.y, rb.z};
+  for (int k = 7; k >= 1; k--) {
+    const int j = (int)__umulhi(r[7 - k], (unsigned)(k + 1));
+    const int tmp = perm[k];
+    perm[k] = perm[j];
+    perm[j] = tmp;
+  }
+}
+
 // The arrays of one layout.  A select, not an index: indexing the parameter
 // struct by a runtime value would copy it to local memory.
 __device__ __forceinline__ int *cnt_of(const SysPtrs &p, int layout) { return layout ? p.cnt[1] : p.cnt[0]; }

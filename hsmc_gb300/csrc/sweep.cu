@@ -29,6 +29,12 @@ namespace hsmc {
 template <bool BATCH>
 __global__ void __launch_bounds__(256) k_build(SysPtrs p1, const SysPtrs *reps, const int *nstart, int n_reps,
                                                long long offset) {
+  // A programmatic dependent of the pass before it (launch_build): the
+  // blocks may become resident while that pass drains and wait here for its
+  // positions; the first pass of the sweep may then be scheduled, and waits
+  // for this build in turn.
+  asm volatile("griddepcontrol.wait;\n" ::: "memory");
+  asm volatile("griddepcontrol.launch_dependents;\n" ::: "memory");
   int i = blockIdx.x * blockDim.x + threadIdx.x;
   uint32_t rep = 0u;
   if (BATCH) {
@@ -41,11 +47,10 @@ __global__ void __launch_bounds__(256) k_build(SysPtrs p1, const SysPtrs *reps, 
   const Box *bx = p.box;
   const unsigned long long s = st->sweep_base + (unsigned long long)offset;
   const unsigned long long seed = st->seed;
-  const U32x4 rs = draw4(seed, rep << 8, 0u, s, TAG_SHIFT);
-  const float w0 = bx->w32[0], w1 = bx->w32[1], w2 = bx->w32[2];
-  const float sh0 = __fmul_rn(__uint2float_rn(rs.x >> 8) * 5.9604644775390625e-08f, w0);
-  const float sh1 = __fmul_rn(__uint2float_rn(rs.y >> 8) * 5.9604644775390625e-08f, w1);
-  const float sh2 = __fmul_rn(__uint2float_rn(rs.z >> 8) * 5.9604644775390625e-08f, w2);
+  const float w[3] = {bx->w32[0], bx->w32[1], bx->w32[2]};
+  float sh[3];
+  sweep_shift(seed, rep, s, w, sh);
+  const float sh0 = sh[0], sh1 = sh[1], sh2 = sh[2];
   const int layout = (int)(s & 1ull);
   if (i == 0) {
     DevState *ws = p.st;
@@ -53,15 +58,8 @@ __global__ void __launch_bounds__(256) k_build(SysPtrs p1, const SysPtrs *reps, 
     ws->params.shift32[0] = sh0;
     ws->params.shift32[1] = sh1;
     ws->params.shift32[2] = sh2;
-    int perm[8] = {0, 1, 2, 3, 4, 5, 6, 7};
-    const U32x4 ra = draw4(seed, rep << 8, 0u, s, TAG_PERM), rb = draw4(seed, (rep << 8) | 1u, 0u, s, TAG_PERM);
-    const uint32_t r[7] = {ra.x, ra.y, ra.z, ra.w, rb.x, rb.y, rb.z};
-    for (int k = 7; k >= 1; k--) {  // Fisher-Yates
-      int j = (int)__umulhi(r[7 - k], (unsigned)(k + 1));
-      int tmp = perm[k];
-      perm[k] = perm[j];
-      perm[j] = tmp;
-    }
+    int perm[8];
+    sweep_perm(seed, rep, s, perm);
     for (int k = 0; k < 8; k++) ws->params.perm[k] = perm[k];
   }
   if (i >= p.n) return;
@@ -228,7 +226,19 @@ void launch_volume_move(const SysPtrs &p, long long sweep_offset, double margin,
 void launch_build(const SysPtrs &p, long long sweep_offset, int num_sms, cudaStream_t s) {
   (void)num_sms;
   const int blocks = (p.n + 255) / 256;
-  k_build<false><<<blocks > 0 ? blocks : 1, 256, 0, s>>>(p, nullptr, nullptr, 0, sweep_offset);
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = dim3((unsigned)(blocks > 0 ? blocks : 1));
+  cfg.blockDim = dim3(256);
+  cfg.dynamicSmemBytes = 0;
+  cfg.stream = s;
+  cudaLaunchAttribute attr[1];
+  attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+  attr[0].val.programmaticStreamSerializationAllowed = 1;
+  cfg.attrs = attr;
+  cfg.numAttrs = 1;
+  const SysPtrs *no_reps = nullptr;
+  const int *no_start = nullptr;
+  cudaLaunchKernelEx(&cfg, k_build<false>, p, no_reps, no_start, 0, sweep_offset);
 }
 
 void launch_build_batch(const SysPtrs *reps, const int *nstart, int n_reps, int tot_n, long long sweep_offset,

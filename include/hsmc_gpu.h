@@ -252,6 +252,27 @@ int hsmc_batch_pressv(hsmc_batch *b, double dr, double rmax, int nbins, uint64_t
 /* device time of the last hsmc_batch_sweeps call, in milliseconds */
 int hsmc_batch_last_timing(hsmc_batch *b, double *total_ms);
 
+/* Schedule of hsmc_batch_sweeps.  0 (the default): every sweep is a cell
+ * build and eight colour passes, each one flat launch over the replicas of
+ * one cell capacity, in CUDA graphs of 8 sweeps.  1: persistent, every sweep
+ * of a call in one launch (per cell capacity) of thread-block clusters of
+ * cluster_blocks blocks (1, 2, 4, 8), captured in a CUDA graph: the replicas
+ * are packed into bundles of about tile x (lane groups of a cluster) active
+ * cells (tile 1..64; at most 32 replicas per bundle), one cluster per bundle,
+ * which runs all the call's sweeps of its replicas with the cluster's
+ * hardware barrier between the build and the passes; bundles never wait on
+ * one another.  The chain is the same in both (sweep_nvt, src/nvt.c:201-209,
+ * per replica).  HSMC_ERR_INVALID_ARG for a cluster shape the device cannot
+ * hold.  get_schedule: out = {schedule, cluster_blocks, tile}. */
+int hsmc_batch_set_schedule(hsmc_batch *b, int schedule, int cluster_blocks, int tile);
+int hsmc_batch_get_schedule(hsmc_batch *b, int out[3]);
+
+/* Times schedule 0 and schedule 1 with every cluster size (1, 2, 4, 8) and
+ * tile (1, 2, 4) over sweeps_per_variant sweeps each, after an untimed call
+ * of 8 sweeps, and keeps the fastest (out as get_schedule).  These are
+ * ordinary sweeps of every replica's chain. */
+int hsmc_batch_autotune(hsmc_batch *b, int sweeps_per_variant, int out[3]);
+
 /* ----------------------------------------------------- replay and checks
  * Entry points that evaluate the reference's decisions on given inputs
  * without advancing the chain.  They exist so a caller (or a test) can compare
@@ -280,10 +301,12 @@ int hsmc_gpu_sweeps_traced(hsmc_ctx *ctx, int n_sweeps, uint32_t *rec, int64_t c
 int hsmc_gpu_grid_info(hsmc_ctx *ctx, int nc[3], float len32[3], float inv_w32[3], int *capacity);
 
 /* Times every schedule (below) with every lanes-per-cell mapping (1, 2, 4,
- * 8) over sweeps_per_variant sweeps each (rounded up to a multiple of 8) and
- * keeps the fastest; *lanes_out receives its mapping.  The chain depends on
- * neither (same random counters, exact decisions), so these are ordinary
- * sweeps of the run. */
+ * 8) over sweeps_per_variant sweeps each (rounded up to a multiple of 8),
+ * twice over in two rounds, each timed run after an untimed graph's worth of
+ * sweeps, and keeps the variant with the fastest run; *lanes_out receives
+ * its mapping.  The chain depends on neither (same random counters, exact
+ * decisions), so these are ordinary sweeps of the run: 2 x (8 + S) sweeps
+ * per variant. */
 int hsmc_gpu_autotune(hsmc_ctx *ctx, int sweeps_per_variant, int *lanes_out);
 
 /* Schedule of the eight colour passes of a sweep: 0 = one launch per pass
@@ -308,8 +331,9 @@ int hsmc_gpu_get_schedule(hsmc_ctx *ctx, int *schedule, int *lanes_per_cell);
  * progress words).  The context stays usable throughout. */
 int hsmc_gpu_hold_region(hsmc_ctx *ctx, int region);
 
-/* Timing of the last sweep call, from CUDA events on the context's stream:
- * total device time, and (only with profiling on) the summed time and count
+/* Timing of the last sweep or observable call (g(r), pressure scans, Widom,
+ * q_l), from CUDA events on the context's stream around its kernels: total
+ * device time, and (for sweeps with profiling on) the summed time and count
  * of the move-pass kernel launches.  With profiling on, sweeps are launched
  * one kernel at a time instead of as a CUDA graph, with one event pair around
  * the eight move passes of each sweep (the passes keep their programmatic

@@ -99,3 +99,83 @@ def test_replica_pressures_follow_carnahan_starling(gpu_lib):
         eta = math.pi * rho / 6
         z_cs = (1 + eta + eta**2 - eta**3) / (1 - eta) ** 3
         assert abs(z - z_cs) < 0.12 * z_cs, (rho, z, z_cs)
+
+
+def _persistent_vs_flat(systems, sweeps, variants, min_cell_edge=0.0):
+    from hsmc_gb300.batch import ReplicaBatch
+
+    flat = ReplicaBatch(systems, min_cell_edge=min_cell_edge)
+    want_c = sum(flat.sweeps(n) for n in sweeps)
+    want = [flat.download(k) for k in range(len(systems))]
+    flat.close()
+    for cb, tile in variants:
+        b = ReplicaBatch(systems, min_cell_edge=min_cell_edge)
+        b.set_schedule(1, cb, tile)
+        assert b.get_schedule() == (1, cb, tile)
+        got_c = sum(b.sweeps(n) for n in sweeps)
+        for k in range(len(systems)):
+            assert np.array_equal(b.download(k), want[k]), (cb, tile, k)
+        assert np.array_equal(got_c, want_c), (cb, tile)
+        b.close()
+
+
+def test_persistent_schedule_is_the_flat_chain(gpu_lib):
+    """Every sweep of a call in one launch of thread-block clusters, one
+    cluster per bundle of replicas: every replica's configuration and
+    counters bit-identical to the flat launches', for several cluster sizes
+    and tiles (one replica per bundle up to many), over calls of 1, 7 and 16
+    sweeps."""
+    rng = np.random.default_rng(11)
+    systems = [(float(rng.uniform(0.3, 0.94)), int(rng.integers(3, 9)), 0.12, 300 + k) for k in range(40)]
+    _persistent_vs_flat(systems, [1, 7, 16], [(1, 1), (2, 2), (4, 1), (8, 4)])
+
+
+def test_persistent_schedule_mixed_cell_capacities(gpu_lib):
+    """Larger cells (16 and 32 slots, 4 and 8 lanes per cell) in the same
+    batch: one persistent launch per capacity, still the flat chain."""
+    systems = [(0.45, 6, 0.3, 5), (0.80, 6, 0.15, 6), (0.30, 7, 0.4, 7), (0.60, 5, 0.25, 8)]
+    _persistent_vs_flat(systems, [9], [(2, 1), (4, 2)], min_cell_edge="auto")
+
+
+def test_persistent_replica_zero_and_observables(gpu_lib):
+    """Replica 0 under the persistent schedule is the single context's chain,
+    and the layout it leaves behind serves the observables (virial counts
+    equal a single context's on the same configuration)."""
+    from hsmc_gb300.batch import ReplicaBatch
+
+    systems = [(0.80, 6, 0.15, 77), (0.50, 4, 0.30, 78), (0.92, 5, 0.08, 79)]
+    b = ReplicaBatch(systems)
+    b.set_schedule(1, 2, 1)
+    c = b.sweeps(27)
+    s = gpu_lib.HardSphereSystem(rho=0.80, cells=6, dr_max=0.15, seed=77)
+    cs = s.sweep_nvt(27)
+    assert np.array_equal(b.download(0), s.download())
+    assert np.array_equal(c[0], cs)
+    nb, dr = 5, 0.01
+    got = b.pressv_counts(dr, 1.0 + nb * dr, nb)
+    for k, (rho, n, d, seed) in enumerate(systems):
+        t = gpu_lib.HardSphereSystem(rho=rho, cells=n, dr_max=d, seed=seed, conf=b.download(k))
+        assert np.array_equal(got[k], t.compute_pressv_counts(dr, 1.0 + nb * dr, nb))
+    # switching back to the flat launches continues the same chain
+    b.set_schedule(0)
+    b.sweeps(5)
+    s.sweep_nvt(5)
+    assert np.array_equal(b.download(0), s.download())
+
+
+def test_batch_autotune_keeps_the_chain(gpu_lib):
+    from hsmc_gb300.batch import ReplicaBatch
+
+    systems = [(0.7, 5, 0.2, 40 + k) for k in range(6)]
+    a = ReplicaBatch(systems)
+    sched = a.autotune(8)
+    assert sched[0] in (0, 1) and sched[1] in (1, 2, 4, 8) and sched[2] in (1, 2, 4)
+    assert a.get_schedule() == sched
+    a.sweeps(10)
+    # the same tuning sweeps, then the other schedule: the same chain
+    b = ReplicaBatch(systems)
+    b.autotune(8)
+    b.set_schedule(1 - sched[0], 2, 2)
+    b.sweeps(10)
+    for k in range(len(systems)):
+        assert np.array_equal(a.download(k), b.download(k))
