@@ -531,8 +531,14 @@ size_t cluster_small_smem(int n, int ncell) {
 int cluster_grid(int n, int ncell, int num_sms) {
   const size_t small = cluster_small_smem(n, ncell);
   if (small) {
-    if (cudaFuncSetAttribute(k_cluster_small, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)small) ==
-        cudaSuccess)
+    // the allowance is the kernel's, shared by every context on the device:
+    // set to the device's limit, so a smaller system never lowers it below
+    // what an earlier, larger one needs
+    int dev = 0, optin = 0;
+    if (cudaGetDevice(&dev) == cudaSuccess &&
+        cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev) == cudaSuccess &&
+        small <= (size_t)optin &&
+        cudaFuncSetAttribute(k_cluster_small, cudaFuncAttributeMaxDynamicSharedMemorySize, optin) == cudaSuccess)
       return 0;  // the one-block shared-memory kernel
     cudaGetLastError();
   }

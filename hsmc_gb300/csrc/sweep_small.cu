@@ -495,12 +495,18 @@ size_t sweep_small_smem(int n, int ncell, int cap) {
   return bytes <= 224 * 1024 ? bytes : 0;  // of the 227 KB a block may have
 }
 
+// The shared-memory allowance is a property of the kernel, shared by every
+// context on the device: it is set to the device's limit, so that a context
+// with a smaller system never lowers what an earlier, larger one needs.
 bool prepare_sweep_small(size_t smem) {
-  return smem > 0 &&
-         cudaFuncSetAttribute(k_sweep_small<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) ==
+  int dev = 0, optin = 0;
+  if (smem == 0 || cudaGetDevice(&dev) != cudaSuccess ||
+      cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev) != cudaSuccess ||
+      smem > (size_t)optin)
+    return false;
+  return cudaFuncSetAttribute(k_sweep_small<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, optin) ==
              cudaSuccess &&
-         cudaFuncSetAttribute(k_sweep_small<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) ==
-             cudaSuccess;
+         cudaFuncSetAttribute(k_sweep_small<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, optin) == cudaSuccess;
 }
 
 void launch_sweep_small(const SysPtrs &p, int n_sweeps, bool npt, bool cavity, double margin, size_t smem,

@@ -340,3 +340,21 @@ def test_dataflow_wait_runs_out_and_reports(gpu_lib):
     s.rng_set_state(s.rng_state())  # rebuild the layout for the next sweep
     c = s.sweep_nvt(2)
     assert c[0] == 2 * s.n
+
+
+def test_contexts_of_different_sizes_coexist(gpu_lib):
+    """The shared-memory allowance of the one-block kernels is the kernel's,
+    not a context's: creating a smaller system after a larger one must not
+    stop the larger one from sweeping or making cluster moves."""
+    big = gpu_lib.HardSphereSystem(rho=0.8, cells=6, dr_max=0.15, seed=1)     # N = 864
+    big.sweep_nvt(1)
+    big.cluster_moves(1)
+    small = gpu_lib.HardSphereSystem(rho=0.5, cells=3, dr_max=0.3, seed=2)    # N = 108
+    assert big.get_schedule()[0] == 2 and small.get_schedule()[0] == 2
+    small.sweep_nvt(3)
+    small.cluster_moves(2)
+    c = big.sweep_nvt(5)
+    assert c[0] == 5 * big.n
+    assert len(big.cluster_moves(2)) == 2
+    small.close()
+    big.close()
