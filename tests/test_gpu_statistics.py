@@ -2,7 +2,8 @@
 10x10x10 FCC lattice at rho = 0.5): the GPU chain and the reference algorithm's
 chain (the CPU oracle, MT19937 draws) sample the same observables, and every
 one must agree within 3 combined blocking standard errors; the pressure also
-against Carnahan-Starling (src/analytic.c:112).
+against Carnahan-Starling (src/analytic.c:112) within 3 standard errors.  Each
+error is printed.
 
 The contact value comes from a linear fit of g(r) on [1, 1.05) as the
 reference's analysis does (python/hsmc_pressure.py:11-41): Z = 1 + 2 pi/3 rho g(1).
@@ -82,5 +83,6 @@ def test_observables_agree_with_reference_chain(oracle_mod, gpu_lib):
         report.append(f"{key}: gpu {mg:.5f} +- {eg:.5f}  reference {mr:.5f} +- {er:.5f}")
         assert abs(mg - mr) <= 3.0 * math.hypot(eg, er) + 1e-12, "\n".join(report)
     mz, ez = gpu["Z"]
-    assert abs(mz - z_cs) <= 3.0 * ez + 0.02 * z_cs, (mz, ez, z_cs)
-    print("\n".join(report), f"\nZ_CS = {z_cs:.5f}")
+    report.append(f"Z vs Carnahan-Starling {z_cs:.5f}: {(mz - z_cs) / ez:+.2f} sigma ({(mz - z_cs) / z_cs:+.3%})")
+    print("\n" + "\n".join(report))
+    assert abs(mz - z_cs) <= 3.0 * ez, "\n".join(report)
