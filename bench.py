@@ -247,7 +247,12 @@ def run_gpu_arm(args):
     import hsmc_gb300
 
     sysm = hsmc_gb300.HardSphereSystem(rho=RHO, cells=CELLS, dr_max=DR_MAX, seed=2026 + rank)
-    lanes = sysm.autotune(8)
+    if args.lanes:
+        sysm.set_schedule(1 if args.schedule == "dataflow" else 0, args.lanes)
+        lanes = args.lanes
+    else:
+        sysm.sweep_nvt(200)  # tune on the fluid, not on the lattice it starts from
+        lanes = sysm.autotune(16)
     schedule, _ = sysm.get_schedule()  # 1: dataflow sweep (one launch), 0: one launch per colour pass
     # the autotuner's sweeps are not part of the chain: restart from the lattice
     sysm.upload(hsmc_gb300.lattice_config(RHO, (CELLS,) * 3))
@@ -856,6 +861,93 @@ def run_cluster(args):
     return 0
 
 
+def run_kernels(args):
+    """Each kernel of the path, one at a time, on the large NVT fluid
+    (N = 256,000, rho = 0.85, 40^3 FCC start melted for --equil sweeps) and
+    the learned-Widom kernels on a 13,824-sphere fluid at rho = 0.94 (24^3
+    simple-cubic start, 500 sweeps): device time per call from CUDA events on
+    the engine's stream, units per call, and the kernel's algorithmic bytes
+    per unit, hence the achieved GB/s against the HBM peak.  The per-kernel
+    ncu summaries are captures of this command."""
+    import numpy as np
+    from hsmc_gb300 import HardSphereSystem
+    from hsmc_gb300.lwidom import LearnedWidom
+
+    peak, peak_kind = peaks()
+    s = HardSphereSystem(rho=RHO, cells=CELLS, dr_max=DR_MAX, seed=5)
+    s.set_schedule(0, 2)
+    s.sweep_nvt(args.equil)
+    reps = 5
+    rows = {}
+
+    def add(name, ms, units, unit, bytes_per_unit, note=""):
+        gbs = units * bytes_per_unit / (ms * 1e-3) / 1e9 if bytes_per_unit else None
+        rows[name] = {"ms_per_call": ms, "units_per_call": units, "unit": unit, "units_per_s": units / (ms * 1e-3),
+                      "algorithmic_bytes_per_unit": bytes_per_unit, "achieved_gbs": gbs,
+                      "frac_of_peak": gbs / peak if gbs else None, "note": note}
+
+    def med(fn):
+        ts = []
+        for _ in range(reps):
+            fn()
+            ts.append(s.last_timing()[0])
+        return float(np.median(ts))
+
+    s.set_profiling(True)
+    sweeps = 16
+    s.sweep_nvt(sweeps)
+    tot, mv, k = s.last_timing()
+    s.set_profiling(False)
+    add("k_move_pass", mv / k, N / 8, "trial move", B_MOVE, "events around the 8 passes of each sweep")
+    add("k_build", (tot - mv) / sweeps, N, "particle", 52.0,
+        "sweep time less its passes (build + one advance per 8 sweeps); 32 B position read, 16 B slot, 4 B count")
+    nb, dr = 400, 0.01
+    c = s.compute_rdf_counts(dr, 1 + nb * dr, nb)
+    add("k_pair_hist (g(r), r < 5)", med(lambda: s.compute_rdf_counts(dr, 1 + nb * dr, nb)), float(c.sum()),
+        "ordered pair within r_max", None, "FP64 distance per pair in the stencil's single-precision cut")
+    add("k_pair_hist (virial, [1, 1.05))", med(lambda: s.compute_pressv_counts(0.01, 1.05, 5)), N, "particle",
+        24.0 * (1 + 27 * RHO), "one 27-cell neighbourhood per particle")
+    xi = np.arange(1, 21) * 0.0005
+    sf = (1.0 - xi) ** (1.0 / 3.0)
+    add("k_scaled_scan (20 xi)", med(lambda: s.compute_presst(sf)), N, "particle", 24.0 * (1 + 27 * RHO),
+        "one neighbourhood per particle for all 20 scale factors")
+    add("k_vol_scan", med(lambda: s.scan_overlap(0.9999)), N, "particle", 24.0 * (1 + 27 * RHO),
+        "the NpT volume move's scan (early exit on an overlap)")
+    n_ins = 1_000_000
+    add("k_widom (10^6 insertions)", med(lambda: s.widom_insertion(n_ins)), n_ins, "insertion", 24.0 * 27 * RHO)
+    add("k_ql (l = 6, rc = 1.5)", med(lambda: s.global_ql(6, 1.5)), N, "particle", None,
+        "FP64 Legendre recurrences per bond")
+    s.close()
+
+    w = HardSphereSystem(rho=0.94, cells=24, lattice_type=1, dr_max=0.08, seed=77)
+    w.sweep_nvt(500)
+    lw = LearnedWidom(w, 0.5, seed=78, train_capacity=2_000_000)
+    lw.use_prior()
+    t_ref = [lw.refresh() for _ in range(reps)]
+    add("k_mlp_logits (refresh)", float(np.median(t_ref)), float(lw.n_subcells), "sub-cell pattern", None,
+        "MLP 27-64-64-1 forward on tcgen05, 12.3 kflop per pattern, then the proposal's scan")
+    lw.insert(20_000_000, alpha=0.1, keep_failures=0.05)
+    t_is = []
+    for _ in range(reps):
+        lw.insert(n_ins, alpha=0.1)
+        t_is.append(lw.last_ms())
+    add("k_widom_is (10^6 learned insertions)", float(np.median(t_is)), n_ins, "insertion", 24.0 * 27 * 0.94)
+    n_s, _ = lw.samples()
+    lw.train(epochs=1, batch=65536, lr=1e-3)
+    add("k_mlp_grad + Adam (1 epoch)", lw.last_ms(), float(n_s), "training outcome", None,
+        "forward + backward on tcgen05, about 57 kflop per outcome")
+    lw.close()
+    w.close()
+    line = {"metric": "per-kernel device time and achieved GB/s", "n_gpus": 1, "peak_gbs": peak,
+            "peak_kind": peak_kind, "data": "synthetic (lattice starts, seeded random streams)",
+            "config": {"workload": "kernels one at a time: NVT fluid N=256000 rho=0.85 (40^3 FCC, "
+                                   f"{args.equil} sweeps) and a rho=0.94 fluid N=13824 for the learned Widom",
+                       "dr_max": DR_MAX, "calls_per_kernel": reps},
+            "kernels": rows}
+    print(json.dumps(line), flush=True)
+    return 0
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -863,7 +955,12 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
-    ap.add_argument("--workload", default="fluid", choices=["fluid", "replicas", "widom", "npt", "cluster", "cavity", "small", "readme"])
+    ap.add_argument("--workload", default="fluid",
+                    choices=["fluid", "replicas", "widom", "npt", "cluster", "cavity", "small", "readme", "kernels"])
+    ap.add_argument("--lanes", type=int, default=0,
+                    help="fluid: lanes per cell (1, 2, 4, 8) instead of the autotuner's choice")
+    ap.add_argument("--schedule", default="barrier", choices=["barrier", "dataflow"],
+                    help="fluid, with --lanes: one launch per colour pass or the dataflow sweep")
     ap.add_argument("--replicas", type=int, default=512)
     ap.add_argument("--cell-edge", default="0",
                     help='replicas: smallest device-cell edge, a number or "auto" (min(rho^-1/3, 1.4))')
@@ -889,6 +986,8 @@ def main():
         return run_small(args)
     if args.workload == "readme":
         return run_readme(args)
+    if args.workload == "kernels":
+        return run_kernels(args)
     return run_gpu_arm(args)
 
 
