@@ -388,6 +388,7 @@ def run_replicas(args):
     n_tot = int(sum(b.n))
     dr, acc = b.tune_steps(0.1, target=TARGET_ACC)
     b.sweeps(args.equil)
+    schedule = b.autotune(16)  # flat launches or persistent clusters, cluster size and tile
     sweeps = args.sweeps
     per = 10
     nb, bin_ = 5, 0.01
@@ -428,6 +429,9 @@ def run_replicas(args):
         "config": {"workload": f"{reps} NVT replicas, n~U{{6..20}} (N 864..32000), rho~U[0.30,0.94], "
                                f"{sweeps} sweeps after {args.equil}", "n_particles_total": n_tot,
                    "min_cell_edge": args.cell_edge,
+                   "schedule": ("persistent: one launch of thread-block clusters per call, "
+                                f"{schedule[1]} blocks per cluster, tile {schedule[2]}") if schedule[0] == 1
+                               else "flat launches per colour pass, CUDA graphs of 8 sweeps",
                    "acceptance_min_max": [float(acc.min()), float(acc.max())]},
         "gpu_ms": t_gpu,
         "pressure": {"within_3se_of_cs": float(np.mean(np.abs(dev) < 3)),

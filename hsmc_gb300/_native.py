@@ -107,5 +107,6 @@ def load() -> C.CDLL:
     L.hsmc_gpu_cavity_trace_read.argtypes = [_vp, _vp, C.c_int64, _P(C.c_int64)]
     L.hsmc_gpu_cluster_move_at.argtypes = [_vp, _vp, C.c_int, C.c_int, _P(C.c_int64)]
     L.hsmc_gpu_last_timing.argtypes = [_vp, _P(C.c_double), _P(C.c_double), _P(C.c_int)]
+    L.hsmc_gpu_optimize.argtypes = [_vp, C.c_int, C.c_int, C.c_double, C.c_double, _vp]
     _lib = L
     return L

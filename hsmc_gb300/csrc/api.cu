@@ -632,6 +632,38 @@ static int run_sweeps(hsmc_ctx *ctx, int n_sweeps, bool trace, bool npt, uint64_
   return HSMC_OK;
 }
 
+// Enqueues n_sweeps ordinary sweeps on the production path (one block, or
+// graphs of 8 sweeps and single sweeps after them) without waiting for
+// them: the same kernels in the same order as run_sweeps, so the same chain.
+static int enqueue_sweeps(hsmc_ctx *ctx, int n_sweeps, bool npt) {
+  if (n_sweeps <= 0) return HSMC_OK;
+  if (ctx->small && ctx->cav_trace_cap == 0) {
+    launch_sweep_small(ctx->sp, n_sweeps, npt, ctx->cavity, ctx->margin, ctx->small_smem, ctx->stream);
+    ctx->sweep_base += (unsigned long long)n_sweeps;
+    for (int l = 0; l < 2; l++)
+      HSMC_CUDA(cudaMemsetAsync(ctx->sp.cnt[l], 0, sizeof(int) * (size_t)ctx->sp.ncell_alloc, ctx->stream));
+    launch_build(ctx->sp, -1, ctx->num_sms, ctx->stream);
+    reset_progress(ctx);
+    return HSMC_OK;
+  }
+  int e = ensure_graph(ctx, npt);
+  if (e) return e;
+  const bool direct = ctx->cav_trace_cap > 0 || (ctx->flow && ctx->flow_graph == 0);
+  int done = 0;
+  if (!direct) {
+    while (n_sweeps - done >= kGraphSweeps) {
+      HSMC_CUDA(cudaGraphLaunch(npt ? ctx->graph_npt : ctx->graph, ctx->stream));
+      done += kGraphSweeps;
+    }
+  }
+  const int rest = n_sweeps - done;
+  for (int s = 0; s < rest; s++) HSMC_CUDA(enqueue_sweep(ctx, s, false, npt));
+  if (rest > 0) launch_advance(ctx->sp, rest, ctx->stream);
+  ctx->sweep_base += (unsigned long long)n_sweeps;
+  if (npt || ctx->cavity) rebuild_current_layout(ctx);
+  return HSMC_OK;
+}
+
 static void drop_graphs(hsmc_ctx *ctx) {
   if (ctx->graph) cudaGraphExecDestroy(ctx->graph);
   if (ctx->graph_npt) cudaGraphExecDestroy(ctx->graph_npt);
@@ -714,6 +746,44 @@ int hsmc_gpu_autotune(hsmc_ctx *ctx, int sweeps_per_variant, int *lanes_out) {
   }
   if (lanes_out) *lanes_out = best_g;
   return HSMC_OK;
+}
+
+// The reference's optimiser (opt_nvt / opt_npt / opt_cavity_nvt,
+// src/optimizer.c:23-212) as one call: its opt_samples + 2 samples of
+// opt_sweeps / opt_samples sweeps are enqueued back to back, each followed
+// by k_opt_step, which sets the step for the next sample on the device; the
+// host waits once, at the end.
+int hsmc_gpu_optimize(hsmc_ctx *ctx, int opt_sweeps, int opt_samples, double part_target, double vol_target,
+                      double out[4]) {
+  if (!ctx || !ctx->uploaded || opt_samples <= 0 || opt_sweeps / opt_samples <= 0) return HSMC_ERR_INVALID_ARG;
+  const bool npt = ctx->prm.pressure > 0;
+  const int per = opt_sweeps / opt_samples;
+  clear_counters_async(ctx);
+  HSMC_CUDA(cudaMemsetAsync(&ctx->sp.st->status, 0, sizeof(int), ctx->stream));
+  HSMC_CUDA(cudaMemsetAsync(&ctx->sp.st->opt_acc0, 0, 4 * sizeof(unsigned long long), ctx->stream));
+  HSMC_CUDA(cudaEventRecord(ctx->ev_start, ctx->stream));
+  for (int j = 0; j < opt_samples + 2; j++) {
+    int e = enqueue_sweeps(ctx, per, npt);
+    if (e) return e;
+    launch_opt_step(ctx->sp, j, opt_samples, (unsigned long long)ctx->n * (unsigned long long)per * (j + 1),
+                    part_target, vol_target, npt, ctx->stream);
+  }
+  HSMC_CUDA(cudaEventRecord(ctx->ev_stop, ctx->stream));
+  int e = check_kernels(ctx);
+  if (e) return e;
+  timing_read(ctx);
+  DevState s;
+  if ((e = read_state(ctx, s))) return e;
+  if (npt) HSMC_CUDA(cudaMemcpy(&ctx->hbox, ctx->sp.box, sizeof(Box), cudaMemcpyDeviceToHost));
+  ctx->prm.dr_max = s.dr_max;
+  ctx->prm.dv_max = s.dv_max;
+  if (out) {
+    out[0] = s.dr_max;
+    out[1] = s.opt_a[1];
+    out[2] = s.dv_max;
+    out[3] = npt ? s.opt_av[1] : 0.0;
+  }
+  return s.status ? status_to_code(s.status) : HSMC_OK;
 }
 
 int hsmc_gpu_set_schedule(hsmc_ctx *ctx, int schedule, int lanes_per_cell) {

@@ -532,13 +532,17 @@ int cluster_grid(int n, int ncell, int num_sms) {
   const size_t small = cluster_small_smem(n, ncell);
   if (small) {
     // the allowance is the kernel's, shared by every context on the device:
-    // set to the device's limit, so a smaller system never lowers it below
-    // what an earlier, larger one needs
+    // set to the most the device allows beside the kernel's static shared
+    // memory, so a smaller system never lowers it below what an earlier,
+    // larger one needs
     int dev = 0, optin = 0;
+    cudaFuncAttributes fa{};
     if (cudaGetDevice(&dev) == cudaSuccess &&
         cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev) == cudaSuccess &&
-        small <= (size_t)optin &&
-        cudaFuncSetAttribute(k_cluster_small, cudaFuncAttributeMaxDynamicSharedMemorySize, optin) == cudaSuccess)
+        cudaFuncGetAttributes(&fa, k_cluster_small) == cudaSuccess &&
+        small <= (size_t)(optin - (int)fa.sharedSizeBytes) &&
+        cudaFuncSetAttribute(k_cluster_small, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             optin - (int)fa.sharedSizeBytes) == cudaSuccess)
       return 0;  // the one-block shared-memory kernel
     cudaGetLastError();
   }

@@ -220,6 +220,11 @@ struct DevState {
   // exactly when r2 <= cav_r2max (sqrt is correctly rounded, so monotone)
   double cav_r2min, cav_r2max;
   hsmc_cavity_psi_coeffs psi;
+  // the device optimiser (hsmc_gpu_optimize): the secant's last two points
+  // (step, acceptance) for the particle and the volume step, and the counters
+  // at the start of the current sample
+  double opt_d[2], opt_a[2], opt_v[2], opt_av[2];
+  unsigned long long opt_acc0, opt_moves0, opt_vacc0, opt_vmoves0;
 };
 
 // One particle in a cell: its grid coordinates t (single precision, from

@@ -129,6 +129,8 @@ int make_box(const double len[3], double rho, Box &b, int &cap, double min_edge 
 void launch_build(const SysPtrs &p, long long sweep_offset, int num_sms, cudaStream_t s);
 void launch_move_pass(const SysPtrs &p, int pass, int group, bool trace, int grid, cudaStream_t s);
 void launch_advance(const SysPtrs &p, int n_sweeps, cudaStream_t s);
+void launch_opt_step(const SysPtrs &p, int j, int n_samples, unsigned long long sweep_moves, double part_target,
+                     double vol_target, bool npt, cudaStream_t s);
 void launch_fill_u32(uint32_t *p, int n, uint32_t v, cudaStream_t s);
 void launch_volume_move(const SysPtrs &p, long long sweep_offset, double margin, cudaStream_t s);
 void launch_volume_scan(const SysPtrs &p, cudaStream_t s);

@@ -82,6 +82,80 @@ __global__ void __launch_bounds__(256) k_build(SysPtrs p1, const SysPtrs *reps, 
 
 __global__ void k_advance(DevState *st, int n) { st->sweep_base += (unsigned long long)n; }
 
+// One step of the reference's optimiser after sample j of the sampling loop
+// (opt_nvt src/optimizer.c:23-64, opt_npt :83-148, opt_cavity_nvt :172-212):
+// the sample's acceptance from the counters since the previous step, then
+// after the first sample the step doubled or halved, after the others the
+// secant step toward the target with the reference's clamps, as long as a
+// sample follows (j < n_samples + 1).  The arithmetic is the reference's
+// double-precision expression with no contraction.  sweep_moves: the
+// particle trial moves of every sample so far.
+__global__ void k_opt_step(DevState *st, int j, int n_samples, unsigned long long sweep_moves, double part_target,
+                           double vol_target, int npt) {
+  const unsigned long long acc = st->acc + st->cav_acc;
+  const unsigned long long moves = sweep_moves + st->cav_moves;
+  const double a = __ddiv_rn((double)(acc - st->opt_acc0), (double)(moves - st->opt_moves0));
+  const double av = npt ? __ddiv_rn((double)(st->vol_acc - st->opt_vacc0), (double)(st->vol_moves - st->opt_vmoves0))
+                        : 0.0;
+  st->opt_acc0 = acc;
+  st->opt_moves0 = moves;
+  st->opt_vacc0 = st->vol_acc;
+  st->opt_vmoves0 = st->vol_moves;
+  double dr = st->dr_max, dv = st->dv_max;
+  if (j == 0) {
+    st->opt_d[0] = dr;
+    st->opt_a[0] = a;
+    dr = a > part_target ? __dmul_rn(dr, 2.0) : __ddiv_rn(dr, 2.0);
+    if (npt) {
+      st->opt_v[0] = dv;
+      st->opt_av[0] = av;
+      dv = av > vol_target ? __dmul_rn(dv, 2.0) : __ddiv_rn(dv, 2.0);
+    }
+  } else {
+    st->opt_d[1] = dr;
+    st->opt_a[1] = a;
+    if (npt) {
+      st->opt_v[1] = dv;
+      st->opt_av[1] = av;
+    }
+    if (j <= n_samples) {
+      const double d1 = st->opt_d[0], d2 = st->opt_d[1], a1 = st->opt_a[0], a2 = st->opt_a[1];
+      dr = __dsub_rn(d2, __ddiv_rn(__dmul_rn(__dsub_rn(a2, part_target), __dsub_rn(d2, d1)), __dsub_rn(a2, a1)));
+      if (npt) {
+        const double v1 = st->opt_v[0], v2 = st->opt_v[1], b1 = st->opt_av[0], b2 = st->opt_av[1];
+        dv = __dsub_rn(v2, __ddiv_rn(__dmul_rn(__dsub_rn(b2, vol_target), __dsub_rn(v2, v1)), __dsub_rn(b2, b1)));
+        if (dr > 1.0) dr = 1.0;
+        if (dr <= 0.0) {
+          dr = -dr;
+          if (dr > 1.0) dr = __ddiv_rn(d2, 2.0);
+        }
+        if (dv <= 0.0) {
+          dv = -dv;
+          if (dv > 0.1) dv = __ddiv_rn(v2, 2.0);
+        }
+        st->opt_v[0] = v2;
+        st->opt_av[0] = b2;
+      } else {
+        if (dr > 1.0) {
+          dr = 1.0;
+        } else if (dr <= 0.0) {
+          dr = -dr;
+          if (dr > 1.0) dr = __ddiv_rn(d2, 2.0);
+        }
+      }
+      st->opt_d[0] = d2;
+      st->opt_a[0] = a2;
+    }
+  }
+  st->dr_max = dr;
+  st->dv_max = dv;
+}
+
+void launch_opt_step(const SysPtrs &p, int j, int n_samples, unsigned long long sweep_moves, double part_target,
+                     double vol_target, bool npt, cudaStream_t s) {
+  k_opt_step<<<1, 1, 0, s>>>(p.st, j, n_samples, sweep_moves, part_target, vol_target, npt ? 1 : 0);
+}
+
 __global__ void k_fill_u32(uint32_t *p, int n, uint32_t v) {
   for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) p[i] = v;
 }

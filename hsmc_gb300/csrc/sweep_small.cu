@@ -496,17 +496,27 @@ size_t sweep_small_smem(int n, int ncell, int cap) {
 }
 
 // The shared-memory allowance is a property of the kernel, shared by every
-// context on the device: it is set to the device's limit, so that a context
-// with a smaller system never lowers what an earlier, larger one needs.
-bool prepare_sweep_small(size_t smem) {
+// context on the device: it is set to the most the device allows beside the
+// kernel's static shared memory, so that a context with a smaller system
+// never lowers what an earlier, larger one needs.
+template <bool CAV>
+static bool allow_sweep_small(size_t smem) {
   int dev = 0, optin = 0;
-  if (smem == 0 || cudaGetDevice(&dev) != cudaSuccess ||
+  cudaFuncAttributes fa{};
+  if (cudaGetDevice(&dev) != cudaSuccess ||
       cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev) != cudaSuccess ||
-      smem > (size_t)optin)
+      cudaFuncGetAttributes(&fa, k_sweep_small<CAV>) != cudaSuccess)
     return false;
-  return cudaFuncSetAttribute(k_sweep_small<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, optin) ==
-             cudaSuccess &&
-         cudaFuncSetAttribute(k_sweep_small<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, optin) == cudaSuccess;
+  const int most = optin - (int)fa.sharedSizeBytes;
+  return smem <= (size_t)most &&
+         cudaFuncSetAttribute(k_sweep_small<CAV>, cudaFuncAttributeMaxDynamicSharedMemorySize, most) == cudaSuccess;
+}
+
+bool prepare_sweep_small(size_t smem) {
+  if (smem == 0) return false;
+  const bool ok = allow_sweep_small<false>(smem) && allow_sweep_small<true>(smem);
+  if (!ok) cudaGetLastError();
+  return ok;
 }
 
 void launch_sweep_small(const SysPtrs &p, int n_sweeps, bool npt, bool cavity, double margin, size_t smem,

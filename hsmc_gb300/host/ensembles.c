@@ -69,94 +69,56 @@ static void run_block(host_run *r, bool prod, int offset, bool npt) {
   host_sweeps(r, pending, npt);
 }
 
-/* get_sample_nvt / get_sample_npt (src/optimizer.c:66-78, 150-166). */
-static void sample_acceptance(host_run *r, int sweeps, bool npt, double *acc_part, double *acc_vol) {
-  host_reset_counters(r);
-  host_sweeps(r, sweeps, npt);
-  *acc_part = (double)r->counters[HSMC_CNT_ACCEPTED] / ((double)r->counters[HSMC_CNT_MOVES]);
-  if (acc_vol) *acc_vol = (double)r->counters[HSMC_CNT_VOL_ACCEPTED] / ((double)r->counters[HSMC_CNT_VOL_MOVES]);
-}
-
 /* opt_nvt (src/optimizer.c:23-64): secant search of dr_max; opt_cavity_nvt
  * (src/optimizer.c:172-212) is the same search over cavity sweeps, printed
- * with a space before the newline of its acceptance line. */
+ * with a space before the newline of its acceptance line.  The sampling loop
+ * and the secant steps run on the device in one call (hsmc_gpu_optimize),
+ * with the reference's arithmetic. */
 static void opt_nvt_as(host_run *r, bool cavity) {
   host_input *in = &r->in;
-  int per = in->opt_sweeps / in->opt_samples;
-  double a1, a2, d1, d2;
   printf("---------------------------------------------------\n");
   printf("Maximum displacement optimization started ...\n");
   printf("Sweeps for optimization: %d\n", in->opt_sweeps);
   printf("Number of samples: %d\n", in->opt_samples);
-  sample_acceptance(r, per, false, &a1, NULL);
-  d1 = in->dr_max;
-  if (a1 > in->opt_part_target) in->dr_max *= 2;
-  else in->dr_max /= 2;
-  sample_acceptance(r, per, false, &a2, NULL);
-  d2 = in->dr_max;
-  for (int k = 0; k < in->opt_samples; k++) {
-    in->dr_max = d2 - (a2 - in->opt_part_target) * (d2 - d1) / (a2 - a1);
-    if (in->dr_max > 1.0) {
-      in->dr_max = 1.0;
-    } else if (in->dr_max <= 0.0) {
-      in->dr_max = -in->dr_max;
-      if (in->dr_max > 1.0) in->dr_max = d2 / 2;
-    }
-    d1 = d2;
-    a1 = a2;
-    sample_acceptance(r, per, false, &a2, NULL);
-    d2 = in->dr_max;
-  }
+  double out[4];
+  host_gpu_check(hsmc_gpu_set_step(r->gpu, in->dr_max, in->dv_max), "set_step");
+  host_gpu_check(hsmc_gpu_optimize(r->gpu, in->opt_sweeps, in->opt_samples, in->opt_part_target,
+                                   in->opt_vol_target, out),
+                 "hsmc_gpu_optimize");
+  in->dr_max = out[0];
   printf("Optimal maximum displacement: %.8f\n", in->dr_max);
-  printf(cavity ? "Acceptance ratio: %.8f \n" : "Acceptance ratio: %.8f\n", a2);
+  printf(cavity ? "Acceptance ratio: %.8f \n" : "Acceptance ratio: %.8f\n", out[1]);
   printf("Maximum displacement optimization completed\n");
 }
 
 static void opt_nvt(host_run *r) { opt_nvt_as(r, false); }
 
-/* opt_npt (src/optimizer.c:83-148): secant search of dr_max and dv_max. */
+/* opt_npt (src/optimizer.c:83-148): secant search of dr_max and dv_max, on
+ * the device in one call as above. */
 static void opt_npt(host_run *r) {
   host_input *in = &r->in;
-  int per = in->opt_sweeps / in->opt_samples;
-  double ap1, ap2, av1, av2, d1, d2, v1, v2;
   printf("---------------------------------------------------\n");
   printf("Maximum displacement optimization started ...\n");
   printf("Sweeps for optimization: %d\n", in->opt_sweeps);
   printf("Number of samples: %d\n", in->opt_samples);
-  sample_acceptance(r, per, true, &ap1, &av1);
-  d1 = in->dr_max;
-  v1 = in->dv_max;
-  if (ap1 > in->opt_part_target) in->dr_max *= 2;
-  else in->dr_max /= 2;
-  if (av1 > in->opt_vol_target) in->dv_max *= 2;
-  else in->dv_max /= 2;
-  sample_acceptance(r, per, true, &ap2, &av2);
-  d2 = in->dr_max;
-  v2 = in->dv_max;
-  for (int k = 0; k < in->opt_samples; k++) {
-    in->dr_max = d2 - (ap2 - in->opt_part_target) * (d2 - d1) / (ap2 - ap1);
-    in->dv_max = v2 - (av2 - in->opt_vol_target) * (v2 - v1) / (av2 - av1);
-    if (in->dr_max > 1.0) in->dr_max = 1.0;
-    if (in->dr_max <= 0.0) {
-      in->dr_max = -in->dr_max;
-      if (in->dr_max > 1.0) in->dr_max = d2 / 2;
-    }
-    if (in->dv_max <= 0.0) {
-      in->dv_max = -in->dv_max;
-      if (in->dv_max > 0.1) in->dv_max = v2 / 2;
-    }
-    d1 = d2;
-    v1 = v2;
-    ap1 = ap2;
-    av1 = av2;
-    sample_acceptance(r, per, true, &ap2, &av2);
-    d2 = in->dr_max;
-    v2 = in->dv_max;
-  }
+  double out[4];
+  host_gpu_check(hsmc_gpu_set_step(r->gpu, in->dr_max, in->dv_max), "set_step");
+  host_gpu_check(hsmc_gpu_optimize(r->gpu, in->opt_sweeps, in->opt_samples, in->opt_part_target,
+                                   in->opt_vol_target, out),
+                 "hsmc_gpu_optimize");
+  in->dr_max = out[0];
+  in->dv_max = out[2];
+  double b[5];
+  host_gpu_check(hsmc_gpu_get_box(r->gpu, b), "get_box");
+  r->in.rho = b[4];
+  r->box.lx = b[0];
+  r->box.ly = b[1];
+  r->box.lz = b[2];
+  r->box.vol = b[3];
   printf("Optimal maximum particle displacement: %.8f\n", in->dr_max);
-  printf("Acceptance ratio: %.8f \n", ap2);
+  printf("Acceptance ratio: %.8f \n", out[1]);
   printf("Optimal maximum volume deformation: %.8f\n", in->dv_max);
-  printf("Acceptance ratio: %.8f \n", av2);
+  printf("Acceptance ratio: %.8f \n", out[3]);
   printf("Maximum displacement optimization completed\n");
 }
 

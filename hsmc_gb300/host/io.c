@@ -4,7 +4,8 @@
  * restart_%0Nd.bin keeps the reference's block order and raw layouts
  * (src/io_config.c:28-130): dr_max, dv_max, the box record, the particle
  * record, the N x 4 configuration; the last block holds this engine's
- * random-stream position (4 x uint64: seed, sweeps done, Widom calls done, 0)
+ * random-stream position (4 x uint64: seed, index of the next sweep, Widom
+ * calls, cluster moves)
  * where the reference stores its GSL generator state.  config_%06d.dat.gz is
  * written byte-compatibly from a device download (src/io_config.c:134-191).
  */

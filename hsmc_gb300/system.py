@@ -335,6 +335,16 @@ class HardSphereSystem:
         st = np.ascontiguousarray(st, dtype=np.uint64)
         _check(self._lib.hsmc_gpu_rng_set_state(self._h, st.ctypes.data), "hsmc_gpu_rng_set_state")
 
+    def optimize(self, opt_sweeps: int, opt_samples: int, part_target: float = 0.4, vol_target: float = 0.5):
+        """The reference's optimiser (opt_nvt / opt_npt, src/optimizer.c:23-148)
+        in one device call; returns (dr_max, last acceptance, dv_max, last
+        volume acceptance) and keeps the new steps."""
+        out = np.zeros(4, dtype=np.float64)
+        _check(self._lib.hsmc_gpu_optimize(self._h, opt_sweeps, opt_samples, part_target, vol_target,
+                                           out.ctypes.data), "hsmc_gpu_optimize")
+        self.dr_max, self.dv_max = float(out[0]), float(out[2])
+        return float(out[0]), float(out[1]), float(out[2]), float(out[3])
+
     def autotune(self, sweeps_per_variant: int = 5) -> int:
         lanes = C.c_int()
         _check(self._lib.hsmc_gpu_autotune(self._h, sweeps_per_variant, C.byref(lanes)), "hsmc_gpu_autotune")

@@ -96,6 +96,20 @@ int hsmc_gpu_download_config(hsmc_ctx *ctx, double (*conf)[4], int n);
  * written by the optimiser, src/optimizer.c:23-166). */
 int hsmc_gpu_set_step(hsmc_ctx *ctx, double dr_max, double dv_max);
 
+/* The reference's optimiser in one call (opt_nvt src/optimizer.c:23-64,
+ * opt_npt :83-148 for an NpT context, opt_cavity_nvt :172-212 for a cavity
+ * run): opt_samples + 2 samples of opt_sweeps / opt_samples sweeps each, the
+ * step after the first sample doubled or halved toward part_target (and
+ * vol_target for the volume step), then secant steps with the reference's
+ * clamps.  The samples run back to back on the device, which sets the step
+ * for each next sample itself; the host waits once.  The steps and
+ * acceptances are the reference's double arithmetic on the same counters,
+ * so the result is the host-side loop's bit for bit.
+ * out (may be NULL): {dr_max, last particle acceptance, dv_max, last volume
+ * acceptance (0 for NVT)}; the context keeps the new steps. */
+int hsmc_gpu_optimize(hsmc_ctx *ctx, int opt_sweeps, int opt_samples, double part_target, double vol_target,
+                      double out[4]);
+
 /* Counter order used by the sweep calls: the six move counters of
  * get_moves_counters (src/moves.c:231-241), 64-bit, for this call only. */
 enum {

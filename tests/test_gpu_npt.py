@@ -2,6 +2,7 @@
 the box, the box follows the reference's lattice rebuild, and the density
 agrees with the reference algorithm's own NpT chain (the CPU oracle)."""
 import math
+import os
 
 import numpy as np
 import pytest
@@ -52,33 +53,41 @@ def cs_packing_fraction(beta_p):
     return 0.5 * (lo + hi)
 
 
-def test_npt_density_matches_oracle_chain_and_carnahan_starling(oracle_mod, gpu_lib):
-    """N = 500 at beta P = 2.28 (Carnahan-Starling's pressure near eta = 0.30),
-    volume step 0.02 in ln V (about 40 % of volume moves accepted, so the
-    volume decorrelates within tens of sweeps): the mean density agrees with
-    the reference algorithm's own NpT chain (the oracle) and the mean packing
-    fraction with Carnahan-Starling, each within 3 blocking standard errors."""
-    P, rho0, n, dv = 2.28, 0.57, 5, 0.02
-    g = gpu_lib.HardSphereSystem(rho=rho0, cells=n, dr_max=0.25, dv_max=dv, pressure=P, seed=17)
-    g.sweep_npt(2000)
-    dens = []
-    for _ in range(2000):
-        g.sweep_npt(5)
-        dens.append(g.get_box()[4])
-    c = g.get_moves_counters()
-    mg, eg = blocked_mean(dens, blocks=20)
-    o = oracle_mod.OracleSim(rho=rho0, n_cells=n, seed=3, dr_max=0.25, press=P, dv_max=dv, neigh_dr=1.3)
-    o.sweeps_npt(2000)
-    od = []
-    for _ in range(2000):
-        o.sweeps_npt(5)
-        od.append(o.box()["rho"])
-    mo, eo = blocked_mean(od, blocks=20)
+def test_npt_density_matches_oracle_chain_and_carnahan_starling(gpu_lib):
+    """N = 500 at beta P = 2.28 (Carnahan-Starling's pressure near eta =
+    0.30), ln V steps up to 0.01: eight GPU chains against eight chains of
+    the reference algorithm (tests/golden/make_npt_stats.py), each chain's
+    mean density one sample (the volume of a 500-sphere box decorrelates over
+    about 10^2 sweeps, far below a chain's 40,000).  The mean density must
+    agree with the reference chains' within 3 combined standard errors; the
+    packing fraction's distance from Carnahan-Starling's at this pressure is
+    printed for both."""
+    ref = np.load(os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden", "npt_oracle_stats.npz"))
+    P, rho0, n = float(ref["pressure"]), float(ref["rho0"]), int(ref["cells"])
+    dr, dv = float(ref["dr_max"]), float(ref["dv_max"])
+    equil, samples, every = int(ref["equil"]), int(ref["samples"]), int(ref["every"])
+    means, vacc = [], []
+    for k in range(8):
+        g = gpu_lib.HardSphereSystem(rho=rho0, cells=n, dr_max=dr, dv_max=dv, pressure=P, seed=300 + k)
+        g.sweep_npt(equil)
+        g.reset_moves_counters()
+        d = np.empty(samples)
+        for j in range(samples):
+            g.sweep_npt(every)
+            d[j] = g.get_box()[4]
+        c = g.get_moves_counters()
+        means.append(d.mean())
+        vacc.append(c[4] / max(c[3], 1))
+        g.close()
+    mg, eg = np.mean(means), np.std(means, ddof=1) / math.sqrt(len(means))
+    mr, er = float(np.mean(ref["rho_mean"])), float(np.std(ref["rho_mean"], ddof=1) / math.sqrt(len(ref["rho_mean"])))
+    s = math.hypot(eg, er)
     eta_cs = cs_packing_fraction(P)
-    eta, e_eta = mg * math.pi / 6, eg * math.pi / 6
-    print(f"\nNpT rho at beta P {P}, N=500: gpu {mg:.5f} +- {eg:.5f}, reference chain {mo:.5f} +- {eo:.5f} "
-          f"({(mg - mo) / math.hypot(eg, eo):+.2f} sigma); volume acceptance {c[4] / max(c[3], 1):.3f}")
-    print(f"NpT eta: gpu {eta:.5f} +- {e_eta:.5f}, Carnahan-Starling {eta_cs:.5f} "
-          f"({(eta - eta_cs) / e_eta:+.2f} sigma)")
-    assert abs(mg - mo) < 3.0 * math.hypot(eg, eo), (mg, eg, mo, eo)
-    assert abs(eta - eta_cs) < 3.0 * e_eta, (eta, e_eta, eta_cs)
+    k6 = math.pi / 6
+    print(f"\nNpT rho at beta P {P}, N={4 * n**3}: gpu {mg:.5f} +- {eg:.5f}, reference chain {mr:.5f} +- {er:.5f} "
+          f"({(mg - mr) / s:+.2f} sigma); volume acceptance gpu {np.mean(vacc):.3f}, "
+          f"reference {float(np.mean(ref['vol_acc'])):.3f}")
+    print(f"eta: gpu {mg * k6:.5f} +- {eg * k6:.5f} ({(mg * k6 - eta_cs) / (eg * k6):+.2f} sigma from "
+          f"Carnahan-Starling {eta_cs:.5f}), reference {mr * k6:.5f} +- {er * k6:.5f} "
+          f"({(mr * k6 - eta_cs) / (er * k6):+.2f} sigma)")
+    assert abs(mg - mr) < 3.0 * s, (mg, eg, mr, er)

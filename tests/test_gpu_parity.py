@@ -358,3 +358,69 @@ def test_contexts_of_different_sizes_coexist(gpu_lib):
     assert len(big.cluster_moves(2)) == 2
     small.close()
     big.close()
+
+
+def _host_optimizer(g, opt_sweeps, opt_samples, target, npt=False, vtarget=0.5):
+    """opt_nvt / opt_npt (src/optimizer.c:23-148) restated on the host over
+    single sweep calls, the arithmetic in Python floats (IEEE double)."""
+    per = opt_sweeps // opt_samples
+
+    def sample():
+        c = (g.sweep_npt(per) if npt else g.sweep_nvt(per)).astype(np.float64)
+        return c[1] / c[0], (c[4] / c[3] if npt else 0.0)
+
+    a1, b1 = sample()
+    d1, v1 = g.dr_max, g.dv_max
+    g.set_step(d1 * 2 if a1 > target else d1 / 2, (v1 * 2 if b1 > vtarget else v1 / 2) if npt else v1)
+    a2, b2 = sample()
+    d2, v2 = g.dr_max, g.dv_max
+    for _ in range(opt_samples):
+        dr = d2 - (a2 - target) * (d2 - d1) / (a2 - a1)
+        dv = v2 - (b2 - vtarget) * (v2 - v1) / (b2 - b1) if npt else v2
+        if npt:
+            if dr > 1.0:
+                dr = 1.0
+            if dr <= 0.0:
+                dr = -dr
+                if dr > 1.0:
+                    dr = d2 / 2
+            if dv <= 0.0:
+                dv = -dv
+                if dv > 0.1:
+                    dv = v2 / 2
+        elif dr > 1.0:
+            dr = 1.0
+        elif dr <= 0.0:
+            dr = -dr
+            if dr > 1.0:
+                dr = d2 / 2
+        g.set_step(dr, dv)
+        d1, a1, v1, b1 = d2, a2, v2, b2
+        a2, b2 = sample()
+        d2, v2 = g.dr_max, g.dv_max
+    return d2, a2, v2, b2
+
+
+@pytest.mark.parametrize("rho,cells,dr,P,dv,seed", [
+    (0.5, 5, 0.1, 0.0, 0.0, 61),      # N = 500: the one-block schedule
+    (0.85, 10, 0.05, 0.0, 0.0, 62),   # N = 4000: graphs of eight launches per sweep
+    (0.6, 5, 0.2, 5.0, 0.004, 63),    # NpT: particle and volume steps
+])
+def test_device_optimizer_is_the_host_loop(gpu_lib, rho, cells, dr, P, dv, seed):
+    """hsmc_gpu_optimize (every sample and secant step on the device, one
+    host wait) gives the host-side loop's steps, acceptances and chain bit
+    for bit."""
+    runs = []
+    for device in (True, False):
+        g = gpu_lib.HardSphereSystem(rho=rho, cells=cells, dr_max=dr, dv_max=dv or 0.001, pressure=P, seed=seed)
+        if device:
+            res = g.optimize(200, 10, 0.4, 0.5)
+        else:
+            res = _host_optimizer(g, 200, 10, 0.4, npt=P > 0, vtarget=0.5)
+        runs.append((np.array(res), g.download(), np.array(g.get_box())))
+        g.close()
+    (r_dev, c_dev, b_dev), (r_host, c_host, b_host) = runs
+    assert np.array_equal(r_dev, r_host), (r_dev, r_host)
+    assert np.array_equal(c_dev, c_host)
+    assert np.array_equal(b_dev, b_host)
+    assert r_dev[0] != dr  # the step moved
