@@ -26,6 +26,7 @@ namespace {
 
 constexpr int kGraphSweeps = 8;
 constexpr int kDefaultLanes = 2;  // lanes per active cell in a move pass
+constexpr int kFastBins = 2048;   // pair counts with bin thresholds (observables.cu FAST_BINS)
 
 struct Scratch {
   void *ptr = nullptr;
@@ -69,6 +70,11 @@ struct hsmc_ctx {
   double last_total_ms = 0.0, last_move_ms = 0.0;
   int last_move_launches = 0;
   Scratch hist, qbuf, flags, qpos, qids, trace;
+  // bin thresholds of the last pair-count call (hsmc_pair_thresholds)
+  Scratch thr;
+  std::vector<double> thr_host;
+  double thr_dr = 0.0, thr_rmax = 0.0;
+  int thr_nbins = 0;
   // dataflow schedule: one cooperative launch per sweep, progress words per
   // 2x2x2 region; `flow_graph` records whether such launches capture
   bool flow = false;
@@ -374,6 +380,7 @@ void hsmc_gpu_destroy(hsmc_ctx *ctx) {
   ctx->qpos.release();
   ctx->qids.release();
   ctx->trace.release();
+  ctx->thr.release();
   ctx->cl_queue.release();
   ctx->cl_mark.release();
   ctx->cl_ctr.release();
@@ -861,6 +868,47 @@ int hsmc_gpu_grid_info(hsmc_ctx *ctx, int nc[3], float len32[3], float inv_w32[3
   return HSMC_OK;
 }
 
+// --------------------------------------------------- pair-count bins
+// The bin of a pair at squared distance r2 is (int)((sqrt(r2) - 1) / dr)
+// (rdf_hist_compute, src/compute_rdf.c:110-128; pressv_compute_hist,
+// src/compute_press.c:123-165): correctly rounded operations, each
+// monotone, so the bin is a step function of r2 and its steps fall at
+// doubles that can be found once, by bisection over the bit patterns of
+// positive doubles (which order as the doubles do).  The device then bins a
+// pair by comparing r2 with them: the same bin for every double r2.
+static double first_double_where(double lo, double hi, bool (*pred)(double, const double *), const double *arg) {
+  uint64_t a, b;
+  std::memcpy(&a, &lo, 8);
+  std::memcpy(&b, &hi, 8);
+  if (pred(lo, arg)) return lo;
+  while (b - a > 1) {
+    const uint64_t m = a + (b - a) / 2;
+    double x;
+    std::memcpy(&x, &m, 8);
+    if (pred(x, arg)) b = m;
+    else a = m;
+  }
+  double x;
+  std::memcpy(&x, &b, 8);
+  return x;
+}
+
+static bool bin_at_least(double r2, const double *a) { return (std::sqrt(r2) - 1.0) / a[0] >= a[1]; }
+static bool root_at_least(double r2, const double *a) { return std::sqrt(r2) >= a[0]; }
+
+extern "C" int hsmc_pair_thresholds(double dr, double rmax, int nbins, double *thr) {
+  if (!thr || nbins <= 0 || !(dr > 0) || !(rmax > 1.0)) return HSMC_ERR_INVALID_ARG;
+  const double hi = (rmax + dr + 1.0) * (rmax + dr + 1.0);  // above every threshold
+  thr[0] = 1.0;
+  for (int k = 1; k <= nbins; k++) {
+    const double arg[2] = {dr, (double)k};
+    thr[k] = first_double_where(1.0, hi, bin_at_least, arg);
+  }
+  const double arg[1] = {rmax};
+  thr[nbins + 1] = first_double_where(1.0, hi, root_at_least, arg);
+  return HSMC_OK;
+}
+
 static int pair_counts(hsmc_ctx *ctx, double dr, double rmax, int nbins, uint64_t *counts) {
   if (!ctx || !counts || nbins <= 0 || !(dr > 0) || !(rmax > 1.0) || !ctx->uploaded) return HSMC_ERR_INVALID_ARG;
   HSMC_CUDA(ctx->hist.ensure(sizeof(unsigned long long) * (size_t)nbins));
@@ -869,8 +917,24 @@ static int pair_counts(hsmc_ctx *ctx, double dr, double rmax, int nbins, uint64_
   HSMC_CUDA(cudaMemsetAsync(&ctx->sp.st->status, 0, sizeof(int), ctx->stream));
   int k[3];
   stencil_for(ctx->hbox, rmax, k);
+  // the bin thresholds, kept on the device while dr, rmax and nbins stay
+  const double *thr = nullptr;
+  if (nbins <= kFastBins) {
+    if (ctx->thr_dr != dr || ctx->thr_rmax != rmax || ctx->thr_nbins != nbins) {
+      ctx->thr_host.resize((size_t)nbins + 2);
+      int e = hsmc_pair_thresholds(dr, rmax, nbins, ctx->thr_host.data());
+      if (e) return e;
+      HSMC_CUDA(ctx->thr.ensure(sizeof(double) * ctx->thr_host.size()));
+      HSMC_CUDA(cudaMemcpy(ctx->thr.ptr, ctx->thr_host.data(), sizeof(double) * ctx->thr_host.size(),
+                           cudaMemcpyHostToDevice));
+      ctx->thr_dr = dr;
+      ctx->thr_rmax = rmax;
+      ctx->thr_nbins = nbins;
+    }
+    thr = (const double *)ctx->thr.ptr;
+  }
   timing_begin(ctx);
-  launch_pair_hist(ctx->sp, dr, rmax, nbins, d, k, ctx->stream);
+  launch_pair_hist(ctx->sp, dr, rmax, nbins, d, k, ctx->stream, thr);
   timing_end(ctx);
   int e = check_kernels(ctx);
   if (e) return e;

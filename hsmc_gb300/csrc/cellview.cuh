@@ -16,6 +16,7 @@ struct CellView {
   int cap;
   int nc[3];
   float sh[3], L32[3], iw[3];
+  float band;  // the move pass's guard band on r^2 (the box's)
 };
 
 __device__ __forceinline__ CellView current_view(const SysPtrs &p) {
@@ -32,6 +33,7 @@ __device__ __forceinline__ CellView current_view(const SysPtrs &p) {
     v.L32[d] = bx->len32[d];
     v.iw[d] = bx->inv_w32[d];
   }
+  v.band = bx->band;
   return v;
 }
 
@@ -93,17 +95,26 @@ __device__ __forceinline__ float approx_r2(float ax, float ay, float az, const S
 
 // widom_rand_pos (src/compute_widom_chem_pot.c:73-80): x = u * L with u the
 // reference's closed uniform; widom_compute_dist (:130-160): insertion minus
-// particle, one minimum-image branch, overlap when r < 1.
+// particle, one minimum-image branch, overlap when r < 1.  The
+// single-precision r^2 decides outside the guard band of contact (its error
+// is below the band, as in the move pass's screen: the minimum-image shift
+// here is an exact subtraction of the box side); inside it the reference's
+// FP64 distance decides.
 __device__ __forceinline__ bool point_overlaps(const CellView &v, const SysPtrs &p, const Stencil &s, double x,
                                                double y, double z, int skip, const double *len,
                                                const double *half) {
   float x32, y32, z32;  // grid coordinates, as the slots hold them
   grid_coords(v, x, y, z, x32, y32, z32);
+  const float lo = 1.0f - v.band, hi = 1.0f + v.band;
   bool ov = false;
   for_each_near(v, s, x, y, z, [&](const Slot &o) {
     if (ov || o.id == skip) return;
     const float r2 = approx_r2(x32, y32, z32, o, v.L32);
-    if (r2 > 1.01f) return;
+    if (r2 < lo) {
+      ov = true;
+      return;
+    }
+    if (r2 > hi) return;
     double ox, oy, oz;
     load_xyz(p.pos, o.id, ox, oy, oz);
     if (ref_r2(x, y, z, ox, oy, oz, len, half) < 1.0) ov = true;

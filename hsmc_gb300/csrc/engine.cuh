@@ -194,7 +194,7 @@ void launch_cavity_psi(const SysPtrs &p, const double *x, int n, double *out, cu
 
 // observables.cu
 void launch_pair_hist(const SysPtrs &p, double bin, double rmax, int nbins, unsigned long long *counts,
-                      int stencil[3], cudaStream_t s);
+                      int stencil[3], cudaStream_t s, const double *thr = nullptr);
 void launch_scaled_scan(const SysPtrs &p, const double *sf, int n_sf, int stencil[3], cudaStream_t s);
 void launch_widom(const SysPtrs &p, long long n, unsigned long long seq, const double *pos_in, uint8_t *ov_out,
                   cudaStream_t s);

@@ -89,12 +89,135 @@ __global__ void __launch_bounds__(256) k_pair_hist(SysPtrs p1, const SysPtrs *re
       if (sh[b]) atomicAdd(counts + b, (unsigned long long)sh[b]);
 }
 
+// The same counts with the reference's bin formula evaluated only where it
+// is needed.  thr[k] (k = 1..nbins) is the smallest double r2 whose bin
+// (int)((sqrt(r2) - 1) / dr) reaches k, thr[nbins + 1] the smallest whose
+// root reaches rmax (thr[0] = 1), found on the host with the same correctly
+// rounded operations (pair_thresholds, api.cu), so that for every double
+// r2 in [1, thr[nbins]) the bin is the number of thresholds at or below it.
+// A pair's single-precision r2 (grid coordinates, the cell's periodic
+// image) is within band (1 + r2) of the reference's FP64 r2 (the move
+// pass's guard band, scaled for distances up to rmax), so a pair whose
+// single-precision r2 is farther than that from every threshold is binned
+// without FP64 work; the others take the reference's FP64 distance.  Each
+// unordered pair is visited once (half stencil; in the own cell j > i) and
+// counts 2, as the reference's +2.0 per pair: the FP64 distance of (i, j)
+// and (j, i) is the same number.  Needs a stencil narrower than the grid.
+constexpr int FAST_BINS = 2048;
+
+__device__ __forceinline__ int exact_bin(double r2, const double *thr, int nbins, double bin, double rmax, int guess,
+                                         bool &bad) {
+  if (r2 < 1.0 || !(r2 < thr[nbins])) {  // overlapping or beyond the last bin: the reference's formula
+    const double r = __dsqrt_rn(r2);
+    if (!(r < rmax)) return -1;
+    const int b = (int)__ddiv_rn(__dsub_rn(r, 1.0), bin);
+    if (b < 0 || b >= nbins) {
+      bad = true;
+      return -1;
+    }
+    return b;
+  }
+  // thr[0] = 1 <= r2 < thr[nbins]: the largest k with thr[k] <= r2 (positive
+  // doubles order as their bit patterns)
+  const long long x = __double_as_longlong(r2);
+  int k = guess < 0 ? 0 : (guess >= nbins ? nbins - 1 : guess);
+  while (k > 0 && __double_as_longlong(__ldg(thr + k)) > x) k--;
+  while (k + 1 < nbins && __double_as_longlong(__ldg(thr + k + 1)) <= x) k++;
+  return k;
+}
+
+__global__ void __launch_bounds__(256) k_pair_hist_fast(SysPtrs p, Stencil s, double bin, double rmax, int nbins,
+                                                        unsigned long long *counts, float cut2, const double *thr) {
+  __shared__ unsigned int sh[FAST_BINS];
+  __shared__ float thr_f[FAST_BINS + 2];
+  for (int b = threadIdx.x; b < nbins; b += blockDim.x) sh[b] = 0;
+  for (int k = threadIdx.x; k < nbins + 2; k += blockDim.x) thr_f[k] = (float)__ldg(thr + k);
+  __syncthreads();
+  const CellView v = current_view(p);
+  const Box *bx = p.box;
+  const double len[3] = {bx->len[0], bx->len[1], bx->len[2]};
+  const double half[3] = {bx->half[0], bx->half[1], bx->half[2]};
+  const float band = bx->band;
+  const float inv_bin = (float)(1.0 / bin);
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  bool bad = false;
+  if (i < p.n) {
+    double x, y, z;
+    load_xyz(p.pos, i, x, y, z);
+    int ci[3];
+    float t[3];
+    axis_cell(__double2float_rn(x), v.sh[0], v.L32[0], v.iw[0], v.nc[0], ci[0], t[0]);
+    axis_cell(__double2float_rn(y), v.sh[1], v.L32[1], v.iw[1], v.nc[1], ci[1], t[1]);
+    axis_cell(__double2float_rn(z), v.sh[2], v.L32[2], v.iw[2], v.nc[2], ci[2], t[2]);
+    for (int a = 0; a <= s.k[2]; a++) {
+      int cz = ci[2] + a;
+      const float imz = cz >= v.nc[2] ? v.L32[2] : 0.f;
+      cz -= cz >= v.nc[2] ? v.nc[2] : 0;
+      for (int b = (a == 0 ? 0 : -s.k[1]); b <= s.k[1]; b++) {
+        int cy = ci[1] + b;
+        const float imy = cy < 0 ? -v.L32[1] : (cy >= v.nc[1] ? v.L32[1] : 0.f);
+        cy += cy < 0 ? v.nc[1] : (cy >= v.nc[1] ? -v.nc[1] : 0);
+        for (int e = ((a == 0 && b == 0) ? 0 : -s.k[0]); e <= s.k[0]; e++) {
+          int cx = ci[0] + e;
+          const float imx = cx < 0 ? -v.L32[0] : (cx >= v.nc[0] ? v.L32[0] : 0.f);
+          cx += cx < 0 ? v.nc[0] : (cx >= v.nc[0] ? -v.nc[0] : 0);
+          const bool own = a == 0 && b == 0 && e == 0;
+          const int c = cx + v.nc[0] * (cy + v.nc[1] * cz);
+          const int m = v.cnt[c];
+          const int n = m < v.cap ? m : v.cap;  // an overfull cell was flagged by the build
+          const Slot *sl = v.slot + (size_t)c * v.cap;
+          for (int q = 0; q < n; q++) {
+            const Slot o = sl[q];
+            if (own && o.id <= i) continue;
+            const float4 ent = imaged_entry(o, imx, imy, imz);
+            const float r2f = dist2(t[0], t[1], t[2], ent);
+            if (r2f > cut2) continue;
+            // single precision where it decides: the bin whose thresholds lie
+            // farther than the error bound on both sides
+            const float err = band * (1.0f + r2f) + 2.4e-7f * (1.0f + r2f);
+            int k = (int)((sqrtf(r2f) - 1.0f) * inv_bin);
+            k = k < 0 ? 0 : (k > nbins - 1 ? nbins - 1 : k);
+            while (k > 0 && thr_f[k] > r2f) k--;
+            while (k + 1 < nbins && thr_f[k + 1] <= r2f) k++;
+            int bn;
+            if (r2f - err > thr_f[nbins + 1]) {
+              continue;  // beyond rmax
+            } else if (r2f - err > thr_f[k] && r2f + err < thr_f[k + 1] && k + 1 <= nbins) {
+              bn = k;
+            } else {
+              double ox, oy, oz;
+              load_xyz(p.pos, o.id, ox, oy, oz);
+              bn = exact_bin(ref_r2(x, y, z, ox, oy, oz, len, half), thr, nbins, bin, rmax, k, bad);
+              if (bn < 0) continue;
+            }
+            // warp aggregation: one shared-memory atomic per distinct bin
+            cg::coalesced_group active = cg::coalesced_threads();
+            cg::coalesced_group same = cg::labeled_partition(active, bn);
+            if (same.thread_rank() == 0) atomicAdd(&sh[bn], 2u * same.size());
+          }
+        }
+      }
+    }
+  }
+  if (bad) atomicOr(&p.st->status, ST_BAD_BIN);
+  __syncthreads();
+  for (int b = threadIdx.x; b < nbins; b += blockDim.x)
+    if (sh[b]) atomicAdd(counts + b, (unsigned long long)sh[b]);
+}
+
+// thr: the r2 thresholds of the bins (nbins + 2 doubles, see above) or
+// nullptr for the exact per-pair FP64 kernel, which also serves more bins
+// than FAST_BINS and grids too small for a half stencil.
 void launch_pair_hist(const SysPtrs &p, double bin, double rmax, int nbins, unsigned long long *counts,
-                      int stencil[3], cudaStream_t st) {
+                      int stencil[3], cudaStream_t st, const double *thr) {
   Stencil s{{stencil[0], stencil[1], stencil[2]}};
   const float cut = (float)rmax + 1e-3f;
   const int blocks = (p.n + 255) / 256;
-  k_pair_hist<false><<<blocks > 0 ? blocks : 1, 256, 0, st>>>(p, nullptr, s, bin, rmax, nbins, counts, cut * cut);
+  const bool fast = thr && nbins <= FAST_BINS && stencil[0] >= 0 && stencil[1] >= 0 && stencil[2] >= 0;
+  if (fast)
+    k_pair_hist_fast<<<blocks > 0 ? blocks : 1, 256, 0, st>>>(p, s, bin, rmax, nbins, counts, cut * cut, thr);
+  else
+    k_pair_hist<false><<<blocks > 0 ? blocks : 1, 256, 0, st>>>(p, nullptr, s, bin, rmax, nbins, counts, cut * cut);
 }
 
 void launch_pair_hist_batch(const SysPtrs *reps, int n_reps, int max_n, double bin, double rmax, int nbins,
@@ -107,6 +230,7 @@ void launch_pair_hist_batch(const SysPtrs *reps, int n_reps, int max_n, double b
 // ------------------------------------------------------- scaled overlap
 constexpr int MAX_SF = 256;
 __constant__ double c_sf[MAX_SF];
+__constant__ float c_sf2f[MAX_SF];  // (float)(sf * sf)
 
 __global__ void __launch_bounds__(256) k_scaled_scan(SysPtrs p, Stencil s, int n_sf, float cut2) {
   const CellView v = current_view(p);
@@ -119,14 +243,29 @@ __global__ void __launch_bounds__(256) k_scaled_scan(SysPtrs p, Stencil s, int n
     load_xyz(p.pos, i, x, y, z);
     float x32, y32, z32;  // grid coordinates, as the slots hold them
     grid_coords(v, x, y, z, x32, y32, z32);
+    // the scaled single-precision r^2 decides outside twice the guard band of
+    // contact (scaling by sf <= 1 shrinks the screen's error); inside it the
+    // reference's scaled FP64 distance does
+    const float lo = 1.0f - 2.0f * v.band, hi = 1.0f + 2.0f * v.band;
     for_each_near(v, s, x, y, z, [&](const Slot &o) {
       if (o.id == i) return;
-      if (approx_r2(x32, y32, z32, o, v.L32) > cut2) return;
-      double ox, oy, oz;
-      load_xyz(p.pos, o.id, ox, oy, oz);
+      const float r2f = approx_r2(x32, y32, z32, o, v.L32);
+      if (r2f > cut2) return;
+      bool loaded = false;
+      double ox = 0.0, oy = 0.0, oz = 0.0;
       for (int k = 0; k < n_sf; k++) {
         const unsigned long long bit = 1ull << (k & 63);
         if (m[k >> 6] & bit) continue;
+        const float est = r2f * c_sf2f[k];
+        if (est < lo) {
+          m[k >> 6] |= bit;
+          continue;
+        }
+        if (est > hi) continue;
+        if (!loaded) {
+          load_xyz(p.pos, o.id, ox, oy, oz);
+          loaded = true;
+        }
         if (ref_r2_scaled(x, y, z, ox, oy, oz, len, c_sf[k]) < 1.0) m[k >> 6] |= bit;
       }
     });
@@ -142,6 +281,9 @@ void launch_scaled_scan(const SysPtrs &p, const double *sf, int n_sf, int stenci
   double smallest = 1.0;
   for (int k = 0; k < n_sf; k++) smallest = sf[k] < smallest ? sf[k] : smallest;
   cudaMemcpyToSymbolAsync(c_sf, sf, sizeof(double) * (size_t)n_sf, 0, cudaMemcpyHostToDevice, st);
+  float sf2f[MAX_SF];
+  for (int k = 0; k < n_sf; k++) sf2f[k] = (float)(sf[k] * sf[k]);
+  cudaMemcpyToSymbolAsync(c_sf2f, sf2f, sizeof(float) * (size_t)n_sf, 0, cudaMemcpyHostToDevice, st);
   Stencil s{{stencil[0], stencil[1], stencil[2]}};
   const float cut = (float)(1.0 / smallest) + 1e-3f;
   const int blocks = (p.n + 255) / 256;

@@ -207,6 +207,8 @@ __global__ void __launch_bounds__(256) k_vol_scan(SysPtrs p) {
   const float sh[3] = {st->params.shift32[0], st->params.shift32[1], st->params.shift32[2]};
   const int nc[3] = {bx->nc[0], bx->nc[1], bx->nc[2]};
   const float reach = (float)(1.0 / sf) + 1e-3f;
+  const float sf2f = (float)(sf * sf);
+  const float lo = 1.0f - 2.0f * bx->band, hi = 1.0f + 2.0f * bx->band;
   double x, y, z;
   load_xyz(p.pos, i, x, y, z);
   const float xr[3] = {__double2float_rn(x), __double2float_rn(y), __double2float_rn(z)};
@@ -234,7 +236,16 @@ __global__ void __launch_bounds__(256) k_vol_scan(SysPtrs p) {
           dx -= L32[0] * rintf(dx / L32[0]);
           dy -= L32[1] * rintf(dy / L32[1]);
           dz -= L32[2] * rintf(dz / L32[2]);
-          if (dx * dx + dy * dy + dz * dz > reach * reach) continue;
+          const float r2f = dx * dx + dy * dy + dz * dz;
+          if (r2f > reach * reach) continue;
+          // the scaled single-precision r^2 decides outside twice the guard
+          // band of contact; inside it the reference's scaled FP64 distance
+          const float est = r2f * sf2f;
+          if (est < lo) {
+            ov = true;
+            continue;
+          }
+          if (est > hi) continue;
           double ox, oy, oz;
           load_xyz(p.pos, o.id, ox, oy, oz);
           if (ref_r2_scaled(x, y, z, ox, oy, oz, len, sf) < 1.0) ov = true;

@@ -154,6 +154,16 @@ int hsmc_gpu_rdf(hsmc_ctx *ctx, double dr, double rmax, int nbins, uint64_t *cou
 #define HSMC_RDF_NOALLOC_MAX_BINS 16384
 int hsmc_gpu_rdf_noalloc(hsmc_ctx *ctx, double dr, double rmax, int nbins, uint64_t *counts);
 
+/* Host helper, no device work: the squared distances at which the bin of
+ * rdf_hist_compute / pressv_compute_hist (src/compute_rdf.c:110-128,
+ * src/compute_press.c:123-165), (int)((sqrt(r2) - 1) / dr), steps up.
+ * thr[0] = 1; thr[k] (k = 1..nbins) is the smallest double r2 whose bin is
+ * at least k; thr[nbins + 1] the smallest whose root reaches rmax.  For
+ * every double r2 in [1, thr[nbins]) the bin is the largest k with
+ * thr[k] <= r2.  The pair counts use them to bin pairs exactly without the
+ * square root and division; thr holds nbins + 2 doubles. */
+int hsmc_pair_thresholds(double dr, double rmax, int nbins, double *thr);
+
 /* Virial-route contact histogram, the same counting on [1, rmax)
  * (pressv_compute_hist, src/compute_press.c:123-165). */
 int hsmc_gpu_pressv(hsmc_ctx *ctx, double dr, double rmax, int nbins, uint64_t *counts);

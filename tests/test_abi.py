@@ -68,3 +68,33 @@ def test_cavity_range_thresholds_are_exact(gpu_lib):
         assert np.array_equal(r >= c, near >= lo), c
         assert np.array_equal(r <= c, near <= hi), c
     assert lo_f(0.0) == 0.0 and hi_f(float("inf")) == float("inf")
+
+
+@pytest.mark.parametrize("dr,nbins", [(0.01, 400), (0.005, 800), (0.01, 5), (0.02, 200), (0.0123, 17)])
+def test_pair_bin_thresholds_are_the_reference_bins(gpu_lib, dr, nbins):
+    """hsmc_pair_thresholds: for every k the threshold's bin
+    (int)((sqrt(r2) - 1) / dr) reaches k and the double just below does not;
+    the rmax threshold likewise; and binning by thresholds equals the
+    reference's formula on random and boundary r2 (IEEE double here as on
+    the device)."""
+    lib = gpu_lib._native.load()
+    fn = lib.hsmc_pair_thresholds
+    fn.argtypes = [C.c_double, C.c_double, C.c_int, C.c_void_p]
+    rmax = 1.0 + dr * nbins
+    thr = np.zeros(nbins + 2)
+    assert fn(dr, rmax, nbins, thr.ctypes.data) == 0
+
+    def binf(r2):
+        return np.trunc((np.sqrt(r2) - 1.0) / dr)
+
+    assert thr[0] == 1.0 and np.all(np.diff(thr[:nbins + 1]) > 0)
+    below = np.nextafter(thr, 0.0)
+    ks = np.arange(1, nbins + 1)
+    assert np.all(binf(thr[1:nbins + 1]) >= ks) and np.all(binf(below[1:nbins + 1]) < ks)
+    assert np.sqrt(thr[nbins + 1]) >= rmax and np.sqrt(below[nbins + 1]) < rmax
+    rng = np.random.default_rng(nbins)
+    r2 = np.concatenate([rng.uniform(1.0, thr[nbins], 200000), thr[1:nbins], below[1:nbins],
+                         np.nextafter(thr[1:nbins], 10.0)])
+    r2 = r2[(r2 >= 1.0) & (r2 < thr[nbins])]
+    by_thr = np.searchsorted(thr[:nbins], r2, side="right") - 1
+    assert np.array_equal(by_thr, binf(r2).astype(int))

@@ -113,3 +113,74 @@ def test_traced_full_size_sweeps_replay_bit_exact(oracle_mod, gpu_lib, cfg, swee
     assert rechecked > 100, rechecked
     assert cnt[1] == np.sum(dec == 0)
     g.close()
+
+
+@pytest.mark.parametrize("cfg", [C2, C5], ids=["N256k_L67", "N1M_L100"])
+def test_widom_band_edge_insertions_at_large_coordinates(oracle_mod, gpu_lib, cfg):
+    """Insertion points at |r| = 1 + k 2^-52 and r^2 = 1 +- f band from a
+    particle, most near the box faces: the single-precision decisions outside
+    the band and the FP64 ones inside it equal the reference's
+    widom_compute_dist test (src/compute_widom_chem_pot.c:130-160)."""
+    o, g, conf = prepared(oracle_mod, gpu_lib, cfg, seed=31)
+    L = o.box()["lx"]
+    band = band_of(L)
+    rng = np.random.default_rng(9)
+    _, pos, kind, sf = adversarial_points(conf, L, band, rng, 20000)
+    got = g.widom_replay(pos)
+    want = o.widom_points(pos)
+    mism = np.flatnonzero(got != want)
+    assert mism.size == 0, f"{mism.size} insertion decisions differ"
+    assert 0 < want.sum() < len(want)
+    g.close()
+
+
+@pytest.mark.parametrize("cfg", [C2, C5], ids=["N256k_L67", "N1M_L100"])
+def test_scaled_scans_at_band_edges(oracle_mod, gpu_lib, cfg):
+    """The thermodynamic-pressure scan and the volume-move scan at scale
+    factors placed around the closest pair's contact: sf = (1 + d) / r_min
+    with d a few ulps or a fraction of the guard band on either side, where
+    the single-precision estimate decides alone or hands over to FP64
+    (presst_compute_hist src/compute_press.c:243-273; vol_move
+    src/moves.c:104-112)."""
+    from scipy.spatial import cKDTree
+
+    o, g, conf = prepared(oracle_mod, gpu_lib, cfg, seed=37)
+    L = o.box()["lx"]
+    band = band_of(L)
+    x = np.mod(conf[:, 1:], L)
+    dmin, _ = cKDTree(x, boxsize=L).query(x, k=2)
+    rmin = float(dmin[:, 1].min())
+    ds = [k * 2.0**-52 for k in (-3, -1, 0, 1, 3)] + [f * band for f in (-3.0, -1.5, -0.6, -0.3, 0.3, 0.6, 1.5, 3.0)]
+    sfs = np.array([(1.0 + d) / rmin for d in ds])
+    sfs = sfs[sfs < 1.0]
+    got = g.compute_presst(sfs)
+    want = o.presst_counts_sf(sfs)
+    assert np.array_equal(got.astype(np.float64), want), (sfs, got, want)
+    for sf in sfs:
+        assert g.scan_overlap(float(sf)) == o.scan_overlap(float(sf)), sf
+    g.close()
+
+
+def test_pair_counts_at_the_benchmark_box(oracle_mod, gpu_lib):
+    """g(r) on [1, 3) in bins of 0.01 and 0.005, and the virial bins, at
+    N = 256,000, rho = 0.85: the counts of the single-precision path with
+    exact bin thresholds equal an all-pairs count within r < 3 by a periodic
+    k-d tree with the reference's bin formula in FP64."""
+    from scipy.spatial import cKDTree
+
+    o, g, conf = prepared(oracle_mod, gpu_lib, C2, seed=41)
+    L = o.box()["lx"]
+    x = conf[:, 1:].copy()
+    pairs = cKDTree(np.mod(x, L), boxsize=L).query_pairs(3.0 + 1e-6, output_type="ndarray")
+    d = x[pairs[:, 0]] - x[pairs[:, 1]]
+    half = L / 2.0
+    d = np.where(d > half, d - L, np.where(d < -half, d + L, d))
+    r = np.sqrt((d[:, 0] * d[:, 0] + d[:, 1] * d[:, 1]) + d[:, 2] * d[:, 2])
+    for dr, nb in ((0.01, 200), (0.005, 400), (0.01, 5)):
+        rmax = 1.0 + dr * nb
+        rr = r[r < rmax]
+        b = np.trunc((rr - 1.0) / dr).astype(np.int64)
+        want = 2 * np.bincount(b, minlength=nb).astype(np.uint64)
+        got = g.compute_rdf_counts(dr, rmax, nb) if nb > 5 else g.compute_pressv_counts(dr, rmax, nb)
+        assert np.array_equal(got, want)
+    g.close()
