@@ -389,6 +389,17 @@ def run_replicas(args):
     n_tot = int(sum(b.n))
     dr, acc = b.tune_steps(0.1, target=TARGET_ACC)
     b.sweeps(args.equil)
+    # every schedule, timed on the same live batch (the chain is the same for
+    # all): reported beside the autotuner's choice
+    variant_ms = {}
+    for sch, cb, tile in [(0, 4, 2)] + [(1, c, t) for c in (1, 2, 4, 8) for t in (1, 2, 4, 8)]:
+        try:
+            b.set_schedule(sch, cb, tile)
+        except Exception:
+            continue
+        b.sweeps(8)
+        b.sweeps(16)
+        variant_ms["flat" if sch == 0 else f"persistent cb={cb} tile={tile}"] = b.last_timing() / 16
     schedule = b.autotune(16)  # flat launches or persistent clusters, cluster size and tile
     sweeps = args.sweeps
     per = 10
@@ -434,7 +445,7 @@ def run_replicas(args):
                                 f"{schedule[1]} blocks per cluster, tile {schedule[2]}") if schedule[0] == 1
                                else "flat launches per colour pass, CUDA graphs of 8 sweeps",
                    "acceptance_min_max": [float(acc.min()), float(acc.max())]},
-        "gpu_ms": t_gpu,
+        "gpu_ms": t_gpu, "ms_per_sweep_by_schedule": variant_ms,
         "pressure": {"within_3se_of_cs": float(np.mean(np.abs(dev) < 3)),
                      "within_3se_of_cs_rho_below_0.90": float(np.mean(np.abs(dev[fluid]) < 3)),
                      "median_abs_rel_dev": float(np.median(np.abs(zm - zcs) / zcs)),
@@ -567,8 +578,13 @@ def run_npt(args):
         box = s.get_box()
         rho.append(s.n / (box[0] * box[1] * box[2]))
     q6 = s.global_ql(6, 1.5)
-    nb = 100
-    g = s.compute_rdf_counts(0.005, 1.0 + nb * 0.005, nb)
+    # g(r) in bins of 0.005 to r = 5, as the workload asks, on the final state
+    nb, dr_g = 800, 0.005
+    g_counts = s.compute_rdf_counts(dr_g, 1.0 + nb * dr_g, nb)
+    g_ms = s.last_timing()[0]
+    box = s.get_box()
+    r1 = 1.0 + dr_g * np.arange(nb)
+    g = g_counts / (4 * np.pi / 3 * ((r1 + dr_g) ** 3 - r1**3) * box[4] * s.n)
     line = {
         "metric": "trial moves/s, NpT N=1048576 betaP=11", "value": moves / (t * 1e-3), "unit": "trial moves/s",
         "n_gpus": 1, "higher_is_better": True, "dtype": "f64", "data": "synthetic (FCC start)",
@@ -576,7 +592,11 @@ def run_npt(args):
                                "one volume move per sweep", "sweeps": args.sweeps, "equil": args.equil,
                    "dr_max": dr, "acceptance": acc, "dv_max": dv, "volume_acceptance": vacc},
         "rho_mean": float(np.mean(rho)), "rho_sd": float(np.std(rho)), "q6": float(q6),
-        "rdf_peak_bin": int(np.argmax(g)), "gpu_ms": t,
+        "gpu_ms": t,
+        "rdf": {"dr": dr_g, "rmax": 1.0 + nb * dr_g, "gpu_ms": g_ms,
+                "first_peak_r": float(r1[np.argmax(g)] + dr_g / 2), "first_peak_g": float(np.max(g)),
+                "g_at_r": {f"{rr:.3f}": float(g[int(round((rr - 1.0) / dr_g))])
+                           for rr in (1.0025, 1.1025, 1.5025, 2.0025, 3.0025, 4.0025, 4.9975)}},
     }
     print(json.dumps(line), flush=True)
     return 0
@@ -866,6 +886,51 @@ def run_cluster(args):
     return 0
 
 
+def run_cadence(args):
+    """The large NVT fluid with its sampling cadence: after every 100 sweeps
+    g(r) in bins of 0.01 to r = 5, the virial contact histogram (5 bins),
+    the thermodynamic scan (20 compressions), 10^4 Widom insertions and q6
+    with bond cutoff 1.5.  Trial moves/s over sweeps and samples together
+    (device time of every call), and each part's share."""
+    import numpy as np
+    import hsmc_gb300
+
+    s = hsmc_gb300.HardSphereSystem(rho=RHO, cells=CELLS, dr_max=DR_MAX, seed=11)
+    s.sweep_nvt(200)
+    lanes = s.autotune(16)
+    s.upload(hsmc_gb300.lattice_config(RHO, (CELLS,) * 3))
+    s.sweep_nvt(args.equil)
+    xi = np.arange(1, 21) * 0.0005
+    sf = (1.0 - xi) ** (1.0 / 3.0)
+    parts = {"sweeps": 0.0, "g(r)": 0.0, "virial": 0.0, "thermodynamic scan": 0.0, "widom": 0.0, "q6": 0.0}
+
+    def timed(name, fn):
+        fn()
+        parts[name] += s.last_timing()[0]
+
+    for _ in range(args.samples):
+        timed("sweeps", lambda: s.sweep_nvt(100))
+        timed("g(r)", lambda: s.compute_rdf_counts(0.01, 5.0, 400))
+        timed("virial", lambda: s.compute_pressv_counts(0.01, 1.05, 5))
+        timed("thermodynamic scan", lambda: s.compute_presst(sf))
+        timed("widom", lambda: s.widom_insertion(10_000))
+        timed("q6", lambda: s.global_ql(6, 1.5))
+    total = sum(parts.values())
+    moves = N * 100 * args.samples
+    line = {
+        "metric": "trial moves/s with sampling every 100 sweeps @N=256k rho=0.85", "value": moves / (total * 1e-3),
+        "unit": "trial moves/s", "n_gpus": 1, "higher_is_better": True, "dtype": "f64",
+        "data": "synthetic (FCC lattice start, seeded random streams)",
+        "config": {"workload": "NVT fluid N=256000 rho=0.85, g(r) dr 0.01 r<5, virial and thermodynamic pressure, "
+                               "Widom 10^4 per sample, q6 (rc 1.5), every 100 sweeps",
+                   "dr_max": DR_MAX, "samples": args.samples, "equil": args.equil, "lanes_per_cell": lanes},
+        "gpu_ms": total, "ms_by_part": parts, "share_by_part": {k: v / total for k, v in parts.items()},
+    }
+    print(json.dumps(line), flush=True)
+    s.close()
+    return 0
+
+
 def run_kernels(args):
     """Each kernel of the path, one at a time, on the large NVT fluid
     (N = 256,000, rho = 0.85, 40^3 FCC start melted for --equil sweeps) and
@@ -879,6 +944,11 @@ def run_kernels(args):
     from hsmc_gb300.lwidom import LearnedWidom
 
     peak, peak_kind = peaks()
+    only = set(args.only.split(",")) if args.only else None
+
+    def want(*names):
+        return only is None or any(n in only for n in names)
+
     s = HardSphereSystem(rho=RHO, cells=CELLS, dr_max=DR_MAX, seed=5)
     s.set_schedule(0, 2)
     s.sweep_nvt(args.equil)
@@ -899,32 +969,41 @@ def run_kernels(args):
             ts.append(s.last_timing()[0])
         return float(np.median(ts))
 
-    s.set_profiling(True)
-    s.sweep_nvt(8)  # first direct launches of each variant, untimed
-    sweeps = 64
-    s.sweep_nvt(sweeps)
-    tot, mv, k = s.last_timing()
-    s.set_profiling(False)
-    add("k_move_pass", mv / k, N / 8, "trial move", B_MOVE, "events around the 8 passes of each sweep")
-    add("k_build", (tot - mv) / sweeps, N, "particle", 52.0,
-        "sweep time less its passes (build + one advance per 8 sweeps); 32 B position read, 16 B slot, 4 B count")
-    nb, dr = 400, 0.01
-    c = s.compute_rdf_counts(dr, 1 + nb * dr, nb)
-    add("k_pair_hist (g(r), r < 5)", med(lambda: s.compute_rdf_counts(dr, 1 + nb * dr, nb)), float(c.sum()),
-        "ordered pair within r_max", None, "FP64 distance per pair in the stencil's single-precision cut")
-    add("k_pair_hist (virial, [1, 1.05))", med(lambda: s.compute_pressv_counts(0.01, 1.05, 5)), N, "particle",
-        24.0 * (1 + 27 * RHO), "one 27-cell neighbourhood per particle")
-    xi = np.arange(1, 21) * 0.0005
-    sf = (1.0 - xi) ** (1.0 / 3.0)
-    add("k_scaled_scan (20 xi)", med(lambda: s.compute_presst(sf)), N, "particle", 24.0 * (1 + 27 * RHO),
-        "one neighbourhood per particle for all 20 scale factors")
-    add("k_vol_scan", med(lambda: s.scan_overlap(0.9999)), N, "particle", 24.0 * (1 + 27 * RHO),
-        "the NpT volume move's scan (early exit on an overlap)")
+    if want("k_move_pass", "k_build"):
+        s.set_profiling(True)
+        s.sweep_nvt(8)  # first direct launches of each variant, untimed
+        sweeps = 64
+        s.sweep_nvt(sweeps)
+        tot, mv, k = s.last_timing()
+        s.set_profiling(False)
+        add("k_move_pass", mv / k, N / 8, "trial move", B_MOVE, "events around the 8 passes of each sweep")
+        add("k_build", (tot - mv) / sweeps, N, "particle", 52.0,
+            "sweep time less its passes (build + one advance per 8 sweeps); 32 B position read, 16 B slot, 4 B count")
+    if want("k_pair_hist"):
+        nb, dr = 400, 0.01
+        c = s.compute_rdf_counts(dr, 1 + nb * dr, nb)
+        add("k_pair_hist (g(r), r < 5)", med(lambda: s.compute_rdf_counts(dr, 1 + nb * dr, nb)), float(c.sum()),
+            "ordered pair within r_max", None, "FP64 distance per pair in the stencil's single-precision cut")
+        add("k_pair_hist (virial, [1, 1.05))", med(lambda: s.compute_pressv_counts(0.01, 1.05, 5)), N, "particle",
+            24.0 * (1 + 27 * RHO), "one 27-cell neighbourhood per particle")
+    if want("k_scaled_scan"):
+        xi = np.arange(1, 21) * 0.0005
+        sf = (1.0 - xi) ** (1.0 / 3.0)
+        add("k_scaled_scan (20 xi)", med(lambda: s.compute_presst(sf)), N, "particle", 24.0 * (1 + 27 * RHO),
+            "one neighbourhood per particle for all 20 scale factors")
+    if want("k_vol_scan"):
+        add("k_vol_scan", med(lambda: s.scan_overlap(0.9999)), N, "particle", 24.0 * (1 + 27 * RHO),
+            "the NpT volume move's scan (early exit on an overlap)")
     n_ins = 1_000_000
-    add("k_widom (10^6 insertions)", med(lambda: s.widom_insertion(n_ins)), n_ins, "insertion", 24.0 * 27 * RHO)
-    add("k_ql (l = 6, rc = 1.5)", med(lambda: s.global_ql(6, 1.5)), N, "particle", None,
-        "FP64 Legendre recurrences per bond")
+    if want("k_widom"):
+        add("k_widom (10^6 insertions)", med(lambda: s.widom_insertion(n_ins)), n_ins, "insertion",
+            24.0 * 27 * RHO)
+    if want("k_ql"):
+        add("k_ql (l = 6, rc = 1.5)", med(lambda: s.global_ql(6, 1.5)), N, "particle", None,
+            "FP64 Legendre recurrences per bond")
     s.close()
+    if not want("k_mlp_logits", "k_widom_is", "k_mlp_grad"):
+        return emit_kernels(args, peak, peak_kind, rows, reps)
 
     w = HardSphereSystem(rho=0.94, cells=24, lattice_type=1, dr_max=0.08, seed=77)
     w.sweep_nvt(500)
@@ -947,11 +1026,15 @@ def run_kernels(args):
         "forward + backward on tcgen05, about 57 kflop per outcome")
     lw.close()
     w.close()
+    return emit_kernels(args, peak, peak_kind, rows, reps)
+
+
+def emit_kernels(args, peak, peak_kind, rows, reps):
     line = {"metric": "per-kernel device time and achieved GB/s", "n_gpus": 1, "peak_gbs": peak,
             "peak_kind": peak_kind, "data": "synthetic (lattice starts, seeded random streams)",
             "config": {"workload": "kernels one at a time: NVT fluid N=256000 rho=0.85 (40^3 FCC, "
                                    f"{args.equil} sweeps) and a rho=0.94 fluid N=13824 for the learned Widom",
-                       "dr_max": DR_MAX, "calls_per_kernel": reps},
+                       "dr_max": DR_MAX, "calls_per_kernel": reps, "only": args.only or None},
             "kernels": rows}
     print(json.dumps(line), flush=True)
     return 0
@@ -965,7 +1048,8 @@ def main():
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--workload", default="fluid",
-                    choices=["fluid", "replicas", "widom", "npt", "cluster", "cavity", "small", "readme", "kernels"])
+                    choices=["fluid", "replicas", "widom", "npt", "cluster", "cavity", "small", "readme", "kernels",
+                             "cadence"])
     ap.add_argument("--lanes", type=int, default=0,
                     help="fluid: lanes per cell (1, 2, 4, 8) instead of the autotuner's choice")
     ap.add_argument("--schedule", default="barrier", choices=["barrier", "dataflow"],
@@ -976,6 +1060,9 @@ def main():
     ap.add_argument("--sweeps", type=int, default=5000)
     ap.add_argument("--equil", type=int, default=500)
     ap.add_argument("--samples", type=int, default=20)
+    ap.add_argument("--only", default="",
+                    help="kernels: a comma list of kernels to run (k_move_pass, k_build, k_pair_hist, k_scaled_scan, "
+                         "k_vol_scan, k_widom, k_ql, k_mlp_logits, k_widom_is, k_mlp_grad)")
     args = ap.parse_args()
     if args.warmup < 3 and args.impl == "gb300" and args.steps > 2:
         args.warmup = 3
@@ -997,6 +1084,8 @@ def main():
         return run_readme(args)
     if args.workload == "kernels":
         return run_kernels(args)
+    if args.workload == "cadence":
+        return run_cadence(args)
     return run_gpu_arm(args)
 
 

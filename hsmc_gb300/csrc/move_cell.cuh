@@ -219,8 +219,8 @@ __device__ __forceinline__ void move_cell(const PassEnv &e, const PassSm &m, int
   // write the same bank column in one instruction.
   if (!direct) {
     if (G == 2 || G == 4) {
-#pragma unroll
-      for (int ph = 0; ph < G; ph++) {
+#pragma unroll 1
+      for (int ph = 0; ph < G; ph++) {  // not unrolled: the smaller code measured 0.5 % faster
         const int col = (lane + ph) & (G - 1);
         int k0 = first;
 #pragma unroll

@@ -403,7 +403,48 @@ struct QlCoef {
 };
 __constant__ QlCoef c_ql;
 
+// One bond's contribution to q_lm, m = 0..l (Y_lm by the recurrences of
+// QlCoef; cos m phi, sin m phi by the angle-addition recurrence).
+__device__ __forceinline__ void ql_bond(double dx, double dy, double dz, double r, int l, double *re, double *im) {
+  const double inv_sqrt_4pi = 0.28209479177387814;
+  const double ct = dz / r;
+  const double st = sqrt((1.0 - ct) * (1.0 + ct));
+  const double rho = sqrt(dx * dx + dy * dy);
+  const double cp = rho > 0.0 ? dx / rho : 1.0, sp = rho > 0.0 ? dy / rho : 0.0;
+  double pmm = inv_sqrt_4pi, cm = 1.0, sm = 0.0;
+  for (int m = 0; m <= l; m++) {
+    if (m > 0) {
+      pmm *= -c_ql.diag[m] * st;
+      const double c2 = cm * cp - sm * sp;
+      sm = sm * cp + cm * sp;
+      cm = c2;
+    }
+    double plm = pmm;
+    if (l > m) {
+      double p2 = pmm, p1 = ct * c_ql.first[m] * pmm;
+      for (int ll = m + 2; ll <= l; ll++) {
+        const double pn = c_ql.a[ll][m] * (ct * p1 - c_ql.b[ll][m] * p2);
+        p2 = p1;
+        p1 = pn;
+      }
+      plm = p1;
+    }
+    re[m] += plm * cm;
+    im[m] += plm * sm;
+  }
+}
+
+// Per particle: first its bonds (neighbours with r <= rc: the
+// single-precision r^2 decides outside a guard band of rc^2, the
+// reference's FP64 distance inside it), kept as ids in shared memory; then
+// the FP64 harmonics of one bond per lane per step.  A warp's FP64 sequence
+// then runs once per bond of its busiest lane, not once per candidate
+// neighbour of any lane.  Bonds are summed in the order found (the first
+// QL_MAXB; a particle with more adds the rest as it finds them).
+constexpr int QL_MAXB = 64;
+
 __global__ void __launch_bounds__(128) k_ql(SysPtrs p, Stencil s, int l, double rc, float cut2, double *q_out) {
+  __shared__ int bond_id[QL_MAXB][128];
   const CellView v = current_view(p);
   const Box *bx = p.box;
   const double len[3] = {bx->len[0], bx->len[1], bx->len[2]};
@@ -417,44 +458,39 @@ __global__ void __launch_bounds__(128) k_ql(SysPtrs p, Stencil s, int l, double 
   double re[QL_LMAX + 1], im[QL_LMAX + 1];
   for (int m = 0; m <= QL_LMAX; m++) re[m] = im[m] = 0.0;
   int bonds = 0;
-  const double inv_sqrt_4pi = 0.28209479177387814;
+  const float rc2f = (float)(rc * rc);
+  const float err = v.band * (1.0f + rc2f) + 2.4e-7f * (1.0f + rc2f);
   for_each_near(v, s, x, y, z, [&](const Slot &o) {
     if (o.id == i) return;
-    if (approx_r2(x32, y32, z32, o, v.L32) > cut2) return;
+    const float r2f = approx_r2(x32, y32, z32, o, v.L32);
+    if (r2f > cut2 || r2f > rc2f + err) return;
+    if (r2f >= rc2f - err || bonds >= QL_MAXB) {
+      double ox, oy, oz;
+      load_xyz(p.pos, o.id, ox, oy, oz);
+      const double dx = min_image(__dsub_rn(x, ox), len[0], half[0]);
+      const double dy = min_image(__dsub_rn(y, oy), len[1], half[1]);
+      const double dz = min_image(__dsub_rn(z, oz), len[2], half[2]);
+      const double r = __dsqrt_rn(__dadd_rn(__dadd_rn(__dmul_rn(dx, dx), __dmul_rn(dy, dy)), __dmul_rn(dz, dz)));
+      if (!(r <= rc)) return;
+      if (bonds >= QL_MAXB) {  // beyond the list: summed now
+        ql_bond(dx, dy, dz, r, l, re, im);
+        bonds++;
+        return;
+      }
+    }
+    bond_id[bonds][threadIdx.x] = o.id;
+    bonds++;
+  });
+  const int listed = bonds < QL_MAXB ? bonds : QL_MAXB;
+  for (int b = 0; b < listed; b++) {
     double ox, oy, oz;
-    load_xyz(p.pos, o.id, ox, oy, oz);
+    load_xyz(p.pos, bond_id[b][threadIdx.x], ox, oy, oz);
     const double dx = min_image(__dsub_rn(x, ox), len[0], half[0]);
     const double dy = min_image(__dsub_rn(y, oy), len[1], half[1]);
     const double dz = min_image(__dsub_rn(z, oz), len[2], half[2]);
     const double r = __dsqrt_rn(__dadd_rn(__dadd_rn(__dmul_rn(dx, dx), __dmul_rn(dy, dy)), __dmul_rn(dz, dz)));
-    if (!(r <= rc)) return;
-    bonds++;
-    const double ct = dz / r;
-    const double st = sqrt((1.0 - ct) * (1.0 + ct));
-    const double rho = sqrt(dx * dx + dy * dy);
-    const double cp = rho > 0.0 ? dx / rho : 1.0, sp = rho > 0.0 ? dy / rho : 0.0;
-    double pmm = inv_sqrt_4pi, cm = 1.0, sm = 0.0;
-    for (int m = 0; m <= l; m++) {
-      if (m > 0) {
-        pmm *= -c_ql.diag[m] * st;
-        const double c2 = cm * cp - sm * sp;
-        sm = sm * cp + cm * sp;
-        cm = c2;
-      }
-      double plm = pmm;
-      if (l > m) {
-        double p2 = pmm, p1 = ct * c_ql.first[m] * pmm;
-        for (int ll = m + 2; ll <= l; ll++) {
-          const double pn = c_ql.a[ll][m] * (ct * p1 - c_ql.b[ll][m] * p2);
-          p2 = p1;
-          p1 = pn;
-        }
-        plm = p1;
-      }
-      re[m] += plm * cm;
-      im[m] += plm * sm;
-    }
-  });
+    ql_bond(dx, dy, dz, r, l, re, im);
+  }
   double sum = 0.0;
   if (bonds > 0) {
     const double inv = 1.0 / bonds;

@@ -29,12 +29,6 @@ namespace hsmc {
 template <bool BATCH>
 __global__ void __launch_bounds__(256) k_build(SysPtrs p1, const SysPtrs *reps, const int *nstart, int n_reps,
                                                long long offset) {
-  // A programmatic dependent of the pass before it (launch_build): the
-  // blocks may become resident while that pass drains and wait here for its
-  // positions; the first pass of the sweep may then be scheduled, and waits
-  // for this build in turn.
-  asm volatile("griddepcontrol.wait;\n" ::: "memory");
-  asm volatile("griddepcontrol.launch_dependents;\n" ::: "memory");
   int i = blockIdx.x * blockDim.x + threadIdx.x;
   uint32_t rep = 0u;
   if (BATCH) {
@@ -308,22 +302,13 @@ void launch_volume_move(const SysPtrs &p, long long sweep_offset, double margin,
 
 // ------------------------------------------------------------------ launch
 
+// An ordinary launch: as a programmatic dependent of the last colour pass
+// (its blocks resident early, waiting for the pass's positions) the sweep
+// measured 1.7 % slower.
 void launch_build(const SysPtrs &p, long long sweep_offset, int num_sms, cudaStream_t s) {
   (void)num_sms;
   const int blocks = (p.n + 255) / 256;
-  cudaLaunchConfig_t cfg = {};
-  cfg.gridDim = dim3((unsigned)(blocks > 0 ? blocks : 1));
-  cfg.blockDim = dim3(256);
-  cfg.dynamicSmemBytes = 0;
-  cfg.stream = s;
-  cudaLaunchAttribute attr[1];
-  attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
-  attr[0].val.programmaticStreamSerializationAllowed = 1;
-  cfg.attrs = attr;
-  cfg.numAttrs = 1;
-  const SysPtrs *no_reps = nullptr;
-  const int *no_start = nullptr;
-  cudaLaunchKernelEx(&cfg, k_build<false>, p, no_reps, no_start, 0, sweep_offset);
+  k_build<false><<<blocks > 0 ? blocks : 1, 256, 0, s>>>(p, nullptr, nullptr, 0, sweep_offset);
 }
 
 void launch_build_batch(const SysPtrs *reps, const int *nstart, int n_reps, int tot_n, long long sweep_offset,

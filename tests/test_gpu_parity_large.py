@@ -27,6 +27,9 @@ pytestmark = pytest.mark.gpu
 
 C2 = dict(rho=0.85, cells=40, dr=0.13, melt=300)   # N = 256,000
 C5 = dict(rho=1.04, cells=64, dr=0.11, melt=20)    # N = 1,048,576
+# C5's box side with a dilute fluid (N = 296,352): at rho = 1.04 the system is
+# a crystal in which no insertion point is free
+C5_DILUTE = dict(rho=1.04 * (42 / 64) ** 3, cells=42, dr=0.4, melt=50)
 
 
 def band_of(L):
@@ -115,22 +118,68 @@ def test_traced_full_size_sweeps_replay_bit_exact(oracle_mod, gpu_lib, cfg, swee
     g.close()
 
 
-@pytest.mark.parametrize("cfg", [C2, C5], ids=["N256k_L67", "N1M_L100"])
+def cavity_band_points(g, conf, L, band, rng, n_random=24_000_000, chunk=4_000_000, max_cav=2000):
+    """Insertion points at a band edge of exactly one contact.  A dense
+    fluid has few cavities (about one uniform point in 10^5 is free at
+    rho = 0.85), so uniform points are screened for free ones first; each
+    free point c is then pulled along the ray from its nearest particle j to
+    |p - x_j| = t with t = 1 + k 2^-52 (kind 0) or t^2 = 1 + s f band
+    (kind 1).  Every other particle stays at least t away from p (triangle
+    inequality, since |c - x_k| >= |c - x_j| >= t), so j's band edge
+    decides."""
+    from scipy.spatial import cKDTree
+
+    free, found = [], 0
+    for _ in range(n_random // chunk):
+        c = rng.random((chunk, 3)) * L
+        free.append(c[g.widom_replay(c) == 0])
+        found += len(free[-1])
+        if found >= max_cav:
+            break
+    c = np.concatenate(free)[:max_cav]
+    x = np.mod(conf[:, 1:], L)
+    _, j = cKDTree(x, boxsize=L).query(np.mod(c, L), k=1)
+    d = c - x[j]
+    d -= L * np.round(d / L)
+    r = np.linalg.norm(d, axis=1)
+    keep = r * r > 1.0 + 2.0 * band + 1e-12   # every target t <= r: p lies between x_j and c
+    c, j, d, r = c[keep], j[keep], d[keep], r[keep]
+    per = 24
+    count = len(c) * per
+    kind = np.tile(np.repeat([0, 1], per // 2), len(c))
+    k = rng.integers(-4, 5, count)
+    f = rng.uniform(0.5, 2.0, count)
+    s = np.where(rng.random(count) < 0.5, -1.0, 1.0)
+    t = np.where(kind == 0, 1.0 + k * 2.0**-52, np.sqrt(1.0 + s * f * band))
+    src = np.repeat(np.arange(len(c)), per)
+    p = x[j[src]] + d[src] * (t / r[src])[:, None]
+    p = np.where(p >= L, p - L, np.where(p < 0.0, p + L, p))
+    return len(c), p, kind, s * f
+
+
+@pytest.mark.parametrize("cfg", [C2, C5_DILUTE], ids=["N256k_L67", "N296k_L100"])
 def test_widom_band_edge_insertions_at_large_coordinates(oracle_mod, gpu_lib, cfg):
-    """Insertion points at |r| = 1 + k 2^-52 and r^2 = 1 +- f band from a
-    particle, most near the box faces: the single-precision decisions outside
-    the band and the FP64 ones inside it equal the reference's
-    widom_compute_dist test (src/compute_widom_chem_pot.c:130-160)."""
+    """Insertion points at |r| = 1 + k 2^-52 and r^2 = 1 +- f band from one
+    particle and no closer to any other: the single-precision decisions
+    outside the band and the FP64 ones inside it equal the reference's
+    widom_compute_dist test (src/compute_widom_chem_pot.c:130-160).  At
+    L = 100.27 the fluid is dilute: the rho = 1.04 crystal has no free
+    insertion point, and the band depends on the box side only."""
     o, g, conf = prepared(oracle_mod, gpu_lib, cfg, seed=31)
     L = o.box()["lx"]
     band = band_of(L)
     rng = np.random.default_rng(9)
-    _, pos, kind, sf = adversarial_points(conf, L, band, rng, 20000)
+    n_cav, pos, kind, sf = cavity_band_points(g, conf, L, band, rng)
+    print(f"L = {L:.4f}: {n_cav} cavities, {len(pos)} insertion points")
+    assert n_cav >= 20, n_cav
     got = g.widom_replay(pos)
     want = o.widom_points(pos)
     mism = np.flatnonzero(got != want)
-    assert mism.size == 0, f"{mism.size} insertion decisions differ"
-    assert 0 < want.sum() < len(want)
+    assert mism.size == 0, f"{mism.size} of {len(want)} insertion decisions differ"
+    outside = (kind == 1) & (np.abs(sf) > 1.0)
+    assert want[outside & (sf < 0)].all()           # inside contact: overlap
+    assert not want[outside & (sf > 0)].any()       # beyond contact, all others farther: free
+    assert 0 < want[kind == 0].sum() < (kind == 0).sum()
     g.close()
 
 
