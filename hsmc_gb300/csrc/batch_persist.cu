@@ -76,6 +76,7 @@ __device__ __forceinline__ PassEnv persist_env(const SysPtrs &p, uint32_t rep, i
   e.lo = 1.0f - bx->band;
   e.hi = 1.0f + bx->band;
   e.frozen = p.st->frozen;
+  e.signal = false;
   e.rep = rep;
   e.trace = nullptr;
   e.trace_cap = 0;

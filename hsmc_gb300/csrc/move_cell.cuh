@@ -82,6 +82,7 @@ struct PassEnv {
   int nc[3];
   float lo, hi;
   int frozen;  // particles below this id stay in place (the cavities of a cavity run)
+  bool signal;  // a colour pass: let the next pass launch once the neighbours are copied
   uint32_t rep;
   uint32_t *trace;
   unsigned long long trace_cap;
@@ -260,6 +261,9 @@ __device__ __forceinline__ void move_cell(const PassEnv &e, const PassSm &m, int
     }
   }
   if (G > 1) __syncwarp(gmask);
+  // The next pass's blocks may take free block slots from here on: started
+  // earlier, their loads would compete with this pass's neighbour copies.
+  if (e.signal) asm volatile("griddepcontrol.launch_dependents;\n" ::: "memory");
 
   // This lane's column holds `rows` entries; it is padded with far-away
   // entries (never within the band of contact, never rechecked) up to a
@@ -537,6 +541,7 @@ __device__ __forceinline__ PassEnv pass_env(const SysPtrs &p, uint32_t rep, int 
   e.lo = 1.0f - bx->band;
   e.hi = 1.0f + bx->band;
   e.frozen = st->frozen;
+  e.signal = false;
   e.rep = rep;
   e.trace = p.trace;
   e.trace_cap = p.trace_cap;

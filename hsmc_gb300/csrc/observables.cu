@@ -12,9 +12,10 @@
 //   k_replay        check_overlap on given trial positions, screened as the move
 //                   pass screens a trial (src/moves.c:157-212)
 //   k_ql            Steinhardt q_l per particle (src/compute_order_parameter.c:99-229)
-// Every decision that the reference takes in FP64 is taken here in FP64 with
-// its operation order; single precision only discards pairs that are
-// clearly beyond the cutoff.
+// Every decision that the reference takes in FP64 is taken here either in
+// FP64 with its operation order, or in single precision where the single
+// precision value lies farther from the decision's threshold than its error
+// bound (the guard band), so that both give the same answer.
 #include <cooperative_groups.h>
 
 #include "cellview.cuh"
@@ -59,9 +60,9 @@ __global__ void __launch_bounds__(256) k_pair_hist(SysPtrs p1, const SysPtrs *re
     load_xyz(p.pos, i, x, y, z);
     float x32, y32, z32;  // grid coordinates, as the slots hold them
     grid_coords(v, x, y, z, x32, y32, z32);
-    for_each_near(v, s, x, y, z, [&](const Slot &o) {
-      if (o.id == i) return;
-      if (approx_r2(x32, y32, z32, o, v.L32) > cut2) return;
+    for_each_near(v, s, x, y, z, cut2, [&](const Slot &o) {
+      if (o.id == i) return false;
+      if (approx_r2(x32, y32, z32, o, v.L32) > cut2) return false;
       double ox, oy, oz;
       load_xyz(p.pos, o.id, ox, oy, oz);
       const double r = __dsqrt_rn(ref_r2(x, y, z, ox, oy, oz, len, half));
@@ -69,7 +70,7 @@ __global__ void __launch_bounds__(256) k_pair_hist(SysPtrs p1, const SysPtrs *re
         const int b = (int)__ddiv_rn(__dsub_rn(r, 1.0), bin);
         if (b < 0 || b >= nbins) {
           bad = true;
-          return;
+          return false;
         }
         if (use_sh) {
           // warp aggregation: one shared-memory atomic per distinct bin
@@ -80,6 +81,7 @@ __global__ void __launch_bounds__(256) k_pair_hist(SysPtrs p1, const SysPtrs *re
           atomicAdd(counts + b, 1ull);
         }
       }
+      return false;
     });
   }
   if (bad) atomicOr(&p.st->status, ST_BAD_BIN);
@@ -126,10 +128,29 @@ __device__ __forceinline__ int exact_bin(double r2, const double *thr, int nbins
   return k;
 }
 
+// A pair that single precision cannot bin waits in its warp's queue, and
+// the warp bins 32 of them at a time with every lane on the FP64 path: left
+// in the pair loop, the FP64 instructions of one or two lanes would stall
+// the warp in most iterations (about one pair in twelve is near a threshold
+// at r_max = 5).  The pair loop runs to the warp's fullest cell, so the
+// lanes are converged at each queue step.
+constexpr int PAIR_QUEUE = 64;  // per warp: up to 31 waiting + 32 appended
+
+__device__ __forceinline__ void bin_pending(const SysPtrs &p, const int4 e, const double len[3],
+                                            const double half[3], const double *thr, int nbins, double bin,
+                                            double rmax, unsigned int *sh, bool &bad) {
+  double x, y, z, ox, oy, oz;
+  load_xyz(p.pos, e.x, x, y, z);
+  load_xyz(p.pos, e.y, ox, oy, oz);
+  const int bn = exact_bin(ref_r2(x, y, z, ox, oy, oz, len, half), thr, nbins, bin, rmax, e.z, bad);
+  if (bn >= 0) atomicAdd(&sh[bn], 2u);
+}
+
 __global__ void __launch_bounds__(256) k_pair_hist_fast(SysPtrs p, Stencil s, double bin, double rmax, int nbins,
                                                         unsigned long long *counts, float cut2, const double *thr) {
   __shared__ unsigned int sh[FAST_BINS];
   __shared__ float thr_f[FAST_BINS + 2];
+  __shared__ int4 queue[256 / 32][PAIR_QUEUE];
   for (int b = threadIdx.x; b < nbins; b += blockDim.x) sh[b] = 0;
   for (int k = threadIdx.x; k < nbins + 2; k += blockDim.x) thr_f[k] = (float)__ldg(thr + k);
   __syncthreads();
@@ -140,65 +161,90 @@ __global__ void __launch_bounds__(256) k_pair_hist_fast(SysPtrs p, Stencil s, do
   const float band = bx->band;
   const float inv_bin = (float)(1.0 / bin);
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  const int lane = threadIdx.x & 31;
+  int4 *q = queue[threadIdx.x >> 5];
+  int qn = 0;  // the warp's waiting pairs, the same in every lane
   bool bad = false;
-  if (i < p.n) {
+  const bool live = i < p.n;
+  int ci[3] = {0, 0, 0};
+  float t[3] = {0.f, 0.f, 0.f};
+  StencilGap gap;
+  if (live) {
     double x, y, z;
     load_xyz(p.pos, i, x, y, z);
-    int ci[3];
-    float t[3];
     axis_cell(__double2float_rn(x), v.sh[0], v.L32[0], v.iw[0], v.nc[0], ci[0], t[0]);
     axis_cell(__double2float_rn(y), v.sh[1], v.L32[1], v.iw[1], v.nc[1], ci[1], t[1]);
     axis_cell(__double2float_rn(z), v.sh[2], v.L32[2], v.iw[2], v.nc[2], ci[2], t[2]);
-    for (int a = 0; a <= s.k[2]; a++) {
-      int cz = ci[2] + a;
-      const float imz = cz >= v.nc[2] ? v.L32[2] : 0.f;
-      cz -= cz >= v.nc[2] ? v.nc[2] : 0;
-      for (int b = (a == 0 ? 0 : -s.k[1]); b <= s.k[1]; b++) {
-        int cy = ci[1] + b;
-        const float imy = cy < 0 ? -v.L32[1] : (cy >= v.nc[1] ? v.L32[1] : 0.f);
-        cy += cy < 0 ? v.nc[1] : (cy >= v.nc[1] ? -v.nc[1] : 0);
-        for (int e = ((a == 0 && b == 0) ? 0 : -s.k[0]); e <= s.k[0]; e++) {
-          int cx = ci[0] + e;
-          const float imx = cx < 0 ? -v.L32[0] : (cx >= v.nc[0] ? v.L32[0] : 0.f);
-          cx += cx < 0 ? v.nc[0] : (cx >= v.nc[0] ? -v.nc[0] : 0);
-          const bool own = a == 0 && b == 0 && e == 0;
-          const int c = cx + v.nc[0] * (cy + v.nc[1] * cz);
+    gap.init(ci, t, v.w);
+  }
+  for (int a = 0; a <= s.k[2]; a++) {
+    int cz = ci[2] + a;
+    const float imz = cz >= v.nc[2] ? v.L32[2] : 0.f;
+    cz -= cz >= v.nc[2] ? v.nc[2] : 0;
+    const float gz = gap.sq(2, a);
+    if (__all_sync(0xffffffffu, !live || gz > cut2)) break;  // farther a only farther
+    for (int b = (a == 0 ? 0 : -s.k[1]); b <= s.k[1]; b++) {
+      int cy = ci[1] + b;
+      const float imy = cy < 0 ? -v.L32[1] : (cy >= v.nc[1] ? v.L32[1] : 0.f);
+      cy += cy < 0 ? v.nc[1] : (cy >= v.nc[1] ? -v.nc[1] : 0);
+      const float gzy = gz + gap.sq(1, b);
+      if (__all_sync(0xffffffffu, !live || gzy > cut2)) continue;
+      for (int e = ((a == 0 && b == 0) ? 0 : -s.k[0]); e <= s.k[0]; e++) {
+        int cx = ci[0] + e;
+        const float imx = cx < 0 ? -v.L32[0] : (cx >= v.nc[0] ? v.L32[0] : 0.f);
+        cx += cx < 0 ? v.nc[0] : (cx >= v.nc[0] ? -v.nc[0] : 0);
+        const bool own = a == 0 && b == 0 && e == 0;
+        const int c = cx + v.nc[0] * (cy + v.nc[1] * cz);
+        int n = 0;
+        if (live && gzy + gap.sq(0, e) <= cut2) {  // the cell's nearest point is within the cut
           const int m = v.cnt[c];
-          const int n = m < v.cap ? m : v.cap;  // an overfull cell was flagged by the build
-          const Slot *sl = v.slot + (size_t)c * v.cap;
-          for (int q = 0; q < n; q++) {
-            const Slot o = sl[q];
-            if (own && o.id <= i) continue;
+          n = m < v.cap ? m : v.cap;  // an overfull cell was flagged by the build
+        }
+        const Slot *sl = v.slot + (size_t)c * v.cap;
+        const int n_warp = __reduce_max_sync(0xffffffffu, n);
+        for (int k0 = 0; k0 < n_warp; k0++) {
+          int bn = -1, guess = 0, j = 0;
+          bool wait = false;
+          if (k0 < n) {
+            const Slot o = sl[k0];
             const float4 ent = imaged_entry(o, imx, imy, imz);
             const float r2f = dist2(t[0], t[1], t[2], ent);
-            if (r2f > cut2) continue;
-            // single precision where it decides: the bin whose thresholds lie
-            // farther than the error bound on both sides
-            const float err = band * (1.0f + r2f) + 2.4e-7f * (1.0f + r2f);
-            int k = (int)((sqrtf(r2f) - 1.0f) * inv_bin);
-            k = k < 0 ? 0 : (k > nbins - 1 ? nbins - 1 : k);
-            while (k > 0 && thr_f[k] > r2f) k--;
-            while (k + 1 < nbins && thr_f[k + 1] <= r2f) k++;
-            int bn;
-            if (r2f - err > thr_f[nbins + 1]) {
-              continue;  // beyond rmax
-            } else if (r2f - err > thr_f[k] && r2f + err < thr_f[k + 1] && k + 1 <= nbins) {
-              bn = k;
-            } else {
-              double ox, oy, oz;
-              load_xyz(p.pos, o.id, ox, oy, oz);
-              bn = exact_bin(ref_r2(x, y, z, ox, oy, oz, len, half), thr, nbins, bin, rmax, k, bad);
-              if (bn < 0) continue;
+            if (!(own && o.id <= i) && r2f <= cut2) {
+              // single precision where it decides: the bin whose thresholds
+              // lie farther than the error bound on both sides
+              const float err = band * (1.0f + r2f) + 2.4e-7f * (1.0f + r2f);
+              int k = (int)((sqrtf(r2f) - 1.0f) * inv_bin);
+              k = k < 0 ? 0 : (k > nbins - 1 ? nbins - 1 : k);
+              while (k > 0 && thr_f[k] > r2f) k--;
+              while (k + 1 < nbins && thr_f[k + 1] <= r2f) k++;
+              if (r2f - err > thr_f[nbins + 1]) {
+                // beyond rmax
+              } else if (r2f - err > thr_f[k] && r2f + err < thr_f[k + 1] && k + 1 <= nbins) {
+                bn = k;
+              } else {
+                wait = true;
+                guess = k;
+                j = o.id;
+              }
             }
-            // warp aggregation: one shared-memory atomic per distinct bin
-            cg::coalesced_group active = cg::coalesced_threads();
-            cg::coalesced_group same = cg::labeled_partition(active, bn);
-            if (same.thread_rank() == 0) atomicAdd(&sh[bn], 2u * same.size());
+          }
+          if (bn >= 0) atomicAdd(&sh[bn], 2u);
+          const unsigned wq = __ballot_sync(0xffffffffu, wait);
+          if (wait) q[qn + __popc(wq & ((1u << lane) - 1u))] = make_int4(i, j, guess, 0);
+          qn += __popc(wq);
+          if (qn >= 32) {
+            __syncwarp();
+            qn -= 32;
+            const int4 w = q[qn + lane];
+            __syncwarp();
+            bin_pending(p, w, len, half, thr, nbins, bin, rmax, sh, bad);
           }
         }
       }
     }
   }
+  __syncwarp();
+  if (lane < qn) bin_pending(p, q[lane], len, half, thr, nbins, bin, rmax, sh, bad);
   if (bad) atomicOr(&p.st->status, ST_BAD_BIN);
   __syncthreads();
   for (int b = threadIdx.x; b < nbins; b += blockDim.x)
@@ -247,10 +293,10 @@ __global__ void __launch_bounds__(256) k_scaled_scan(SysPtrs p, Stencil s, int n
     // contact (scaling by sf <= 1 shrinks the screen's error); inside it the
     // reference's scaled FP64 distance does
     const float lo = 1.0f - 2.0f * v.band, hi = 1.0f + 2.0f * v.band;
-    for_each_near(v, s, x, y, z, [&](const Slot &o) {
-      if (o.id == i) return;
+    for_each_near<false>(v, s, x, y, z, cut2, [&](const Slot &o) {
+      if (o.id == i) return false;
       const float r2f = approx_r2(x32, y32, z32, o, v.L32);
-      if (r2f > cut2) return;
+      if (r2f > cut2) return false;
       bool loaded = false;
       double ox = 0.0, oy = 0.0, oz = 0.0;
       for (int k = 0; k < n_sf; k++) {
@@ -268,6 +314,7 @@ __global__ void __launch_bounds__(256) k_scaled_scan(SysPtrs p, Stencil s, int n
         }
         if (ref_r2_scaled(x, y, z, ox, oy, oz, len, c_sf[k]) < 1.0) m[k >> 6] |= bit;
       }
+      return false;
     });
   }
   for (int w = 0; w < 4; w++) {
@@ -291,7 +338,7 @@ void launch_scaled_scan(const SysPtrs &p, const double *sf, int n_sf, int stenci
 }
 
 // ----------------------------------------------------------------- Widom
-__global__ void __launch_bounds__(256) k_widom(SysPtrs p, long long n, unsigned long long seq, const double *pos_in,
+__global__ void __launch_bounds__(256, 3) k_widom(SysPtrs p, long long n, unsigned long long seq, const double *pos_in,
                                                uint8_t *ov_out) {
   const CellView v = current_view(p);
   const Box *bx = p.box;
@@ -460,10 +507,10 @@ __global__ void __launch_bounds__(128) k_ql(SysPtrs p, Stencil s, int l, double 
   int bonds = 0;
   const float rc2f = (float)(rc * rc);
   const float err = v.band * (1.0f + rc2f) + 2.4e-7f * (1.0f + rc2f);
-  for_each_near(v, s, x, y, z, [&](const Slot &o) {
-    if (o.id == i) return;
+  for_each_near(v, s, x, y, z, cut2, [&](const Slot &o) {
+    if (o.id == i) return false;
     const float r2f = approx_r2(x32, y32, z32, o, v.L32);
-    if (r2f > cut2 || r2f > rc2f + err) return;
+    if (r2f > cut2 || r2f > rc2f + err) return false;
     if (r2f >= rc2f - err || bonds >= QL_MAXB) {
       double ox, oy, oz;
       load_xyz(p.pos, o.id, ox, oy, oz);
@@ -471,15 +518,16 @@ __global__ void __launch_bounds__(128) k_ql(SysPtrs p, Stencil s, int l, double 
       const double dy = min_image(__dsub_rn(y, oy), len[1], half[1]);
       const double dz = min_image(__dsub_rn(z, oz), len[2], half[2]);
       const double r = __dsqrt_rn(__dadd_rn(__dadd_rn(__dmul_rn(dx, dx), __dmul_rn(dy, dy)), __dmul_rn(dz, dz)));
-      if (!(r <= rc)) return;
+      if (!(r <= rc)) return false;
       if (bonds >= QL_MAXB) {  // beyond the list: summed now
         ql_bond(dx, dy, dz, r, l, re, im);
         bonds++;
-        return;
+        return false;
       }
     }
     bond_id[bonds][threadIdx.x] = o.id;
     bonds++;
+    return false;
   });
   const int listed = bonds < QL_MAXB ? bonds : QL_MAXB;
   for (int b = 0; b < listed; b++) {
