@@ -392,15 +392,16 @@ def run_replicas(args):
     # every schedule, timed on the same live batch (the chain is the same for
     # all): reported beside the autotuner's choice
     variant_ms = {}
-    for sch, cb, tile in [(0, 4, 2)] + [(1, c, t) for c in (1, 2, 4, 8) for t in (1, 2, 4, 8)]:
+    for sch, cb, tile in [(0, 4, 2), (2, 4, 2)] + [(1, c, t) for c in (1, 2, 4, 8) for t in (1, 2, 4, 8)]:
         try:
             b.set_schedule(sch, cb, tile)
         except Exception:
             continue
         b.sweeps(8)
         b.sweeps(16)
-        variant_ms["flat" if sch == 0 else f"persistent cb={cb} tile={tile}"] = b.last_timing() / 16
-    schedule = b.autotune(16)  # flat launches or persistent clusters, cluster size and tile
+        name = {0: "flat", 2: "persistent grid"}.get(sch, f"persistent clusters cb={cb} tile={tile}")
+        variant_ms[name] = b.last_timing() / 16
+    schedule = b.autotune(16)  # flat launches, the grid launch or clusters (cluster size and tile)
     sweeps = args.sweeps
     per = 10
     nb, bin_ = 5, 0.01
@@ -441,9 +442,11 @@ def run_replicas(args):
         "config": {"workload": f"{reps} NVT replicas, n~U{{6..20}} (N 864..32000), rho~U[0.30,0.94], "
                                f"{sweeps} sweeps after {args.equil}", "n_particles_total": n_tot,
                    "min_cell_edge": args.cell_edge,
-                   "schedule": ("persistent: one launch of thread-block clusters per call, "
-                                f"{schedule[1]} blocks per cluster, tile {schedule[2]}") if schedule[0] == 1
-                               else "flat launches per colour pass, CUDA graphs of 8 sweeps",
+                   "schedule": {0: "flat launches per colour pass, CUDA graphs of 8 sweeps",
+                                1: ("persistent: one launch of thread-block clusters per call, "
+                                    f"{schedule[1]} blocks per cluster, tile {schedule[2]}"),
+                                2: "persistent: one cooperative launch over the device per call, "
+                                   "grid barriers between build and passes"}[schedule[0]],
                    "acceptance_min_max": [float(acc.min()), float(acc.max())]},
         "gpu_ms": t_gpu, "ms_per_sweep_by_schedule": variant_ms,
         "pressure": {"within_3se_of_cs": float(np.mean(np.abs(dev) < 3)),

@@ -136,7 +136,9 @@ class ReplicaBatch:
     def set_schedule(self, schedule: int, cluster_blocks: int = 4, tile: int = 2) -> None:
         """0: flat launches per colour pass (CUDA graphs of 8 sweeps); 1: every
         sweep of a call in one persistent launch of thread-block clusters, one
-        cluster per bundle of replicas.  The same chain."""
+        cluster per bundle of replicas; 2: every sweep of a call in one
+        cooperative launch over the whole device per cell capacity, with grid
+        barriers between the phases.  The same chain."""
         _check(self._lib.hsmc_batch_set_schedule(self._h, schedule, cluster_blocks, tile),
                "hsmc_batch_set_schedule")
 
@@ -146,8 +148,8 @@ class ReplicaBatch:
         return tuple(int(x) for x in out)
 
     def autotune(self, sweeps_per_variant: int = 16):
-        """Times both schedules and every cluster size and tile; keeps the
-        fastest and returns (schedule, cluster_blocks, tile)."""
+        """Times the three schedules (every cluster size and tile for schedule
+        1); keeps the fastest and returns (schedule, cluster_blocks, tile)."""
         out = np.zeros(3, dtype=np.int32)
         _check(self._lib.hsmc_batch_autotune(self._h, sweeps_per_variant, out.ctypes.data), "hsmc_batch_autotune")
         return tuple(int(x) for x in out)

@@ -23,6 +23,11 @@ cudaError_t prepare_batch_persist();
 cudaError_t launch_batch_persist(int cap, const SysPtrs *reps, const int *rep_ids, const int *nstart,
                                  const int *gstart, const int *cstart, const int *bundle, int n_bundles,
                                  int n_sweeps, int cluster_blocks, cudaStream_t s);
+int batch_grid_blocks(int cap, int num_sms);
+cudaError_t prepare_batch_grid();
+cudaError_t launch_batch_grid(int cap, const SysPtrs *reps, const int *rep_ids, const int *nstart, const int *gstart,
+                              const int *cstart, void *params, unsigned *bar, int *abort, int *status, int n_reps,
+                              int n_sweeps, int blocks, cudaStream_t s);
 }  // namespace hsmc
 
 namespace {
@@ -41,6 +46,7 @@ int cuda_fail(cudaError_t e) {
   } while (0)
 
 int code_of(int st) {
+  if (st & ST_FLOW_TIMEOUT) return HSMC_ERR_TIMEOUT;
   if (st & (ST_CELL_OVERFLOW | ST_BAD_CELL)) return HSMC_ERR_CELL_OVERFLOW;
   if (st & ST_BAD_BIN) return HSMC_ERR_BAD_BIN;
   if (st & ST_OUT_OF_BOX) return HSMC_ERR_OUT_OF_BOX;
@@ -92,7 +98,31 @@ struct hsmc_batch {
   int bundled_cb = 0, bundled_tile = 0;
   int persist_graph_sweeps = 0;
   cudaGraphExec_t persist_graph = nullptr;  // one persistent launch per class, for persist_graph_sweeps
+  // schedule 2: every sweep of a call in one cooperative launch per cell
+  // capacity over the whole device (batch_persist.cu, k_batch_grid)
+  struct GridClass {
+    int cap = 8, n = 0, blocks = 0;
+    SysPtrs *d_reps = nullptr;
+    int *d_ids = nullptr, *d_nstart = nullptr, *d_gstart = nullptr, *d_cstart = nullptr;
+    void *d_params = nullptr;
+    unsigned *d_bar = nullptr;  // barrier words and the abort flag
+    int *status = nullptr;      // the class's first replica's status
+  };
+  std::vector<GridClass> grids;
 };
+
+static void free_grids(hsmc_batch *b) {
+  for (auto &q : b->grids) {
+    cudaFree(q.d_reps);
+    cudaFree(q.d_ids);
+    cudaFree(q.d_nstart);
+    cudaFree(q.d_gstart);
+    cudaFree(q.d_cstart);
+    cudaFree(q.d_params);
+    cudaFree(q.d_bar);
+  }
+  b->grids.clear();
+}
 
 static void free_bundles(hsmc_batch *b) {
   for (auto &q : b->bundles) {
@@ -132,6 +162,7 @@ void hsmc_batch_destroy(hsmc_batch *b) {
   if (b->stream) cudaStreamSynchronize(b->stream);
   if (b->graph) cudaGraphExecDestroy(b->graph);
   free_bundles(b);
+  free_grids(b);
   cudaFree(b->d_reps);
   cudaFree(b->d_nstart);
   cudaFree(b->d_gstart);
@@ -466,8 +497,67 @@ static int ensure_persist_graph(hsmc_batch *b, int n_sweeps) {
   return HSMC_OK;
 }
 
+// The grid schedule's tables per cell capacity: the class's replicas in
+// batch order, with prefix sums of their particles, active cells and
+// allocated cells, a parameter slot per replica and the barrier words.
+static int build_grids(hsmc_batch *b) {
+  if (!b->grids.empty()) return HSMC_OK;
+  int dev = 0, sms = 0;
+  BATCH_CUDA(cudaGetDevice(&dev));
+  BATCH_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+  for (int c : {8, 16, 32}) {
+    std::vector<SysPtrs> sp;
+    std::vector<int> ids, ns(1, 0), gs(1, 0), cs(1, 0);
+    for (int k = 0; k < b->reps; k++) {
+      if (b->sp[k].cap != c) continue;
+      sp.push_back(b->sp[k]);
+      ids.push_back(k);
+      ns.push_back(ns.back() + b->sp[k].n);
+      gs.push_back(gs.back() + b->hbox[k].ncell / 8);
+      cs.push_back(cs.back() + b->hbox[k].ncell);
+    }
+    if (sp.empty()) continue;
+    hsmc_batch::GridClass q;
+    q.cap = c;
+    q.n = (int)sp.size();
+    q.blocks = batch_grid_blocks(c, sms);
+    q.status = &sp[0].st->status;
+    const size_t nr = sp.size();
+    cudaError_t ce;
+    if ((ce = cudaMalloc(&q.d_reps, sizeof(SysPtrs) * nr)) || (ce = cudaMalloc(&q.d_ids, sizeof(int) * nr)) ||
+        (ce = cudaMalloc(&q.d_nstart, sizeof(int) * (nr + 1))) ||
+        (ce = cudaMalloc(&q.d_gstart, sizeof(int) * (nr + 1))) ||
+        (ce = cudaMalloc(&q.d_cstart, sizeof(int) * (nr + 1))) || (ce = cudaMalloc(&q.d_params, 16 * nr)) ||
+        (ce = cudaMalloc(&q.d_bar, 4 * sizeof(unsigned))) ||
+        (ce = cudaMemcpy(q.d_reps, sp.data(), sizeof(SysPtrs) * nr, cudaMemcpyHostToDevice)) ||
+        (ce = cudaMemcpy(q.d_ids, ids.data(), sizeof(int) * nr, cudaMemcpyHostToDevice)) ||
+        (ce = cudaMemcpy(q.d_nstart, ns.data(), sizeof(int) * (nr + 1), cudaMemcpyHostToDevice)) ||
+        (ce = cudaMemcpy(q.d_gstart, gs.data(), sizeof(int) * (nr + 1), cudaMemcpyHostToDevice)) ||
+        (ce = cudaMemcpy(q.d_cstart, cs.data(), sizeof(int) * (nr + 1), cudaMemcpyHostToDevice))) {
+      b->grids.push_back(q);
+      free_grids(b);
+      return cuda_fail(ce);
+    }
+    b->grids.push_back(q);
+    if (q.blocks <= 0) {
+      free_grids(b);
+      return HSMC_ERR_INVALID_ARG;
+    }
+  }
+  return HSMC_OK;
+}
+
 int hsmc_batch_set_schedule(hsmc_batch *b, int schedule, int cluster_blocks, int tile) {
-  if (!b || (schedule != 0 && schedule != 1)) return HSMC_ERR_INVALID_ARG;
+  if (!b || schedule < 0 || schedule > 2) return HSMC_ERR_INVALID_ARG;
+  if (schedule == 2) {
+    int dev = 0, coop = 0;
+    BATCH_CUDA(cudaGetDevice(&dev));
+    BATCH_CUDA(cudaDeviceGetAttribute(&coop, cudaDevAttrCooperativeLaunch, dev));
+    if (!coop) return HSMC_ERR_INVALID_ARG;
+    BATCH_CUDA(prepare_batch_grid());
+    int e = build_grids(b);
+    if (e) return e;
+  }
   if (schedule == 1) {
     if ((cluster_blocks != 1 && cluster_blocks != 2 && cluster_blocks != 4 && cluster_blocks != 8) || tile < 1 ||
         tile > 64)
@@ -500,11 +590,16 @@ int hsmc_batch_sweeps(hsmc_batch *b, int n_sweeps, uint64_t *counters) {
   for (int k = 0; k < b->reps; k++)
     if (!b->uploaded[k]) return HSMC_ERR_INVALID_ARG;
   const bool persist = b->schedule == 1 && n_sweeps > 0;
+  const bool grid = b->schedule == 2 && n_sweeps > 0;
   if (persist) {
     int e = ensure_persist_graph(b, n_sweeps);
     if (e) return e;
   }
-  if (!persist && !b->graph) {
+  if (grid) {
+    int e = build_grids(b);
+    if (e) return e;
+  }
+  if (!persist && !grid && !b->graph) {
     cudaGraph_t g = nullptr;
     BATCH_CUDA(cudaStreamBeginCapture(b->stream, cudaStreamCaptureModeThreadLocal));
     for (int s = 0; s < kBatchGraphSweeps; s++) enqueue_batch_sweep(b, s);
@@ -525,6 +620,13 @@ int hsmc_batch_sweeps(hsmc_batch *b, int n_sweeps, uint64_t *counters) {
   BATCH_CUDA(cudaEventRecord(b->ev0, b->stream));
   if (persist) {
     BATCH_CUDA(cudaGraphLaunch(b->persist_graph, b->stream));
+  } else if (grid) {
+    for (const auto &q : b->grids) {
+      BATCH_CUDA(cudaMemsetAsync(q.d_bar, 0, 4 * sizeof(unsigned), b->stream));
+      BATCH_CUDA(launch_batch_grid(q.cap, q.d_reps, q.d_ids, q.d_nstart, q.d_gstart, q.d_cstart, q.d_params, q.d_bar,
+                                   reinterpret_cast<int *>(q.d_bar + 2), q.status, q.n, n_sweeps, q.blocks,
+                                   b->stream));
+    }
   } else {
     int done = 0;
     while (n_sweeps - done >= kBatchGraphSweeps) {
@@ -556,16 +658,17 @@ int hsmc_batch_sweeps(hsmc_batch *b, int n_sweeps, uint64_t *counters) {
   return status;
 }
 
-// Times the flat schedule and the persistent one with every cluster size
-// (1, 2, 4, 8 blocks) and tile (1, 2, 4 active cells per lane group and
-// bundle), each over sweeps_per_variant sweeps after an untimed call of 8,
-// and keeps the fastest.  The chain is the same for all of them.
+// Times the flat schedule, the grid schedule and the cluster schedule with
+// every cluster size (1, 2, 4, 8 blocks) and tile (1, 2, 4 active cells per
+// lane group and bundle), each over sweeps_per_variant sweeps after an
+// untimed call of 8, and keeps the fastest.  The chain is the same for all
+// of them.
 int hsmc_batch_autotune(hsmc_batch *b, int sweeps_per_variant, int out[3]) {
   if (!b || sweeps_per_variant <= 0) return HSMC_ERR_INVALID_ARG;
   struct V {
     int s, cb, tile;
   };
-  std::vector<V> vs{{0, b->cluster_blocks, b->tile}};
+  std::vector<V> vs{{0, b->cluster_blocks, b->tile}, {2, b->cluster_blocks, b->tile}};
   for (int cb : {1, 2, 4, 8})
     for (int tile : {1, 2, 4}) vs.push_back({1, cb, tile});
   V best = vs[0];
@@ -582,8 +685,8 @@ int hsmc_batch_autotune(hsmc_batch *b, int sweeps_per_variant, int out[3]) {
   }
   int e = hsmc_batch_set_schedule(b, best.s, best.cb, best.tile);
   if (e) return e;
-  if (best.s == 0 && (b->cluster_blocks != best.cb || b->tile != best.tile)) {
-    // the flat launches won: keep the cluster shape the batch had before
+  if (best.s != 1 && (b->cluster_blocks != best.cb || b->tile != best.tile)) {
+    // the flat or grid launches won: keep the cluster shape the batch had before
     free_bundles(b);
     b->cluster_blocks = best.cb;
     b->tile = best.tile;

@@ -30,7 +30,7 @@ constexpr int kBundleMaxReps = 32;
 
 // A sweep's shift and colour order of one replica (colour of pass k in
 // nibble k), and the counters a block adds up for it.
-struct RepParams {
+struct alignas(16) RepParams {
   float sh[3];
   uint32_t perm;
 };
@@ -159,8 +159,10 @@ __global__ void __launch_bounds__(128, PassSmem<G, CAP>::min_blocks) k_batch_per
           cnt_of(p, layout ^ 1)[i + c0 - job.cstart[r0 + lr]] = 0;
         }
       }
-      for (int it = cgroup; it < tot_g; it += ncgroups) {
-        if (G > 1) __syncwarp(gmask);  // the previous cell's records are no longer read
+      // the warp's groups take their cells in step (move_pass.cu)
+      for (int it = cgroup; __any_sync(0xffffffffu, it < tot_g); it += ncgroups) {
+        __syncwarp();  // the previous cell's records are no longer read
+        if (it >= tot_g) continue;
         const int lr = find_rep(job.gstart + r0, nr, it + g0);
         const SysPtrs &p = job.reps[r0 + lr];
         const RepParams q = rp[lr];
@@ -201,6 +203,242 @@ __global__ void __launch_bounds__(128, PassSmem<G, CAP>::min_blocks) k_batch_per
     for (int d = 0; d < 3; d++) ws->params.shift32[d] = q.sh[d];
     for (int k = 0; k < 8; k++) ws->params.perm[k] = (int)((q.perm >> (4 * k)) & 7u);
     ws->sweep_base = base + (unsigned long long)job.n_sweeps;
+  }
+}
+
+// ------------------------------------------------------ grid schedule
+// Schedule 2: every sweep of a call, for every replica of one cell
+// capacity, in one cooperative launch of every block the device holds.
+// Per sweep: each replica's shift and colour order, the cell build of every
+// particle, then the eight colour passes over every active cell of every
+// replica, the phases separated by a grid-wide barrier.  A pass spreads all
+// replicas' cells over the whole device, as the flat launches do, with no
+// launch between phases.  The barrier waits are bounded (1 s): one that
+// gives up reports ST_FLOW_TIMEOUT and makes every block leave at its next
+// barrier.
+struct GridJob {
+  const SysPtrs *reps;                  // the class's replicas
+  const int *rep_ids;                   // their index in the batch (enters the random counters)
+  const int *nstart, *gstart, *cstart;  // prefix sums of particles, active cells, allocated cells
+  RepParams *params;                    // the current sweep's shift and colour order per replica
+  unsigned *bar;                        // barrier: arrivals, generation (zero at launch)
+  int *abort;                           // set once a barrier wait gave up (zero at launch)
+  int *status;                          // where that is reported
+  int n_reps, n_sweeps;
+};
+
+__device__ __forceinline__ unsigned long long grid_clock() {
+  unsigned long long t;
+  asm volatile("mov.u64 %0, %%globaltimer;\n" : "=l"(t));
+  return t;
+}
+
+// Every block arrives once per phase; the last to arrive resets the count
+// and advances the generation with a release store, the others wait for it.
+// The CTA barrier before and the fence make the block's writes visible
+// device-wide first (data written in the launch is read through L2 only).
+__device__ __forceinline__ bool grid_barrier(const GridJob &job) {
+  __shared__ int ok_s;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    int ok = 1;
+    const unsigned g = ld_acquire(job.bar + 1);
+    __threadfence();
+    if (atomicAdd(job.bar, 1u) == gridDim.x - 1u) {
+      atomicExch(job.bar, 0u);
+      __threadfence();
+      st_release(job.bar + 1, g + 1u);
+    } else {
+      const unsigned long long t0 = grid_clock();
+      while (ld_acquire(job.bar + 1) == g) {
+        if (*(volatile int *)job.abort) {
+          ok = 0;
+          break;
+        }
+        if (grid_clock() - t0 > 1000000000ull) {
+          atomicOr(job.status, ST_FLOW_TIMEOUT);
+          atomicExch(job.abort, 1);
+          ok = 0;
+          break;
+        }
+        __nanosleep(64);
+      }
+    }
+    __threadfence();
+    ok_s = ok;
+  }
+  __syncthreads();
+  return ok_s != 0;
+}
+
+__device__ __forceinline__ RepParams load_params(const RepParams *q) {
+  const float4 v = __ldcg(reinterpret_cast<const float4 *>(q));
+  RepParams r;
+  r.sh[0] = v.x;
+  r.sh[1] = v.y;
+  r.sh[2] = v.z;
+  r.perm = __float_as_uint(v.w);
+  return r;
+}
+
+template <int G, int CAP>
+__global__ void __launch_bounds__(128, PassSmem<G, CAP>::min_blocks) k_batch_grid(GridJob job) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  const PassSm m = pass_smem_ptrs<G, CAP>(smem_raw);
+  const int tid = (int)threadIdx.x;
+  const int lane = tid % G, gl = tid / G, col0 = tid - lane;
+  const int gbase = (tid & 31) & ~(G - 1);
+  const unsigned gmask = (G == 32) ? 0xffffffffu : (((1u << G) - 1u) << gbase);
+  const int gt = (int)blockIdx.x * 128 + tid, nt = (int)gridDim.x * 128;
+  const int group = gt / G, groups = nt / G;
+  const int nr = job.n_reps;
+  const int tot_n = job.nstart[nr], tot_g = job.gstart[nr], tot_c = job.cstart[nr];
+  // every replica of a batch has made the same number of sweeps; the index
+  // is advanced after the last barrier, once every block has read it
+  const unsigned long long base = job.reps[0].st->sweep_base;
+
+  for (int s = 0; s < job.n_sweeps; s++) {
+    const unsigned long long sweep = base + (unsigned long long)s;
+    const int layout = (int)(sweep & 1ull);
+    // (1) each replica's shift and colour order, published as the cell
+    // build publishes them (for the observables after the call)
+    for (int r = gt; r < nr; r += nt) {
+      const SysPtrs &p = job.reps[r];
+      const uint32_t rep = (uint32_t)job.rep_ids[r];
+      const float w[3] = {p.box->w32[0], p.box->w32[1], p.box->w32[2]};
+      RepParams q;
+      sweep_shift(p.st->seed, rep, sweep, w, q.sh);
+      int perm[8];
+      sweep_perm(p.st->seed, rep, sweep, perm);
+      q.perm = 0u;
+      for (int k = 0; k < 8; k++) q.perm |= (uint32_t)perm[k] << (4 * k);
+      job.params[r] = q;
+      DevState *ws = p.st;
+      ws->params.sweep = sweep;
+      for (int d = 0; d < 3; d++) ws->params.shift32[d] = q.sh[d];
+      for (int k = 0; k < 8; k++) ws->params.perm[k] = perm[k];
+    }
+    if (!grid_barrier(job)) return;
+    // (2) the cell build of every particle (k_build, sweep.cu)
+    for (int i = gt; i < tot_n; i += nt) {
+      const int lr = find_rep(job.nstart, nr, i);
+      const SysPtrs &p = job.reps[lr];
+      const RepParams q = load_params(job.params + lr);
+      const int li = i - job.nstart[lr];
+      const Box *bx = p.box;
+      const double2 a = __ldcg(reinterpret_cast<const double2 *>(p.pos + 4 * (size_t)li));
+      const double2 c2 = __ldcg(reinterpret_cast<const double2 *>(p.pos + 4 * (size_t)li + 2));
+      int cx, cy, cz;
+      float tx, ty, tz;
+      axis_cell(__double2float_rn(a.y), q.sh[0], bx->len32[0], bx->inv_w32[0], bx->nc[0], cx, tx);
+      axis_cell(__double2float_rn(c2.x), q.sh[1], bx->len32[1], bx->inv_w32[1], bx->nc[1], cy, ty);
+      axis_cell(__double2float_rn(c2.y), q.sh[2], bx->len32[2], bx->inv_w32[2], bx->nc[2], cz, tz);
+      const int c = cx + bx->nc[0] * (cy + bx->nc[1] * cz);
+      const int k = atomicAdd(cnt_of(p, layout) + c, 1);
+      if (k < p.cap) {
+        slot_of(p, layout)[(size_t)c * p.cap + k] = Slot{tx, ty, tz, li};
+      } else {
+        atomicOr(&p.st->status, ST_CELL_OVERFLOW);
+      }
+    }
+    if (!grid_barrier(job)) return;
+    // (3) the eight colour passes
+    for (int pass = 0; pass < 8; pass++) {
+      if (pass == 0) {  // the other layout's counts, for the next sweep's build
+        for (int i = gt; i < tot_c; i += nt) {
+          const int lr = find_rep(job.cstart, nr, i);
+          cnt_of(job.reps[lr], layout ^ 1)[i - job.cstart[lr]] = 0;
+        }
+      }
+      // the warp's groups take their cells in step (move_pass.cu)
+      for (int it = group; __any_sync(0xffffffffu, it < tot_g); it += groups) {
+        __syncwarp();  // the previous cell's records are no longer read
+        if (it >= tot_g) continue;
+        const int lr = find_rep(job.gstart, nr, it);
+        const SysPtrs &p = job.reps[lr];
+        const RepParams q = load_params(job.params + lr);
+        const PassEnv e =
+            persist_env(p, (uint32_t)job.rep_ids[lr], layout, q, sweep * 8ull + (unsigned long long)pass);
+        const int colour = (int)((q.perm >> (4 * pass)) & 7u);
+        const int hx = e.nc[0] >> 1, hy = e.nc[1] >> 1;
+        const int ac = it - job.gstart[lr];
+        const int ax = ac % hx, ayz = ac / hx, ay = ayz % hy, az = ayz / hy;
+        PassTally t;
+        bool no_wait = false;
+        move_cell<G, CAP, false, true>(e, m, tid, lane, gl, col0, gmask, 2 * ax + (colour & 1),
+                                       2 * ay + ((colour >> 1) & 1), 2 * az + ((colour >> 2) & 1), t, no_wait);
+        DevState *ws = p.st;
+        if (t.acc) atomicAdd(&ws->acc, (unsigned long long)t.acc);
+        if (t.rej_o) atomicAdd(&ws->rej_overlap, (unsigned long long)t.rej_o);
+        if (t.rej_b) atomicAdd(&ws->rej_boundary, (unsigned long long)t.rej_b);
+        if (t.rechecks) atomicAdd(&ws->rechecks, (unsigned long long)t.rechecks);
+      }
+      if (!grid_barrier(job)) return;
+    }
+  }
+  for (int r = gt; r < nr; r += nt) job.reps[r].st->sweep_base = base + (unsigned long long)job.n_sweeps;
+}
+
+template <int G, int CAP>
+static int grid_blocks_for(int num_sms) {
+  int per_sm = 0;
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_batch_grid<G, CAP>, 128, PassSmem<G, CAP>::bytes) !=
+      cudaSuccess) {
+    cudaGetLastError();
+    return 0;
+  }
+  return per_sm * num_sms;
+}
+
+// Blocks of the grid schedule's launch for cell capacity cap: every block
+// the device holds at once (0: none fits).
+int batch_grid_blocks(int cap, int num_sms) {
+  switch (cap) {
+    case 8: return grid_blocks_for<2, 8>(num_sms);
+    case 16: return grid_blocks_for<4, 16>(num_sms);
+    default: return grid_blocks_for<8, 32>(num_sms);
+  }
+}
+
+template <int G, int CAP>
+static cudaError_t grid_launch(const GridJob &job, int blocks, cudaStream_t s) {
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = dim3((unsigned)blocks);
+  cfg.blockDim = dim3(128);
+  cfg.dynamicSmemBytes = PassSmem<G, CAP>::bytes;
+  cfg.stream = s;
+  cudaLaunchAttribute attr[1];
+  attr[0].id = cudaLaunchAttributeCooperative;
+  attr[0].val.cooperative = 1;
+  cfg.attrs = attr;
+  cfg.numAttrs = 1;
+  return cudaLaunchKernelEx(&cfg, k_batch_grid<G, CAP>, job);
+}
+
+cudaError_t prepare_batch_grid() {
+  cudaError_t e = cudaFuncSetAttribute(k_batch_grid<2, 8>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                       (int)PassSmem<2, 8>::bytes);
+  if (e == cudaSuccess)
+    e = cudaFuncSetAttribute(k_batch_grid<4, 16>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             (int)PassSmem<4, 16>::bytes);
+  if (e == cudaSuccess)
+    e = cudaFuncSetAttribute(k_batch_grid<8, 32>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             (int)PassSmem<8, 32>::bytes);
+  return e;
+}
+
+// One cooperative launch for n_sweeps sweeps of the class's replicas; bar
+// (2 words) and abort must be zero.
+cudaError_t launch_batch_grid(int cap, const SysPtrs *reps, const int *rep_ids, const int *nstart, const int *gstart,
+                              const int *cstart, void *params, unsigned *bar, int *abort, int *status, int n_reps,
+                              int n_sweeps, int blocks, cudaStream_t s) {
+  if (n_reps <= 0 || n_sweeps <= 0) return cudaSuccess;
+  const GridJob job{reps,  rep_ids, nstart, gstart, cstart, reinterpret_cast<RepParams *>(params),
+                    bar,   abort,   status, n_reps, n_sweeps};
+  switch (cap) {
+    case 8: return grid_launch<2, 8>(job, blocks, s);
+    case 16: return grid_launch<4, 16>(job, blocks, s);
+    default: return grid_launch<8, 32>(job, blocks, s);
   }
 }
 

@@ -74,11 +74,16 @@ __global__ void __launch_bounds__(128, PassSmem<G, CAP>::min_blocks)
       ac = gl < per_block ? (int)blockIdx.x * per_block + gl : n_active;
       stride = n_active;
     }
-    for (; ac < n_active; ac += stride) {
-      if (G > 1) __syncwarp(gmask);  // the previous cell's records are no longer read
-      const int ax = ac % hx, ayz = ac / hx, ay = ayz % hy, az = ayz / hy;
-      move_cell<G, CAP, TRACE, false>(e, m, tid, lane, gl, col0, gmask, 2 * ax + cx, 2 * ay + cy, 2 * az + cz, t,
-                                      wait_prev);
+    // The warp takes its cells in step: its groups start each round together
+    // (left to drift, the groups of a warp would run different phases of
+    // different cells, and the warp would issue each phase once per group).
+    for (; __any_sync(0xffffffffu, ac < n_active); ac += stride) {
+      __syncwarp();  // the previous cell's records are no longer read
+      if (ac < n_active) {
+        const int ax = ac % hx, ayz = ac / hx, ay = ayz % hy, az = ayz / hy;
+        move_cell<G, CAP, TRACE, false>(e, m, tid, lane, gl, col0, gmask, 2 * ax + cx, 2 * ay + cy, 2 * az + cz, t,
+                                        wait_prev);
+      }
     }
     add_tally(t, p.st);
     return;

@@ -6,6 +6,7 @@ from __future__ import annotations
 
 import ctypes as C
 import math
+import weakref
 
 import numpy as np
 
@@ -65,6 +66,9 @@ class LearnedWidom:
         _check(lib.hsmc_lwidom_create(system._h, subcell_edge, seed, train_capacity, C.byref(h)),
                "hsmc_lwidom_create")
         self._h = h
+        # runs on the system's stream: the system closes this first, in
+        # whatever order the two are collected
+        system._dependents.append(weakref.ref(self))
         ns = np.zeros(3, dtype=np.int32)
         _check(lib.hsmc_lwidom_subgrid(h, ns.ctypes.data), "hsmc_lwidom_subgrid")
         self.ns = ns

@@ -19,6 +19,7 @@ from __future__ import annotations
 
 import ctypes as C
 import math
+import weakref
 
 import numpy as np
 
@@ -137,6 +138,7 @@ class HardSphereSystem:
         h = C.c_void_p()
         _check(lib.hsmc_gpu_create(C.byref(p), C.byref(h)), "hsmc_gpu_create")
         self._h = h
+        self._dependents = []  # objects that use this context's stream (LearnedWidom), closed first
         self.dr_max = dr_max
         self.dv_max = dv_max
         self._counters = np.zeros(6, dtype=np.uint64)
@@ -146,6 +148,10 @@ class HardSphereSystem:
     def close(self) -> None:
         h = getattr(self, "_h", None)
         if h:
+            for ref in getattr(self, "_dependents", ()):
+                dep = ref()
+                if dep is not None:
+                    dep.close()
             self._lib.hsmc_gpu_destroy(h)
             self._h = None
 

@@ -285,16 +285,22 @@ int hsmc_batch_last_timing(hsmc_batch *b, double *total_ms);
  * cells (tile 1..64; at most 32 replicas per bundle), one cluster per bundle,
  * which runs all the call's sweeps of its replicas with the cluster's
  * hardware barrier between the build and the passes; bundles never wait on
- * one another.  The chain is the same in both (sweep_nvt, src/nvt.c:201-209,
- * per replica).  HSMC_ERR_INVALID_ARG for a cluster shape the device cannot
- * hold.  get_schedule: out = {schedule, cluster_blocks, tile}. */
+ * one another.  2: persistent, every sweep of a call in one cooperative
+ * launch (per cell capacity) of every block the device holds: each sweep's
+ * cell build and eight colour passes over all the replicas' cells, separated
+ * by grid-wide barriers whose waits give up after 1 s (HSMC_ERR_TIMEOUT);
+ * cluster_blocks and tile are kept but not used.  The chain is the same in
+ * all three (sweep_nvt, src/nvt.c:201-209, per replica).
+ * HSMC_ERR_INVALID_ARG for a cluster shape the device cannot hold, or a
+ * device without cooperative launches.  get_schedule: out = {schedule,
+ * cluster_blocks, tile}. */
 int hsmc_batch_set_schedule(hsmc_batch *b, int schedule, int cluster_blocks, int tile);
 int hsmc_batch_get_schedule(hsmc_batch *b, int out[3]);
 
-/* Times schedule 0 and schedule 1 with every cluster size (1, 2, 4, 8) and
- * tile (1, 2, 4) over sweeps_per_variant sweeps each, after an untimed call
- * of 8 sweeps, and keeps the fastest (out as get_schedule).  These are
- * ordinary sweeps of every replica's chain. */
+/* Times schedules 0 and 2, and schedule 1 with every cluster size (1, 2, 4,
+ * 8) and tile (1, 2, 4), over sweeps_per_variant sweeps each, after an
+ * untimed call of 8 sweeps, and keeps the fastest (out as get_schedule).
+ * These are ordinary sweeps of every replica's chain. */
 int hsmc_batch_autotune(hsmc_batch *b, int sweeps_per_variant, int out[3]);
 
 /* ----------------------------------------------------- replay and checks
@@ -393,7 +399,8 @@ typedef struct {
   uint64_t n_learned; /* insertions drawn from the learned component */
 } hsmc_lwidom_stats;
 
-/* train_capacity: outcomes the training buffer holds (0 = none). */
+/* train_capacity: outcomes the training buffer holds (0 = none).  The
+ * proposal runs on ctx's stream and reads its cells: destroy it before ctx. */
 int hsmc_lwidom_create(hsmc_ctx *ctx, double subcell_edge, uint64_t seed, int64_t train_capacity,
                        hsmc_lwidom **out);
 void hsmc_lwidom_destroy(hsmc_lwidom *lw);

@@ -101,7 +101,7 @@ def test_replica_pressures_follow_carnahan_starling(gpu_lib):
         assert abs(z - z_cs) < 0.12 * z_cs, (rho, z, z_cs)
 
 
-def _persistent_vs_flat(systems, sweeps, variants, min_cell_edge=0.0):
+def _persistent_vs_flat(systems, sweeps, variants, min_cell_edge=0.0, schedule=1):
     from hsmc_gb300.batch import ReplicaBatch
 
     flat = ReplicaBatch(systems, min_cell_edge=min_cell_edge)
@@ -110,8 +110,8 @@ def _persistent_vs_flat(systems, sweeps, variants, min_cell_edge=0.0):
     flat.close()
     for cb, tile in variants:
         b = ReplicaBatch(systems, min_cell_edge=min_cell_edge)
-        b.set_schedule(1, cb, tile)
-        assert b.get_schedule() == (1, cb, tile)
+        b.set_schedule(schedule, cb, tile)
+        assert b.get_schedule() == (schedule, cb, tile)
         got_c = sum(b.sweeps(n) for n in sweeps)
         for k in range(len(systems)):
             assert np.array_equal(b.download(k), want[k]), (cb, tile, k)
@@ -135,6 +135,47 @@ def test_persistent_schedule_mixed_cell_capacities(gpu_lib):
     batch: one persistent launch per capacity, still the flat chain."""
     systems = [(0.45, 6, 0.3, 5), (0.80, 6, 0.15, 6), (0.30, 7, 0.4, 7), (0.60, 5, 0.25, 8)]
     _persistent_vs_flat(systems, [9], [(2, 1), (4, 2)], min_cell_edge="auto")
+
+
+def test_grid_schedule_is_the_flat_chain(gpu_lib):
+    """Every sweep of a call in one cooperative launch over the whole device
+    per cell capacity, with grid barriers between the build and the passes:
+    every replica's configuration and counters bit-identical to the flat
+    launches', over calls of 1, 7 and 16 sweeps, and with 16- and 32-slot
+    cells in the same batch."""
+    rng = np.random.default_rng(12)
+    systems = [(float(rng.uniform(0.3, 0.94)), int(rng.integers(3, 9)), 0.12, 500 + k) for k in range(40)]
+    _persistent_vs_flat(systems, [1, 7, 16], [(4, 2)], schedule=2)
+    mixed = [(0.45, 6, 0.3, 5), (0.80, 6, 0.15, 6), (0.30, 7, 0.4, 7), (0.60, 5, 0.25, 8)]
+    _persistent_vs_flat(mixed, [9], [(4, 2)], min_cell_edge="auto", schedule=2)
+
+
+def test_grid_schedule_replica_zero_and_observables(gpu_lib):
+    """Replica 0 under the grid schedule is the single context's chain, the
+    layout it leaves serves the observables, and the flat launches continue
+    the same chain."""
+    from hsmc_gb300.batch import ReplicaBatch
+
+    systems = [(0.80, 6, 0.15, 77), (0.50, 4, 0.30, 78), (0.92, 5, 0.08, 79)]
+    b = ReplicaBatch(systems)
+    b.set_schedule(2)
+    c = b.sweeps(27)
+    s = gpu_lib.HardSphereSystem(rho=0.80, cells=6, dr_max=0.15, seed=77)
+    cs = s.sweep_nvt(27)
+    assert np.array_equal(b.download(0), s.download())
+    assert np.array_equal(c[0], cs)
+    nb, dr = 5, 0.01
+    got = b.pressv_counts(dr, 1.0 + nb * dr, nb)
+    for k, (rho, n, d, seed) in enumerate(systems):
+        t = gpu_lib.HardSphereSystem(rho=rho, cells=n, dr_max=d, seed=seed, conf=b.download(k))
+        assert np.array_equal(got[k], t.compute_pressv_counts(dr, 1.0 + nb * dr, nb))
+        t.close()
+    b.set_schedule(0)
+    b.sweeps(5)
+    s.sweep_nvt(5)
+    assert np.array_equal(b.download(0), s.download())
+    b.close()
+    s.close()
 
 
 def test_persistent_replica_zero_and_observables(gpu_lib):
