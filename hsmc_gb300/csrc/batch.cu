@@ -26,8 +26,8 @@ cudaError_t launch_batch_persist(int cap, const SysPtrs *reps, const int *rep_id
 int batch_grid_blocks(int cap, int num_sms);
 cudaError_t prepare_batch_grid();
 cudaError_t launch_batch_grid(int cap, const SysPtrs *reps, const int *rep_ids, const int *nstart, const int *gstart,
-                              const int *cstart, void *params, unsigned *bar, int *abort, int *status, int n_reps,
-                              int n_sweeps, int blocks, cudaStream_t s);
+                              const int *cstart, void *params, unsigned *bar, int *abort, unsigned *work,
+                              int *status, int n_reps, int n_sweeps, int blocks, cudaStream_t s);
 }  // namespace hsmc
 
 namespace {
@@ -105,7 +105,7 @@ struct hsmc_batch {
     SysPtrs *d_reps = nullptr;
     int *d_ids = nullptr, *d_nstart = nullptr, *d_gstart = nullptr, *d_cstart = nullptr;
     void *d_params = nullptr;
-    unsigned *d_bar = nullptr;  // barrier words and the abort flag
+    unsigned *d_bar = nullptr;  // barrier words, the abort flag and two work counters
     int *status = nullptr;      // the class's first replica's status
   };
   std::vector<GridClass> grids;
@@ -528,7 +528,7 @@ static int build_grids(hsmc_batch *b) {
         (ce = cudaMalloc(&q.d_nstart, sizeof(int) * (nr + 1))) ||
         (ce = cudaMalloc(&q.d_gstart, sizeof(int) * (nr + 1))) ||
         (ce = cudaMalloc(&q.d_cstart, sizeof(int) * (nr + 1))) || (ce = cudaMalloc(&q.d_params, 16 * nr)) ||
-        (ce = cudaMalloc(&q.d_bar, 4 * sizeof(unsigned))) ||
+        (ce = cudaMalloc(&q.d_bar, 8 * sizeof(unsigned))) ||
         (ce = cudaMemcpy(q.d_reps, sp.data(), sizeof(SysPtrs) * nr, cudaMemcpyHostToDevice)) ||
         (ce = cudaMemcpy(q.d_ids, ids.data(), sizeof(int) * nr, cudaMemcpyHostToDevice)) ||
         (ce = cudaMemcpy(q.d_nstart, ns.data(), sizeof(int) * (nr + 1), cudaMemcpyHostToDevice)) ||
@@ -622,10 +622,10 @@ int hsmc_batch_sweeps(hsmc_batch *b, int n_sweeps, uint64_t *counters) {
     BATCH_CUDA(cudaGraphLaunch(b->persist_graph, b->stream));
   } else if (grid) {
     for (const auto &q : b->grids) {
-      BATCH_CUDA(cudaMemsetAsync(q.d_bar, 0, 4 * sizeof(unsigned), b->stream));
+      BATCH_CUDA(cudaMemsetAsync(q.d_bar, 0, 8 * sizeof(unsigned), b->stream));
       BATCH_CUDA(launch_batch_grid(q.cap, q.d_reps, q.d_ids, q.d_nstart, q.d_gstart, q.d_cstart, q.d_params, q.d_bar,
-                                   reinterpret_cast<int *>(q.d_bar + 2), q.status, q.n, n_sweeps, q.blocks,
-                                   b->stream));
+                                   reinterpret_cast<int *>(q.d_bar + 2), q.d_bar + 4, q.status, q.n, n_sweeps,
+                                   q.blocks, b->stream));
     }
   } else {
     int done = 0;

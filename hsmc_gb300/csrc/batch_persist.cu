@@ -223,6 +223,7 @@ struct GridJob {
   RepParams *params;                    // the current sweep's shift and colour order per replica
   unsigned *bar;                        // barrier: arrivals, generation (zero at launch)
   int *abort;                           // set once a barrier wait gave up (zero at launch)
+  unsigned *work;                       // two counters of cells handed out in a pass (zero at launch)
   int *status;                          // where that is reported
   int n_reps, n_sweeps;
 };
@@ -237,7 +238,7 @@ __device__ __forceinline__ unsigned long long grid_clock() {
 // and advances the generation with a release store, the others wait for it.
 // The CTA barrier before and the fence make the block's writes visible
 // device-wide first (data written in the launch is read through L2 only).
-__device__ __forceinline__ bool grid_barrier(const GridJob &job) {
+__device__ __forceinline__ bool grid_barrier(const GridJob &job, unsigned *reset = nullptr) {
   __shared__ int ok_s;
   __syncthreads();
   if (threadIdx.x == 0) {
@@ -246,6 +247,7 @@ __device__ __forceinline__ bool grid_barrier(const GridJob &job) {
     __threadfence();
     if (atomicAdd(job.bar, 1u) == gridDim.x - 1u) {
       atomicExch(job.bar, 0u);
+      if (reset) atomicExch(reset, 0u);  // a work counter, for its next use
       __threadfence();
       st_release(job.bar + 1, g + 1u);
     } else {
@@ -279,6 +281,48 @@ __device__ __forceinline__ RepParams load_params(const RepParams *q) {
   r.sh[2] = v.z;
   r.perm = __float_as_uint(v.w);
   return r;
+}
+
+// The cell build of every particle of the class (k_build, sweep.cu), four
+// particles a thread at a time so that their loads are issued together.  Kept
+// out of line: inlined, its registers pushed the kernel's cell work to spill.
+__device__ __noinline__ void grid_build(const GridJob &job, int layout, int gt, int nt, int tot_n) {
+  const int nr = job.n_reps;
+  constexpr int BU = 4;
+  for (int i0 = gt; i0 < tot_n; i0 += BU * nt) {
+    int lr[BU], c[BU];
+    Slot sl[BU];
+#pragma unroll
+    for (int u = 0; u < BU; u++) {
+      const int i = i0 + u * nt;
+      lr[u] = -1;
+      if (i >= tot_n) continue;
+      lr[u] = find_rep(job.nstart, nr, i);
+      const SysPtrs &p = job.reps[lr[u]];
+      const RepParams q = load_params(job.params + lr[u]);
+      const int li = i - job.nstart[lr[u]];
+      const Box *bx = p.box;
+      const double2 a = __ldcg(reinterpret_cast<const double2 *>(p.pos + 4 * (size_t)li));
+      const double2 c2 = __ldcg(reinterpret_cast<const double2 *>(p.pos + 4 * (size_t)li + 2));
+      int cx, cy, cz;
+      axis_cell(__double2float_rn(a.y), q.sh[0], bx->len32[0], bx->inv_w32[0], bx->nc[0], cx, sl[u].x);
+      axis_cell(__double2float_rn(c2.x), q.sh[1], bx->len32[1], bx->inv_w32[1], bx->nc[1], cy, sl[u].y);
+      axis_cell(__double2float_rn(c2.y), q.sh[2], bx->len32[2], bx->inv_w32[2], bx->nc[2], cz, sl[u].z);
+      sl[u].id = li;
+      c[u] = cx + bx->nc[0] * (cy + bx->nc[1] * cz);
+    }
+#pragma unroll
+    for (int u = 0; u < BU; u++) {
+      if (lr[u] < 0) continue;
+      const SysPtrs &p = job.reps[lr[u]];
+      const int k = atomicAdd(cnt_of(p, layout) + c[u], 1);
+      if (k < p.cap) {
+        slot_of(p, layout)[(size_t)c[u] * p.cap + k] = sl[u];
+      } else {
+        atomicOr(&p.st->status, ST_CELL_OVERFLOW);
+      }
+    }
+  }
 }
 
 template <int G, int CAP>
@@ -320,27 +364,7 @@ __global__ void __launch_bounds__(128, PassSmem<G, CAP>::min_blocks) k_batch_gri
     }
     if (!grid_barrier(job)) return;
     // (2) the cell build of every particle (k_build, sweep.cu)
-    for (int i = gt; i < tot_n; i += nt) {
-      const int lr = find_rep(job.nstart, nr, i);
-      const SysPtrs &p = job.reps[lr];
-      const RepParams q = load_params(job.params + lr);
-      const int li = i - job.nstart[lr];
-      const Box *bx = p.box;
-      const double2 a = __ldcg(reinterpret_cast<const double2 *>(p.pos + 4 * (size_t)li));
-      const double2 c2 = __ldcg(reinterpret_cast<const double2 *>(p.pos + 4 * (size_t)li + 2));
-      int cx, cy, cz;
-      float tx, ty, tz;
-      axis_cell(__double2float_rn(a.y), q.sh[0], bx->len32[0], bx->inv_w32[0], bx->nc[0], cx, tx);
-      axis_cell(__double2float_rn(c2.x), q.sh[1], bx->len32[1], bx->inv_w32[1], bx->nc[1], cy, ty);
-      axis_cell(__double2float_rn(c2.y), q.sh[2], bx->len32[2], bx->inv_w32[2], bx->nc[2], cz, tz);
-      const int c = cx + bx->nc[0] * (cy + bx->nc[1] * cz);
-      const int k = atomicAdd(cnt_of(p, layout) + c, 1);
-      if (k < p.cap) {
-        slot_of(p, layout)[(size_t)c * p.cap + k] = Slot{tx, ty, tz, li};
-      } else {
-        atomicOr(&p.st->status, ST_CELL_OVERFLOW);
-      }
-    }
+    grid_build(job, layout, gt, nt, tot_n);
     if (!grid_barrier(job)) return;
     // (3) the eight colour passes
     for (int pass = 0; pass < 8; pass++) {
@@ -350,9 +374,19 @@ __global__ void __launch_bounds__(128, PassSmem<G, CAP>::min_blocks) k_batch_gri
           cnt_of(job.reps[lr], layout ^ 1)[i - job.cstart[lr]] = 0;
         }
       }
-      // the warp's groups take their cells in step (move_pass.cu)
-      for (int it = group; __any_sync(0xffffffffu, it < tot_g); it += groups) {
+      // Each warp takes the next run of one cell per group from a counter,
+      // so warps that drew light cells take more (a fixed share per warp
+      // left the pass to its unluckiest warp), and its groups take their
+      // cells in step (move_pass.cu).
+      unsigned *counter = job.work + ((s * 8 + pass) & 1);
+      const int wgroups = 32 / G;
+      for (;;) {
+        int base = 0;
+        if ((tid & 31) == 0) base = (int)atomicAdd(counter, (unsigned)wgroups);
+        base = __shfl_sync(0xffffffffu, base, 0);
+        if (base >= tot_g) break;
         __syncwarp();  // the previous cell's records are no longer read
+        const int it = base + (tid & 31) / G;
         if (it >= tot_g) continue;
         const int lr = find_rep(job.gstart, nr, it);
         const SysPtrs &p = job.reps[lr];
@@ -373,7 +407,7 @@ __global__ void __launch_bounds__(128, PassSmem<G, CAP>::min_blocks) k_batch_gri
         if (t.rej_b) atomicAdd(&ws->rej_boundary, (unsigned long long)t.rej_b);
         if (t.rechecks) atomicAdd(&ws->rechecks, (unsigned long long)t.rechecks);
       }
-      if (!grid_barrier(job)) return;
+      if (!grid_barrier(job, job.work + ((s * 8 + pass + 1) & 1))) return;
     }
   }
   for (int r = gt; r < nr; r += nt) job.reps[r].st->sweep_base = base + (unsigned long long)job.n_sweeps;
@@ -428,13 +462,13 @@ cudaError_t prepare_batch_grid() {
 }
 
 // One cooperative launch for n_sweeps sweeps of the class's replicas; bar
-// (2 words) and abort must be zero.
+// (2 words), abort and work (2 words) must be zero.
 cudaError_t launch_batch_grid(int cap, const SysPtrs *reps, const int *rep_ids, const int *nstart, const int *gstart,
-                              const int *cstart, void *params, unsigned *bar, int *abort, int *status, int n_reps,
-                              int n_sweeps, int blocks, cudaStream_t s) {
+                              const int *cstart, void *params, unsigned *bar, int *abort, unsigned *work,
+                              int *status, int n_reps, int n_sweeps, int blocks, cudaStream_t s) {
   if (n_reps <= 0 || n_sweeps <= 0) return cudaSuccess;
-  const GridJob job{reps,  rep_ids, nstart, gstart, cstart, reinterpret_cast<RepParams *>(params),
-                    bar,   abort,   status, n_reps, n_sweeps};
+  const GridJob job{reps, rep_ids, nstart, gstart, cstart, reinterpret_cast<RepParams *>(params),
+                    bar,  abort,   work,   status, n_reps, n_sweeps};
   switch (cap) {
     case 8: return grid_launch<2, 8>(job, blocks, s);
     case 16: return grid_launch<4, 16>(job, blocks, s);
