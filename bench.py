@@ -50,11 +50,11 @@ B_MOVE = 24.0 * (2.0 + 27.0 * RHO)  # algorithmic bytes per trial move
 # workload, from an ncu capture of this bench command with --lanes 2
 # (cache-flushed replay, so cold-cache upper bounds; in the timed graph the
 # working set stays in L2): profiles/k_move_pass_N256k_rho085.md.
-MOVE_DRAM_BYTES = {"k_move_pass": 31835136.0 + 1280.0, "k_move_flow": None}
+MOVE_DRAM_BYTES = {"k_move_pass": 31816960.0 + 0.0, "k_move_flow": None}
 # L2 sectors the SMs requested per launch (lts__t_sectors_srcunit_tex.sum x 32 B,
 # same capture): the working set is L2-resident, so this is the traffic the
 # timed launches actually move.
-MOVE_L2_BYTES = {"k_move_pass": 1530786 * 32.0, "k_move_flow": None}
+MOVE_L2_BYTES = {"k_move_pass": 1537338 * 32.0, "k_move_flow": None}
 # The configuration both arms report: the same state, chain parameters and start.
 CONFIG = {"workload": "NVT fluid N=256000 (40^3 FCC start) rho=0.85 cubic periodic, FP64 positions",
           "n_particles": N, "rho": RHO, "dr_max": DR_MAX, "start": "FCC lattice, melted during the warm-up steps",
