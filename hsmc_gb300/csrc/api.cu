@@ -128,6 +128,7 @@ static int cuda_status(cudaError_t e) {
   } while (0)
 
 static int status_to_code(int st) {
+  if (st & ST_BAD_ID) return HSMC_ERR_INVALID_ARG;
   if (st & ST_CELL_OVERFLOW) return HSMC_ERR_CELL_OVERFLOW;
   if (st & ST_BAD_BIN) return HSMC_ERR_BAD_BIN;
   if (st & ST_OUT_OF_BOX) return HSMC_ERR_OUT_OF_BOX;
@@ -393,26 +394,27 @@ void hsmc_gpu_destroy(hsmc_ctx *ctx) {
   delete ctx;
 }
 
+// The configuration is checked on the device after the copy (ids 0..N-1,
+// coordinates in [0, L]); a configuration that fails leaves the context
+// without one (the sweep calls refuse to run until an upload succeeds).
 int hsmc_gpu_upload_config(hsmc_ctx *ctx, const double (*conf)[4], int n) {
   if (!ctx || !conf || n != ctx->n) return HSMC_ERR_INVALID_ARG;
-  const Box &b = ctx->hbox;
-  for (int i = 0; i < n; i++) {
-    if (conf[i][0] != (double)i) return HSMC_ERR_INVALID_ARG;
-    for (int d = 0; d < 3; d++) {
-      const double x = conf[i][1 + d];
-      if (!(x >= 0.0 && x <= b.len[d])) return HSMC_ERR_OUT_OF_BOX;
-    }
-  }
+  ctx->uploaded = false;
   SysPtrs &sp = ctx->sp;
   HSMC_CUDA(cudaMemcpyAsync(sp.pos, conf, sizeof(double) * 4 * (size_t)n, cudaMemcpyHostToDevice, ctx->stream));
-  for (int l = 0; l < 2; l++)
-    HSMC_CUDA(cudaMemsetAsync(sp.cnt[l], 0, sizeof(int) * (size_t)sp.ncell_alloc, ctx->stream));
   HSMC_CUDA(cudaMemsetAsync(&sp.st->status, 0, sizeof(int), ctx->stream));
-  launch_build(sp, -1, ctx->num_sms, ctx->stream);
-  reset_progress(ctx);
+  launch_check_config(sp, ctx->stream);
   int e = check_kernels(ctx);
   if (e) return e;
   DevState s;
+  if ((e = read_state(ctx, s))) return e;
+  if (s.status) return status_to_code(s.status);
+  for (int l = 0; l < 2; l++)
+    HSMC_CUDA(cudaMemsetAsync(sp.cnt[l], 0, sizeof(int) * (size_t)sp.ncell_alloc, ctx->stream));
+  launch_build(sp, -1, ctx->num_sms, ctx->stream);
+  reset_progress(ctx);
+  e = check_kernels(ctx);
+  if (e) return e;
   if ((e = read_state(ctx, s))) return e;
   if (s.status) return status_to_code(s.status);
   ctx->uploaded = true;

@@ -185,6 +185,7 @@ enum : int {
   ST_FLOW_TIMEOUT = 32,     // a dataflow wait gave up (the sweep's result is invalid)
   ST_CLUSTER_TIMEOUT = 64,  // a cluster move's grid-wide wait gave up (its result is invalid)
   ST_CAVITY_RANGE = 128,    // the cavities' distance was outside the allowed range before a cavity move
+  ST_BAD_ID = 256,          // an uploaded configuration's id column is not 0, 1, ..., N - 1
 };
 
 struct DevState {

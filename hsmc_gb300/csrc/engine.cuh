@@ -127,6 +127,9 @@ int make_box(const double len[3], double rho, Box &b, int &cap, double min_edge 
 
 // sweep.cu
 void launch_build(const SysPtrs &p, long long sweep_offset, int num_sms, cudaStream_t s);
+// Flags an uploaded configuration whose ids are not 0..N-1 (ST_BAD_ID) or
+// with a coordinate outside [0, L] (ST_OUT_OF_BOX; NaN included).
+void launch_check_config(const SysPtrs &p, cudaStream_t s);
 void launch_move_pass(const SysPtrs &p, int pass, int group, bool trace, int grid, cudaStream_t s);
 void launch_advance(const SysPtrs &p, int n_sweeps, cudaStream_t s);
 void launch_opt_step(const SysPtrs &p, int j, int n_samples, unsigned long long sweep_moves, double part_target,

@@ -302,6 +302,24 @@ void launch_volume_move(const SysPtrs &p, long long sweep_offset, double margin,
 
 // ------------------------------------------------------------------ launch
 
+// The checks of hsmc_gpu_upload_config on the device, where the copied
+// array is read at HBM speed (a host loop over it took about as long as 4 %
+// of the sweeps between an upload and a download).
+__global__ void __launch_bounds__(256) k_check_config(SysPtrs p) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= p.n) return;
+  const double2 a = *reinterpret_cast<const double2 *>(p.pos + 4 * (size_t)i);
+  const double2 b = *reinterpret_cast<const double2 *>(p.pos + 4 * (size_t)i + 2);
+  const Box *bx = p.box;
+  if (a.x != (double)i) atomicOr(&p.st->status, ST_BAD_ID);
+  if (!(a.y >= 0.0 && a.y <= bx->len[0]) || !(b.x >= 0.0 && b.x <= bx->len[1]) || !(b.y >= 0.0 && b.y <= bx->len[2]))
+    atomicOr(&p.st->status, ST_OUT_OF_BOX);
+}
+
+void launch_check_config(const SysPtrs &p, cudaStream_t s) {
+  k_check_config<<<(p.n + 255) / 256 > 0 ? (p.n + 255) / 256 : 1, 256, 0, s>>>(p);
+}
+
 // An ordinary launch: as a programmatic dependent of the last colour pass
 // (its blocks resident early, waiting for the pass's positions) the sweep
 // measured 1.7 % slower.

@@ -85,7 +85,11 @@ void hsmc_gpu_destroy(hsmc_ctx *ctx);
 
 /* Copies a host configuration double[n][4] = (id, x, y, z) to the device and
  * builds the cell layout (src/cell_list.c:142-175).  conf[i][0] must equal i
- * and coordinates must lie in [0, L]. */
+ * (else HSMC_ERR_INVALID_ARG) and coordinates must lie in [0, L] (else
+ * HSMC_ERR_OUT_OF_BOX); both are checked on the device after the copy, and
+ * a configuration that fails leaves the context without one: the calls that
+ * need a configuration return HSMC_ERR_INVALID_ARG until an upload
+ * succeeds. */
 int hsmc_gpu_upload_config(hsmc_ctx *ctx, const double (*conf)[4], int n);
 
 /* Copies the device configuration back into double[n][4]
