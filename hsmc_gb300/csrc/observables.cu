@@ -454,10 +454,13 @@ __constant__ QlCoef c_ql;
 // QlCoef; cos m phi, sin m phi by the angle-addition recurrence).
 __device__ __forceinline__ void ql_bond(double dx, double dy, double dz, double r, int l, double *re, double *im) {
   const double inv_sqrt_4pi = 0.28209479177387814;
-  const double ct = dz / r;
-  const double st = sqrt((1.0 - ct) * (1.0 + ct));
+  // cos and sin of the polar angle and of the azimuth from two reciprocals
+  // (the pipe that FP64 division and square root run on bounds this kernel)
+  const double inv_r = 1.0 / r;
   const double rho = sqrt(dx * dx + dy * dy);
-  const double cp = rho > 0.0 ? dx / rho : 1.0, sp = rho > 0.0 ? dy / rho : 0.0;
+  const double inv_rho = rho > 0.0 ? 1.0 / rho : 0.0;
+  const double ct = dz * inv_r, st = rho * inv_r;
+  const double cp = rho > 0.0 ? dx * inv_rho : 1.0, sp = rho > 0.0 ? dy * inv_rho : 0.0;
   double pmm = inv_sqrt_4pi, cm = 1.0, sm = 0.0;
   for (int m = 0; m <= l; m++) {
     if (m > 0) {
