@@ -452,7 +452,11 @@ __constant__ QlCoef c_ql;
 
 // One bond's contribution to q_lm, m = 0..l (Y_lm by the recurrences of
 // QlCoef; cos m phi, sin m phi by the angle-addition recurrence).
-__device__ __forceinline__ void ql_bond(double dx, double dy, double dz, double r, int l, double *re, double *im) {
+// LT > 0: l = LT at compile time (the loops unroll and the sums stay in
+// registers); LT = 0: l from the argument.
+template <int LT>
+__device__ __forceinline__ void ql_bond(double dx, double dy, double dz, double r, int l_arg, double *re, double *im) {
+  const int l = LT > 0 ? LT : l_arg;
   const double inv_sqrt_4pi = 0.28209479177387814;
   // cos and sin of the polar angle and of the azimuth from two reciprocals
   // (the pipe that FP64 division and square root run on bounds this kernel)
@@ -462,7 +466,9 @@ __device__ __forceinline__ void ql_bond(double dx, double dy, double dz, double 
   const double ct = dz * inv_r, st = rho * inv_r;
   const double cp = rho > 0.0 ? dx * inv_rho : 1.0, sp = rho > 0.0 ? dy * inv_rho : 0.0;
   double pmm = inv_sqrt_4pi, cm = 1.0, sm = 0.0;
-  for (int m = 0; m <= l; m++) {
+#pragma unroll
+  for (int m = 0; m <= (LT > 0 ? LT : QL_LMAX); m++) {
+    if (LT == 0 && m > l) break;
     if (m > 0) {
       pmm *= -c_ql.diag[m] * st;
       const double c2 = cm * cp - sm * sp;
@@ -472,7 +478,9 @@ __device__ __forceinline__ void ql_bond(double dx, double dy, double dz, double 
     double plm = pmm;
     if (l > m) {
       double p2 = pmm, p1 = ct * c_ql.first[m] * pmm;
-      for (int ll = m + 2; ll <= l; ll++) {
+#pragma unroll
+      for (int ll = m + 2; ll <= (LT > 0 ? LT : QL_LMAX); ll++) {
+        if (LT == 0 && ll > l) break;
         const double pn = c_ql.a[ll][m] * (ct * p1 - c_ql.b[ll][m] * p2);
         p2 = p1;
         p1 = pn;
@@ -493,7 +501,9 @@ __device__ __forceinline__ void ql_bond(double dx, double dy, double dz, double 
 // QL_MAXB; a particle with more adds the rest as it finds them).
 constexpr int QL_MAXB = 64;
 
-__global__ void __launch_bounds__(128) k_ql(SysPtrs p, Stencil s, int l, double rc, float cut2, double *q_out) {
+template <int LT>
+__global__ void __launch_bounds__(128) k_ql(SysPtrs p, Stencil s, int l_arg, double rc, float cut2, double *q_out) {
+  const int l = LT > 0 ? LT : l_arg;
   __shared__ int bond_id[QL_MAXB][128];
   const CellView v = current_view(p);
   const Box *bx = p.box;
@@ -505,8 +515,10 @@ __global__ void __launch_bounds__(128) k_ql(SysPtrs p, Stencil s, int l, double 
   load_xyz(p.pos, i, x, y, z);
   float x32, y32, z32;  // grid coordinates, as the slots hold them
   grid_coords(v, x, y, z, x32, y32, z32);
-  double re[QL_LMAX + 1], im[QL_LMAX + 1];
-  for (int m = 0; m <= QL_LMAX; m++) re[m] = im[m] = 0.0;
+  constexpr int NM = LT > 0 ? LT + 1 : QL_LMAX + 1;
+  double re[NM], im[NM];
+#pragma unroll
+  for (int m = 0; m < NM; m++) re[m] = im[m] = 0.0;
   int bonds = 0;
   const float rc2f = (float)(rc * rc);
   const float err = v.band * (1.0f + rc2f) + 2.4e-7f * (1.0f + rc2f);
@@ -523,7 +535,7 @@ __global__ void __launch_bounds__(128) k_ql(SysPtrs p, Stencil s, int l, double 
       const double r = __dsqrt_rn(__dadd_rn(__dadd_rn(__dmul_rn(dx, dx), __dmul_rn(dy, dy)), __dmul_rn(dz, dz)));
       if (!(r <= rc)) return false;
       if (bonds >= QL_MAXB) {  // beyond the list: summed now
-        ql_bond(dx, dy, dz, r, l, re, im);
+        ql_bond<LT>(dx, dy, dz, r, l, re, im);
         bonds++;
         return false;
       }
@@ -540,12 +552,14 @@ __global__ void __launch_bounds__(128) k_ql(SysPtrs p, Stencil s, int l, double 
     const double dy = min_image(__dsub_rn(y, oy), len[1], half[1]);
     const double dz = min_image(__dsub_rn(z, oz), len[2], half[2]);
     const double r = __dsqrt_rn(__dadd_rn(__dadd_rn(__dmul_rn(dx, dx), __dmul_rn(dy, dy)), __dmul_rn(dz, dz)));
-    ql_bond(dx, dy, dz, r, l, re, im);
+    ql_bond<LT>(dx, dy, dz, r, l, re, im);
   }
   double sum = 0.0;
   if (bonds > 0) {
     const double inv = 1.0 / bonds;
-    for (int m = 0; m <= l; m++) {
+#pragma unroll
+    for (int m = 0; m < NM; m++) {
+      if (m > l) break;
       const double a = re[m] * inv, b = im[m] * inv;
       sum += (m == 0 ? 1.0 : 2.0) * (a * a + b * b);
     }
@@ -585,7 +599,10 @@ void launch_ql(const SysPtrs &p, int l, double rc, int stencil[3], double *per_p
   Stencil s{{stencil[0], stencil[1], stencil[2]}};
   const float cut = (float)rc + 1e-3f;
   const int blocks = (p.n + 127) / 128;
-  k_ql<<<blocks > 0 ? blocks : 1, 128, 0, st>>>(p, s, l, rc, cut * cut, per_particle);
+  const dim3 grid(blocks > 0 ? blocks : 1);
+  if (l == 6) k_ql<6><<<grid, 128, 0, st>>>(p, s, l, rc, cut * cut, per_particle);
+  else if (l == 4) k_ql<4><<<grid, 128, 0, st>>>(p, s, l, rc, cut * cut, per_particle);
+  else k_ql<0><<<grid, 128, 0, st>>>(p, s, l, rc, cut * cut, per_particle);
   k_sum<<<1, 1024, 0, st>>>(per_particle, p.n, sum);
 }
 
