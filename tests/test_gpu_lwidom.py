@@ -190,9 +190,10 @@ def test_learned_proposal_gain_at_rho_094(gpu_lib):
     """rho = 0.94 fluid, N = 13,824, melted from a 24^3 simple-cubic lattice
     (a face-centred start at this density stays crystalline for > 10^4
     sweeps).  After self-training (10^7 kept outcomes from 10^9 insertions),
-    the variance per insertion of the mixture estimate against that of
-    uniform Widom, p (1 - p), at the estimated p.  The gain is printed; the
-    test requires at least 5x (13x measured when written)."""
+    the learned draws must succeed at least 10x as often as uniform ones;
+    the variance per insertion of the mixture estimate against uniform
+    Widom's, p (1 - p), is printed (over these 2 10^7 insertions it mostly
+    misses the estimator's heavy tail, see the benchmark-state test)."""
     from hsmc_gb300.lwidom import LearnedWidom
 
     s = gpu_lib.HardSphereSystem(rho=0.94, cells=24, lattice_type=1, dr_max=0.08, seed=9)
@@ -202,7 +203,7 @@ def test_learned_proposal_gain_at_rho_094(gpu_lib):
     log = lw.fit()
     n_tot, n_pos = lw.samples()
     sw = sw2 = 0.0
-    nins = 0
+    nins = n_ok = n_learned = 0
     for _ in range(5):
         s.sweep_nvt(20)
         lw.refresh()
@@ -210,31 +211,35 @@ def test_learned_proposal_gain_at_rho_094(gpu_lib):
         sw += st.sum_w
         sw2 += st.sum_w2
         nins += st.n
+        n_ok += st.n_ok
+        n_learned += st.n_learned
     p = sw / nins
     var_l = sw2 / nins - p * p
     assert p > 0 and var_l > 0
     gain = p * (1 - p) / var_l
+    concentration = (n_ok / n_learned) / p
     print(f"\nrho=0.94 N=13824: p={p:.3e} beta_mu={-math.log(p):.3f} kept outcomes {n_tot} "
-          f"({n_pos} successes), variance gain over uniform {gain:.1f}x, log {log}")
-    assert gain > 5.0
+          f"({n_pos} successes), learned draws succeed {concentration:.0f}x as often as uniform ones, "
+          f"variance estimate {gain:.1f}x below uniform's, log {log}")
+    assert concentration >= 10.0
 
 
 def test_learned_proposal_efficiency_at_the_widom_benchmark(gpu_lib):
     """The benchmarked state: a rho = 0.94 fluid of N = 110,592 (melted from
     a 48^3 simple-cubic lattice; a 30^3 face-centred start stays crystalline
-    at this density), self-trained on 10^7 kept outcomes, then 20 samples of
-    10^6 insertions for each estimator.
+    at this density), self-trained on 10^7 kept outcomes, then 40 samples of
+    2.5 10^7 insertions for each estimator (10^9 each).
 
     The learned draws must concentrate on cavities: their success rate at
-    least 10x the insertion probability p (100x and more measured).  The
+    least 10x the insertion probability p (60-120x measured).  The
     efficiency, 1 / (variance per insertion x device time per insertion),
-    against uniform Widom at the same p is printed, not gated: measured from
-    0.6x to 17.6x over runs and states.  The spread is the estimator's heavy
-    tail: a success drawn by the defensive uniform part (alpha = 0.1) in a
-    sub-cell the network scores near zero weighs 1/alpha = 10, and one such
-    success carries 30-99 % of the sum of squared weights when it occurs,
-    about once in a few runs at p ~ 10^-7.  Training time is not counted, as
-    it is paid once per state."""
+    against uniform Widom at the same p is printed, not gated.  The learned
+    estimator's variance is heavy-tailed: a success drawn by the defensive
+    uniform part (alpha = 0.1) in a sub-cell the network scores near zero
+    weighs 1/alpha = 10.  Over 10^9 insertions, which sample that tail, the
+    variance gain at this state is 0.7-2.6x (the efficiency 0.5-1.9x);
+    estimates over 2 10^7 insertions, which mostly miss it, reported
+    10-60x.  Training time is not counted, as it is paid once per state."""
     from hsmc_gb300.lwidom import LearnedWidom
 
     s = gpu_lib.HardSphereSystem(rho=0.94, cells=48, lattice_type=1, dr_max=0.05, seed=77)
@@ -242,8 +247,8 @@ def test_learned_proposal_efficiency_at_the_widom_benchmark(gpu_lib):
     lw = LearnedWidom(s, 0.5, seed=78, train_capacity=10_000_000)
     lw.use_prior()
     lw.fit()
-    ins, sw, sw2, n_l, t_l, t_u, n_u, n_ok, n_learned = 1_000_000, 0.0, 0.0, 0, 0.0, 0.0, 0, 0, 0
-    for _ in range(20):
+    ins, sw, sw2, n_l, t_l, t_u, n_u, n_ok, n_learned = 25_000_000, 0.0, 0.0, 0, 0.0, 0.0, 0, 0, 0
+    for _ in range(40):
         s.sweep_nvt(20)
         t_l += lw.refresh()
         st = lw.insert(ins, alpha=0.1)
