@@ -85,6 +85,10 @@ __global__ void __launch_bounds__(128, PassSmem<G, CAP>::min_blocks)
                                         wait_prev);
       }
     }
+    // A block whose cells were all empty has not waited for the previous
+    // pass: it waits now, so that this pass completes only after that one
+    // (the next pass's wait, and its launch, rely on it).
+    if (wait_prev) asm volatile("griddepcontrol.wait;\n" ::: "memory");
     add_tally(t, p.st);
     return;
   }
