@@ -237,7 +237,7 @@ def test_learned_proposal_efficiency_at_the_widom_benchmark(gpu_lib):
     estimator's variance is heavy-tailed: a success drawn by the defensive
     uniform part (alpha = 0.1) in a sub-cell the network scores near zero
     weighs 1/alpha = 10.  Over 10^9 insertions, which sample that tail, the
-    variance gain at this state is 0.7-2.7x (the efficiency 0.5-2.1x);
+    variance gain at this state is 0.7-4.1x (the efficiency 0.5-3.2x);
     estimates over 2 10^7 insertions, which mostly miss it, reported
     10-60x.  Training time is not counted, as it is paid once per state."""
     from hsmc_gb300.lwidom import LearnedWidom
