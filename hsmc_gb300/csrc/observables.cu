@@ -211,12 +211,13 @@ __global__ void __launch_bounds__(256) k_pair_hist_fast(SysPtrs p, Stencil s, do
             const float r2f = dist2(t[0], t[1], t[2], ent);
             if (!(own && o.id <= i) && r2f <= cut2) {
               // single precision where it decides: the bin whose thresholds
-              // lie farther than the error bound on both sides
+              // lie farther than the error bound on both sides.  The bin is
+              // estimated from sqrt(r2) and only checked against its two
+              // thresholds: an estimate off by one lies within the error
+              // bound of a threshold, and such a pair is queued anyway
               const float err = band * (1.0f + r2f) + 2.4e-7f * (1.0f + r2f);
               int k = (int)((sqrtf(r2f) - 1.0f) * inv_bin);
               k = k < 0 ? 0 : (k > nbins - 1 ? nbins - 1 : k);
-              while (k > 0 && thr_f[k] > r2f) k--;
-              while (k + 1 < nbins && thr_f[k + 1] <= r2f) k++;
               if (r2f - err > thr_f[nbins + 1]) {
                 // beyond rmax
               } else if (r2f - err > thr_f[k] && r2f + err < thr_f[k + 1] && k + 1 <= nbins) {
