@@ -580,6 +580,7 @@ def run_npt(args):
 
     s = HardSphereSystem(rho=1.04, cells=64, dr_max=0.05, dv_max=0.001, pressure=11.0, seed=91)
     dr, acc, dv, vacc = opt_npt(s, TARGET_ACC, None)
+    lanes = s.autotune(16)  # lanes per cell and schedule, timed on live NpT sweeps
     s.sweep_npt(args.equil)
     rho = []
     t = 0.0
@@ -603,7 +604,8 @@ def run_npt(args):
         "n_gpus": 1, "higher_is_better": True, "dtype": "f64", "data": "synthetic (FCC start)",
         "config": {"workload": "NpT 64^3 FCC, beta P 11, dv_max 0.001, dr_max tuned by the reference's optimiser, "
                                "one volume move per sweep", "sweeps": args.sweeps, "equil": args.equil,
-                   "dr_max": dr, "acceptance": acc, "dv_max": dv, "volume_acceptance": vacc},
+                   "dr_max": dr, "acceptance": acc, "dv_max": dv, "volume_acceptance": vacc,
+                   "lanes_per_cell": lanes, "schedule": list(s.get_schedule())},
         "rho_mean": float(np.mean(rho)), "rho_sd": float(np.std(rho)), "q6": float(q6),
         "gpu_ms": t,
         "rdf": {"dr": dr_g, "rmax": 1.0 + nb * dr_g, "gpu_ms": g_ms,
