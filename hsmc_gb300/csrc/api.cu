@@ -284,7 +284,17 @@ int hsmc_gpu_create(const hsmc_params *prm, hsmc_ctx **out) {
   ctx->num_sms = p.multiProcessorCount;
   ctx->hbox = b;
   switch (prm->lanes_per_cell) {
-    case 0: ctx->group = kDefaultLanes; break;
+    case 0: {
+      // A system with more active cells than one wave of 2-lane groups
+      // holds runs each group through several cells a pass; 8 lanes a cell
+      // then shorten each cell's chain more than the extra waves cost
+      // (measured: N = 1,048,576 at 8 lanes 1.27x the trial moves/s of 2).
+      // hsmc_gpu_autotune times every choice on the live system.
+      const long long active = (long long)b.ncell / 8;
+      const long long wave = 4ll * p.multiProcessorCount * (128 / kDefaultLanes);
+      ctx->group = (active > wave && move_pass_fits(8, cap)) ? 8 : kDefaultLanes;
+      break;
+    }
     case 1: case 2: case 4: case 8: ctx->group = prm->lanes_per_cell; break;
     default: delete ctx; return HSMC_ERR_INVALID_ARG;
   }
