@@ -325,6 +325,145 @@ __global__ void __launch_bounds__(256) k_scaled_scan(SysPtrs p, Stencil s, int n
   }
 }
 
+// The same scan over a half stencil (each unordered pair once: the scaled
+// FP64 distance of (i, j) and (j, i) is the same number), warp by warp in
+// step as the pair counts go, with the pairs inside the band of a scaled
+// contact queued per warp and decided 32 at a time in FP64.  The result is
+// an OR over pairs, so a warp stops once every scale factor has an overlap
+// somewhere: after each stencil cell it publishes the bits it found and
+// reads those of the whole grid.  Needs a stencil narrower than the grid.
+__device__ __forceinline__ void scaled_pending(const SysPtrs &p, const int4 e, const double len[3], int n_sf,
+                                               float lo, float hi, unsigned long long m[4]) {
+  double x, y, z, ox, oy, oz;
+  load_xyz(p.pos, e.x, x, y, z);
+  load_xyz(p.pos, e.y, ox, oy, oz);
+  const float r2f = __int_as_float(e.z);
+  for (int k = 0; k < n_sf; k++) {
+    const unsigned long long bit = 1ull << (k & 63);
+    if (m[k >> 6] & bit) continue;
+    const float est = r2f * c_sf2f[k];
+    if (est < lo || est > hi) continue;  // decided in single precision at the queueing
+    if (ref_r2_scaled(x, y, z, ox, oy, oz, len, c_sf[k]) < 1.0) m[k >> 6] |= bit;
+  }
+}
+
+__global__ void __launch_bounds__(256) k_scaled_scan_fast(SysPtrs p, Stencil s, int n_sf, float cut2) {
+  __shared__ int4 queue[256 / 32][PAIR_QUEUE];
+  const CellView v = current_view(p);
+  const Box *bx = p.box;
+  const double len[3] = {bx->len[0], bx->len[1], bx->len[2]};
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  const int lane = threadIdx.x & 31;
+  int4 *q = queue[threadIdx.x >> 5];
+  int qn = 0;
+  const bool live = i < p.n;
+  // the scaled single-precision r^2 decides outside twice the guard band of
+  // contact (scaling by sf <= 1 shrinks the screen's error)
+  const float lo = 1.0f - 2.0f * v.band, hi = 1.0f + 2.0f * v.band;
+  unsigned long long m[4] = {0ull, 0ull, 0ull, 0ull}, full[4];
+#pragma unroll
+  for (int w = 0; w < 4; w++) {
+    const int b = n_sf - 64 * w;  // bits of word w in use
+    full[w] = b >= 64 ? ~0ull : (b > 0 ? (1ull << b) - 1ull : 0ull);
+  }
+  const int nw = (n_sf + 63) >> 6;
+  unsigned long long *gmask = p.st->scan_mask;
+  int ci[3] = {0, 0, 0};
+  float t[3] = {0.f, 0.f, 0.f};
+  StencilGap gap;
+  if (live) {
+    double x, y, z;
+    load_xyz(p.pos, i, x, y, z);
+    axis_cell(__double2float_rn(x), v.sh[0], v.L32[0], v.iw[0], v.nc[0], ci[0], t[0]);
+    axis_cell(__double2float_rn(y), v.sh[1], v.L32[1], v.iw[1], v.nc[1], ci[1], t[1]);
+    axis_cell(__double2float_rn(z), v.sh[2], v.L32[2], v.iw[2], v.nc[2], ci[2], t[2]);
+    gap.init(ci, t, v.w);
+  }
+  bool done = false;
+  for (int a = 0; a <= s.k[2] && !done; a++) {
+    int cz = ci[2] + a;
+    const float imz = cz >= v.nc[2] ? v.L32[2] : 0.f;
+    cz -= cz >= v.nc[2] ? v.nc[2] : 0;
+    const float gz = gap.sq(2, a);
+    if (__all_sync(0xffffffffu, !live || gz > cut2)) break;
+    for (int b = (a == 0 ? 0 : -s.k[1]); b <= s.k[1] && !done; b++) {
+      int cy = ci[1] + b;
+      const float imy = cy < 0 ? -v.L32[1] : (cy >= v.nc[1] ? v.L32[1] : 0.f);
+      cy += cy < 0 ? v.nc[1] : (cy >= v.nc[1] ? -v.nc[1] : 0);
+      const float gzy = gz + gap.sq(1, b);
+      if (__all_sync(0xffffffffu, !live || gzy > cut2)) continue;
+      for (int e = ((a == 0 && b == 0) ? 0 : -s.k[0]); e <= s.k[0] && !done; e++) {
+        int cx = ci[0] + e;
+        const float imx = cx < 0 ? -v.L32[0] : (cx >= v.nc[0] ? v.L32[0] : 0.f);
+        cx += cx < 0 ? v.nc[0] : (cx >= v.nc[0] ? -v.nc[0] : 0);
+        const bool own = a == 0 && b == 0 && e == 0;
+        const int c = cx + v.nc[0] * (cy + v.nc[1] * cz);
+        int n = 0;
+        if (live && gzy + gap.sq(0, e) <= cut2) {
+          const int mm = v.cnt[c];
+          n = mm < v.cap ? mm : v.cap;
+        }
+        const Slot *sl = v.slot + (size_t)c * v.cap;
+        const int n_warp = __reduce_max_sync(0xffffffffu, n);
+        for (int k0 = 0; k0 < n_warp; k0++) {
+          bool wait = false;
+          int j = 0;
+          float r2q = 0.f;
+          if (k0 < n) {
+            const Slot o = sl[k0];
+            const float4 ent = imaged_entry(o, imx, imy, imz);
+            const float r2f = dist2(t[0], t[1], t[2], ent);
+            if (!(own && o.id <= i) && r2f <= cut2) {
+              for (int k = 0; k < n_sf; k++) {
+                const unsigned long long bit = 1ull << (k & 63);
+                if (m[k >> 6] & bit) continue;
+                const float est = r2f * c_sf2f[k];
+                if (est < lo) m[k >> 6] |= bit;
+                else if (est <= hi) wait = true;
+              }
+              j = o.id;
+              r2q = r2f;
+            }
+          }
+          const unsigned wq = __ballot_sync(0xffffffffu, wait);
+          if (wait) q[qn + __popc(wq & ((1u << lane) - 1u))] = make_int4(i, j, __float_as_int(r2q), 0);
+          qn += __popc(wq);
+          if (qn >= 32) {
+            __syncwarp();
+            qn -= 32;
+            const int4 w = q[qn + lane];
+            __syncwarp();
+            scaled_pending(p, w, len, n_sf, lo, hi, m);
+          }
+        }
+        // publish this warp's bits; stop once the grid has all of them
+        bool all = true;
+#pragma unroll
+        for (int w = 0; w < 4; w++) {
+          if (w >= nw) break;
+          unsigned long long r = m[w];
+          for (int o = 16; o > 0; o >>= 1) r |= __shfl_xor_sync(0xffffffffu, r, o);
+          unsigned long long g = 0ull;
+          if (lane == 0) {
+            const unsigned long long seen = *(volatile unsigned long long *)(gmask + w);
+            g = (r & ~seen) ? atomicOr(gmask + w, r) | r : seen;
+          }
+          g = __shfl_sync(0xffffffffu, g, 0);
+          all = all && ((g & full[w]) == full[w]);
+        }
+        done = all;
+      }
+    }
+  }
+  __syncwarp();
+  if (lane < qn) scaled_pending(p, q[lane], len, n_sf, lo, hi, m);
+  for (int w = 0; w < 4; w++) {
+    unsigned long long r = m[w];
+    for (int o = 16; o > 0; o >>= 1) r |= __shfl_xor_sync(0xffffffffu, r, o);
+    if (lane == 0 && r) atomicOr(gmask + w, r);
+  }
+}
+
 void launch_scaled_scan(const SysPtrs &p, const double *sf, int n_sf, int stencil[3], cudaStream_t st) {
   double smallest = 1.0;
   for (int k = 0; k < n_sf; k++) smallest = sf[k] < smallest ? sf[k] : smallest;
@@ -335,7 +474,10 @@ void launch_scaled_scan(const SysPtrs &p, const double *sf, int n_sf, int stenci
   Stencil s{{stencil[0], stencil[1], stencil[2]}};
   const float cut = (float)(1.0 / smallest) + 1e-3f;
   const int blocks = (p.n + 255) / 256;
-  k_scaled_scan<<<blocks > 0 ? blocks : 1, 256, 0, st>>>(p, s, n_sf, cut * cut);
+  if (stencil[0] >= 0 && stencil[1] >= 0 && stencil[2] >= 0)
+    k_scaled_scan_fast<<<blocks > 0 ? blocks : 1, 256, 0, st>>>(p, s, n_sf, cut * cut);
+  else
+    k_scaled_scan<<<blocks > 0 ? blocks : 1, 256, 0, st>>>(p, s, n_sf, cut * cut);
 }
 
 // ----------------------------------------------------------------- Widom

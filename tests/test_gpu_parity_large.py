@@ -207,6 +207,13 @@ def test_scaled_scans_at_band_edges(oracle_mod, gpu_lib, cfg):
     assert np.array_equal(got.astype(np.float64), want), (sfs, got, want)
     for sf in sfs:
         assert g.scan_overlap(float(sf)) == o.scan_overlap(float(sf)), sf
+    # every bit set (the scan may stop early), all but one (sf = 1 has no
+    # overlap: the scan runs to the end), and a mask of two words
+    xi = np.arange(1, 21) * 0.0005
+    bench_sf = (1.0 - xi) ** (1.0 / 3.0)
+    for sfs in (bench_sf, np.append(bench_sf, 1.0), np.linspace(0.999, 1.0, 70)):
+        got = g.compute_presst(sfs)
+        assert np.array_equal(got.astype(np.float64), o.presst_counts_sf(sfs)), sfs
     g.close()
 
 
