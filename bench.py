@@ -249,12 +249,13 @@ def run_gpu_arm(args):
 
     sysm = hsmc_gb300.HardSphereSystem(rho=RHO, cells=CELLS, dr_max=DR_MAX, seed=2026 + rank)
     if args.lanes:
-        sysm.set_schedule(1 if args.schedule == "dataflow" else 0, args.lanes)
+        sysm.set_schedule({"barrier": 0, "dataflow": 1, "ordered": 3}[args.schedule], args.lanes)
         lanes = args.lanes
     else:
         sysm.sweep_nvt(200)  # tune on the fluid, not on the lattice it starts from
         lanes = sysm.autotune(16)
-    schedule, _ = sysm.get_schedule()  # 1: dataflow sweep (one launch), 0: one launch per colour pass
+    # 1: dataflow sweep (one launch); 0, 3: one launch per colour pass (cells in grid / occupancy order)
+    schedule, _ = sysm.get_schedule()
     # the autotuner's sweeps are not part of the chain: restart from the lattice
     sysm.upload(hsmc_gb300.lattice_config(RHO, (CELLS,) * 3))
     flush = torch.empty(256 * 1024 * 1024, dtype=torch.uint8, device="cuda")  # > 129 MB L2
@@ -338,7 +339,8 @@ def run_gpu_arm(args):
         "step": f"{SWEEPS_PER_STEP} checkerboard sweeps of one system per GPU (each N trial moves), CUDA graphs "
                 f"of 8 sweeps",
         "engine": {"lanes_per_cell": lanes,
-                   "schedule": "dataflow (8 passes per launch)" if schedule == 1 else "one launch per colour pass",
+                   "schedule": {1: "dataflow (8 passes per launch)", 3: "one launch per colour pass, cells in occupancy order"}
+                   .get(schedule, "one launch per colour pass"),
                    "acceptance": acc_moves / max(moves, 1), "parallelism": f"replicas x{world}"},
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                      "frac": achieved / peak, "traffic": traffic,
@@ -733,7 +735,9 @@ def run_small(args):
         t0 = time.perf_counter()
         g.sweep_nvt(k)
         dt = time.perf_counter() - t0
-        row = {"N": g.n, "rho": rho, "schedule": ["one launch per pass", "dataflow", "one block"][g.get_schedule()[0]],
+        row = {"N": g.n, "rho": rho,
+               "schedule": ["one launch per pass", "dataflow", "one block", "one launch per pass, occupancy order"]
+               [g.get_schedule()[0]],
                "gpu_us_per_sweep": dt / k * 1e6, "gpu_moves_per_s": g.n * k / dt}
         if not args.no_cpu_baseline:
             o = OracleSim(rho=rho, n_cells=cells, lattice_type=lt, seed=3, dr_max=0.15, neigh_dr=1.05)
@@ -1067,8 +1071,9 @@ def main():
                              "cadence"])
     ap.add_argument("--lanes", type=int, default=0,
                     help="fluid: lanes per cell (1, 2, 4, 8) instead of the autotuner's choice")
-    ap.add_argument("--schedule", default="barrier", choices=["barrier", "dataflow"],
-                    help="fluid, with --lanes: one launch per colour pass or the dataflow sweep")
+    ap.add_argument("--schedule", default="barrier", choices=["barrier", "dataflow", "ordered"],
+                    help="fluid, with --lanes: one launch per colour pass (cells in grid or occupancy order) "
+                         "or the dataflow sweep")
     ap.add_argument("--replicas", type=int, default=512)
     ap.add_argument("--cell-edge", default="0",
                     help='replicas: smallest device-cell edge, a number or "auto" (min(rho^-1/3, 1.4))')

@@ -81,6 +81,9 @@ struct hsmc_ctx {
   int flow_grid = 0;
   int flow_graph = -1;  // -1 untested, 0 no, 1 yes
   uint32_t *prog = nullptr;
+  // schedule 3: each colour's non-empty cells listed fullest first
+  // (SysPtrs::olist points here while that schedule is in use)
+  int *olist = nullptr;
   // cluster moves: queue (N ints), marks (N words), counters, per-move output
   Scratch cl_queue, cl_mark, cl_ctr, cl_out;
   unsigned long long cluster_seq = 0;  // cluster moves drawn from the stream so far
@@ -283,18 +286,21 @@ int hsmc_gpu_create(const hsmc_params *prm, hsmc_ctx **out) {
   ctx->n = prm->n_particles;
   ctx->num_sms = p.multiProcessorCount;
   ctx->hbox = b;
+  // A system with more active cells than one wave of 2-lane groups runs
+  // each group through several cells a pass.  There 8 lanes a cell shorten
+  // each cell's chain more than the extra waves cost, and the occupancy
+  // order (schedule 3) takes the empty cells out of the waves and gives each
+  // warp cells of one occupancy (measured at N = 1,048,576: 8 lanes 1.27x the
+  // trial moves/s of 2, the occupancy order another 1.12x).  Within one wave
+  // the grid order is faster: the two order launches and the scattered
+  // cells cost more there than the shorter trial rounds save.
+  // hsmc_gpu_autotune times every choice on the live system.
+  const long long active_cells = (long long)b.ncell / 8;
+  const bool beyond_wave = active_cells > 4ll * p.multiProcessorCount * (128 / kDefaultLanes);
   switch (prm->lanes_per_cell) {
-    case 0: {
-      // A system with more active cells than one wave of 2-lane groups
-      // holds runs each group through several cells a pass; 8 lanes a cell
-      // then shorten each cell's chain more than the extra waves cost
-      // (measured: N = 1,048,576 at 8 lanes 1.27x the trial moves/s of 2).
-      // hsmc_gpu_autotune times every choice on the live system.
-      const long long active = (long long)b.ncell / 8;
-      const long long wave = 4ll * p.multiProcessorCount * (128 / kDefaultLanes);
-      ctx->group = (active > wave && move_pass_fits(8, cap)) ? 8 : kDefaultLanes;
+    case 0:
+      ctx->group = (beyond_wave && move_pass_fits(8, cap)) ? 8 : kDefaultLanes;
       break;
-    }
     case 1: case 2: case 4: case 8: ctx->group = prm->lanes_per_cell; break;
     default: delete ctx; return HSMC_ERR_INVALID_ARG;
   }
@@ -323,6 +329,10 @@ int hsmc_gpu_create(const hsmc_params *prm, hsmc_ctx **out) {
     if ((ce = cudaMalloc(&sp.slot[l], sizeof(Slot) * (size_t)sp.ncell_alloc * cap)) != cudaSuccess) return fail(ce);
     if ((ce = cudaMemset(sp.cnt[l], 0, sizeof(int) * (size_t)sp.ncell_alloc)) != cudaSuccess) return fail(ce);
   }
+  if ((ce = cudaMalloc(&ctx->olist, sizeof(int) * (size_t)sp.ncell_alloc)) != cudaSuccess) return fail(ce);
+  sp.olist = beyond_wave ? ctx->olist : nullptr;
+  if ((ce = cudaMalloc(&sp.ocnt, sizeof(int) * (size_t)kOrderWords)) != cudaSuccess) return fail(ce);
+  if ((ce = cudaMemset(sp.ocnt, 0, sizeof(int) * (size_t)kOrderWords)) != cudaSuccess) return fail(ce);
   if ((ce = cudaMalloc(&sp.box, sizeof(Box))) != cudaSuccess) return fail(ce);
   if ((ce = cudaMalloc(&sp.st, sizeof(DevState))) != cudaSuccess) return fail(ce);
   if ((ce = cudaMemcpy(sp.box, &b, sizeof(Box), cudaMemcpyHostToDevice)) != cudaSuccess) return fail(ce);
@@ -382,6 +392,8 @@ void hsmc_gpu_destroy(hsmc_ctx *ctx) {
     cudaFree(sp.cnt[l]);
     cudaFree(sp.slot[l]);
   }
+  cudaFree(ctx->olist);
+  cudaFree(sp.ocnt);
   cudaFree(sp.box);
   cudaFree(sp.st);
   cudaFree(ctx->prog);
@@ -466,10 +478,12 @@ int hsmc_gpu_last_timing(hsmc_ctx *ctx, double *total_ms, double *move_kernel_ms
   return HSMC_OK;
 }
 
-// The eight passes of one sweep: one dataflow launch, or eight launches with
-// a kernel boundary after each colour.
+// The eight passes of one sweep: one dataflow launch, or the occupancy
+// order of the cells and eight launches with a kernel boundary after each
+// colour.
 static cudaError_t enqueue_moves(hsmc_ctx *ctx, bool trace) {
   if (ctx->flow) return launch_move_flow(ctx->sp, ctx->prog, ctx->group, trace, ctx->flow_grid, ctx->stream);
+  if (ctx->sp.olist) launch_order(ctx->sp, ctx->stream);
   for (int k = 0; k < 8; k++) launch_move_pass(ctx->sp, k, ctx->group, trace, ctx->pass_grid, ctx->stream);
   return cudaSuccess;
 }
@@ -606,6 +620,7 @@ static int run_sweeps(hsmc_ctx *ctx, int n_sweeps, bool trace, bool npt, uint64_
       // timed as a whole: events between the passes would break the
       // programmatic dependent launches that overlap one pass's tail with
       // the next pass's start, so the eight passes are bracketed together
+      if (ctx->sp.olist) launch_order(ctx->sp, ctx->stream);
       if (timing) HSMC_CUDA(cudaEventRecord(ctx->ev_pass[16 * s], ctx->stream));
       for (int k = 0; k < 8; k++) launch_move_pass(ctx->sp, k, ctx->group, trace, ctx->pass_grid, ctx->stream);
       if (timing) HSMC_CUDA(cudaEventRecord(ctx->ev_pass[16 * s + 1], ctx->stream));
@@ -691,6 +706,7 @@ static void drop_graphs(hsmc_ctx *ctx) {
 
 // Lanes per cell and schedule; the grids follow.  Returns false when the
 // combination cannot run on this device.
+// flow: the schedule of hsmc_gpu_set_schedule (0, 1, 2 or 3).
 static bool apply_schedule(hsmc_ctx *ctx, int flow, int group) {
   if (flow == 2) {  // one block: the lane mapping of the passes is kept for the other schedules
     if (ctx->small_smem == 0) return false;
@@ -700,7 +716,7 @@ static bool apply_schedule(hsmc_ctx *ctx, int flow, int group) {
   if (!move_pass_fits(group, ctx->sp.cap)) return false;
   ctx->small = false;
   int fg = 0;
-  if (flow) {
+  if (flow == 1) {
     int dev = 0, coop = 0;
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&coop, cudaDevAttrCooperativeLaunch, dev);
@@ -709,7 +725,8 @@ static bool apply_schedule(hsmc_ctx *ctx, int flow, int group) {
     if (fg <= 0) return false;
   }
   ctx->group = group;
-  ctx->flow = flow != 0;
+  ctx->flow = flow == 1;
+  ctx->sp.olist = flow == 3 ? ctx->olist : nullptr;
   ctx->flow_grid = fg;
   ctx->pass_grid = move_pass_grid(group, ctx->sp.cap, ctx->sp.ncell_alloc, ctx->num_sms);
   ctx->flow_graph = -1;
@@ -730,11 +747,11 @@ int hsmc_gpu_autotune(hsmc_ctx *ctx, int sweeps_per_variant, int *lanes_out) {
   const int sweeps = ((sweeps_per_variant + kGraphSweeps - 1) / kGraphSweeps) * kGraphSweeps;
   ctx->profiling = false;  // time the production path: graphs of sweeps
   const int g0 = ctx->group;
-  double t[3][4];
-  for (int f = 0; f < 3; f++)
+  double t[4][4];
+  for (int f = 0; f < 4; f++)
     for (int v = 0; v < 4; v++) t[f][v] = 1e300;
   for (int round = 0; round < 2; round++)
-    for (int f = 2; f >= 0; f--)
+    for (int f = 3; f >= 0; f--)
       for (int v = 0; v < 4; v++) {
         if (f == 2 && v > 0) continue;  // one variant
         if (!apply_schedule(ctx, f, f == 2 ? ctx->group : options[v])) continue;
@@ -747,9 +764,9 @@ int hsmc_gpu_autotune(hsmc_ctx *ctx, int sweeps_per_variant, int *lanes_out) {
         }
         if (ctx->last_total_ms < t[f][v]) t[f][v] = ctx->last_total_ms;
       }
-  int best_g = ctx->group, best_f = ctx->small ? 2 : (ctx->flow ? 1 : 0);
+  int best_g = ctx->group, best_f = ctx->small ? 2 : (ctx->flow ? 1 : (ctx->sp.olist ? 3 : 0));
   double best_ms = 1e300;
-  for (int f = 2; f >= 0; f--)
+  for (int f = 3; f >= 0; f--)
     for (int v = 0; v < 4; v++)
       if (t[f][v] < best_ms) {
         best_ms = t[f][v];
@@ -806,7 +823,7 @@ int hsmc_gpu_optimize(hsmc_ctx *ctx, int opt_sweeps, int opt_samples, double par
 }
 
 int hsmc_gpu_set_schedule(hsmc_ctx *ctx, int schedule, int lanes_per_cell) {
-  if (!ctx || schedule < 0 || schedule > 2) return HSMC_ERR_INVALID_ARG;
+  if (!ctx || schedule < 0 || schedule > 3) return HSMC_ERR_INVALID_ARG;
   const int g = lanes_per_cell == 0 ? ctx->group : lanes_per_cell;
   if (g != 1 && g != 2 && g != 4 && g != 8) return HSMC_ERR_INVALID_ARG;
   return apply_schedule(ctx, schedule, g) ? HSMC_OK : HSMC_ERR_INVALID_ARG;
@@ -822,7 +839,7 @@ int hsmc_gpu_hold_region(hsmc_ctx *ctx, int region) {
 
 int hsmc_gpu_get_schedule(hsmc_ctx *ctx, int *schedule, int *lanes_per_cell) {
   if (!ctx) return HSMC_ERR_INVALID_ARG;
-  if (schedule) *schedule = ctx->small ? 2 : (ctx->flow ? 1 : 0);
+  if (schedule) *schedule = ctx->small ? 2 : (ctx->flow ? 1 : (ctx->sp.olist ? 3 : 0));
   if (lanes_per_cell) *lanes_per_cell = ctx->group;
   return HSMC_OK;
 }

@@ -23,7 +23,17 @@ struct SysPtrs {
   int n;               // particles
   int cap;             // slots per cell
   int ncell_alloc;     // cells allocated per layout
+  // Occupancy order of a single system's colour passes (batches: nullptr).
+  // olist: per colour c, entries [c * ncell_alloc / 8, ...) list the colour's
+  // non-empty cells, fullest first.  ocnt: words [32 c + n - 1] count the
+  // cells of colour c holding n particles (n > 32 counts as 32), words
+  // [256 + 32 c + n - 1] are the scatter's cursors, word 512 + c the number
+  // of non-empty cells of colour c.
+  int *olist;
+  int *ocnt;
 };
+
+constexpr int kOrderWords = 520;  // words of SysPtrs::ocnt
 
 // The replica holding flat index x, for batched launches over all replicas:
 // the last r with start[r] <= x (start has n + 1 ascending entries).
@@ -127,6 +137,9 @@ int make_box(const double len[3], double rho, Box &b, int &cap, double min_edge 
 
 // sweep.cu
 void launch_build(const SysPtrs &p, long long sweep_offset, int num_sms, cudaStream_t s);
+// After a sweep's build: each colour's non-empty cells listed fullest first
+// (SysPtrs::olist), which the colour passes hand out to their warps.
+void launch_order(const SysPtrs &p, cudaStream_t s);
 // Flags an uploaded configuration whose ids are not 0..N-1 (ST_BAD_ID) or
 // with a coordinate outside [0, L] (ST_OUT_OF_BOX; NaN included).
 void launch_check_config(const SysPtrs &p, cudaStream_t s);

@@ -60,34 +60,67 @@ __global__ void __launch_bounds__(128, PassSmem<G, CAP>::min_blocks)
       for (int c = blockIdx.x * blockDim.x + threadIdx.x; c < p.ncell_alloc; c += gridDim.x * blockDim.x)
         other[c] = 0;
     }
-    const int hx = e.nc[0] >> 1, hy = e.nc[1] >> 1, hz = e.nc[2] >> 1;
-    const int n_active = hx * hy * hz;
-    const int cx = colour & 1, cy = (colour >> 1) & 1, cz = (colour >> 2) & 1;
     bool wait_prev = pass != 0;
-    // With at most one cell per group, each block takes an equal run of
-    // consecutive active cells (a small system is spread over every SM,
-    // move_pass_grid); otherwise the groups stride over the cells.
-    const int gpb = (int)blockDim.x / G;
-    int ac = group, stride = (int)((gridDim.x * blockDim.x) / G);
-    if (n_active <= (int)gridDim.x * gpb) {
-      const int per_block = (n_active + (int)gridDim.x - 1) / (int)gridDim.x;
-      ac = gl < per_block ? (int)blockIdx.x * per_block + gl : n_active;
-      stride = n_active;
+    const int hx = e.nc[0] >> 1, hy = e.nc[1] >> 1, hz = e.nc[2] >> 1;
+    const int cx = colour & 1, cy = (colour >> 1) & 1, cz = (colour >> 2) & 1;
+    // Which cells the groups take, by rounds: a group takes entry a of a
+    // sequence of cells, then a + stride, while a < limit.
+    //  - spatial (p.olist null): the active cells of the colour in grid order.
+    //    With at most one cell per group, each block takes an equal run of
+    //    consecutive active cells (a small system is spread over every SM,
+    //    move_pass_grid); otherwise the groups stride over the cells.
+    //  - occupancy order (schedule 3): the colour's non-empty cells, fullest
+    //    first (k_order_scatter), in runs of one cell per lane group of a
+    //    warp; run j goes to block j mod grid, so the fullest runs (the
+    //    longest trial chains) spread over every SM.  The list was complete
+    //    before the first pass of the sweep began, so a pass may read it
+    //    before its wait on the previous pass.
+    const bool ordered = p.olist != nullptr;
+    const int *list = nullptr;
+    int a, stride, limit;
+    if (ordered) {
+      constexpr int GPW = 32 / G;  // lane groups per warp
+      limit = p.ocnt[512 + colour];
+      list = p.olist + (size_t)colour * (size_t)(p.ncell_alloc / 8);
+      const int nwb = (int)blockDim.x >> 5;
+      a = ((int)blockIdx.x + (int)gridDim.x * (tid >> 5)) * GPW + (tid & 31) / G;
+      stride = (int)gridDim.x * nwb * GPW;
+    } else {
+      limit = hx * hy * hz;
+      const int gpb = (int)blockDim.x / G;
+      a = group;
+      stride = (int)((gridDim.x * blockDim.x) / G);
+      if (limit <= (int)gridDim.x * gpb) {
+        const int per_block = (limit + (int)gridDim.x - 1) / (int)gridDim.x;
+        a = gl < per_block ? (int)blockIdx.x * per_block + gl : limit;
+        stride = limit;
+      }
     }
     // The warp takes its cells in step: its groups start each round together
     // (left to drift, the groups of a warp would run different phases of
     // different cells, and the warp would issue each phase once per group).
-    for (; __any_sync(0xffffffffu, ac < n_active); ac += stride) {
+    for (; __any_sync(0xffffffffu, a < limit); a += stride) {
       __syncwarp();  // the previous cell's records are no longer read
-      if (ac < n_active) {
-        const int ax = ac % hx, ayz = ac / hx, ay = ayz % hy, az = ayz / hy;
-        move_cell<G, CAP, TRACE, false>(e, m, tid, lane, gl, col0, gmask, 2 * ax + cx, 2 * ay + cy, 2 * az + cz, t,
-                                        wait_prev);
+      if (a < limit) {
+        int ix, iy, iz;
+        if (ordered) {
+          const int c = list[a];
+          const int iyz = c / e.nc[0];
+          ix = c - iyz * e.nc[0];
+          iy = iyz % e.nc[1];
+          iz = iyz / e.nc[1];
+        } else {
+          const int ax = a % hx, ayz = a / hx, ay = ayz % hy, az = ayz / hy;
+          ix = 2 * ax + cx;
+          iy = 2 * ay + cy;
+          iz = 2 * az + cz;
+        }
+        move_cell<G, CAP, TRACE, false>(e, m, tid, lane, gl, col0, gmask, ix, iy, iz, t, wait_prev);
       }
     }
-    // A block whose cells were all empty has not waited for the previous
-    // pass: it waits now, so that this pass completes only after that one
-    // (the next pass's wait, and its launch, rely on it).
+    // A block without cells, or whose cells were all empty, has not waited
+    // for the previous pass: it waits now, so that this pass completes only
+    // after that one (the next pass's wait, and its launch, rely on it).
     if (wait_prev) asm volatile("griddepcontrol.wait;\n" ::: "memory");
     add_tally(t, p.st);
     return;

@@ -37,6 +37,10 @@ __global__ void __launch_bounds__(256) k_build(SysPtrs p1, const SysPtrs *reps, 
     i -= __ldg(nstart + rep);
   }
   const SysPtrs p = BATCH ? reps[rep] : p1;
+  // the occupancy counts of this sweep's order start from zero (k_order_count
+  // adds to them once this build is complete)
+  if (!BATCH && p.ocnt != nullptr && blockIdx.x == 0)
+    for (int t = threadIdx.x; t < 256; t += blockDim.x) p.ocnt[t] = 0;
   const DevState *st = p.st;
   const Box *bx = p.box;
   const unsigned long long s = st->sweep_base + (unsigned long long)offset;
@@ -75,6 +79,89 @@ __global__ void __launch_bounds__(256) k_build(SysPtrs p1, const SysPtrs *reps, 
 }
 
 __global__ void k_advance(DevState *st, int n) { st->sweep_base += (unsigned long long)n; }
+
+// ---------------------------------------------------------- occupancy order
+// A colour pass gives each warp the cells of 32/G consecutive entries of
+// its colour's list, and a warp makes as many trial rounds as its fullest
+// cell holds particles.  Listed fullest first, a warp's cells hold the same
+// number of particles (but for the few warps at the boundary of two
+// occupancies), and empty cells take no lanes.  The order changes nothing in
+// the chain: the cells of one colour are independent, and a cell's random
+// numbers are keyed by the cell, not by the lanes that move it.
+//
+// Two launches after the build, 1024 cells per block: k_order_count counts
+// each colour's cells by occupancy (shared-memory histogram, one global add
+// per bin and block); k_order_scatter places each block's cells of one bin
+// at the bin's start (the cells of more particles come first) plus the
+// block's reservation from the bin's cursor.
+constexpr int kOrderThreads = 256, kOrderPerThread = 4;
+
+// Bin of cell c (colour * 32 + min(n, 32) - 1) of the current grid, or -1
+// for an empty cell or one beyond the grid.
+__device__ __forceinline__ int order_bin(const int *cnt, int c, int ncell, int nc0, int nc1) {
+  if (c >= ncell) return -1;
+  const int n = cnt[c];
+  if (n <= 0) return -1;
+  const int ix = c % nc0, iyz = c / nc0, iy = iyz % nc1, iz = iyz / nc1;
+  return 32 * cell_colour(ix, iy, iz) + (n < 32 ? n : 32) - 1;
+}
+
+__global__ void __launch_bounds__(kOrderThreads) k_order_count(SysPtrs p) {
+  asm volatile("griddepcontrol.wait;\n" ::: "memory");
+  __shared__ int h[256];
+  const int tid = (int)threadIdx.x;
+  h[tid] = 0;
+  if (blockIdx.x == 0) p.ocnt[256 + tid] = 0;  // the scatter's cursors
+  __syncthreads();
+  const Box *bx = p.box;
+  const int nc0 = bx->nc[0], nc1 = bx->nc[1], ncell = bx->ncell;
+  const int *cnt = cnt_of(p, (int)(p.st->params.sweep & 1ull));
+  const int c0 = (blockIdx.x * kOrderThreads + tid) * kOrderPerThread;
+#pragma unroll
+  for (int k = 0; k < kOrderPerThread; k++) {
+    const int b = order_bin(cnt, c0 + k, ncell, nc0, nc1);
+    if (b >= 0) atomicAdd(&h[b], 1);
+  }
+  __syncthreads();
+  if (h[tid]) atomicAdd(&p.ocnt[tid], h[tid]);
+}
+
+__global__ void __launch_bounds__(kOrderThreads) k_order_scatter(SysPtrs p) {
+  asm volatile("griddepcontrol.wait;\n" ::: "memory");
+  __shared__ int h[256], tot[256], start[256];
+  const int tid = (int)threadIdx.x;
+  h[tid] = 0;
+  tot[tid] = p.ocnt[tid];
+  __syncthreads();
+  // the number of non-empty cells of each colour, for the passes
+  if (blockIdx.x == 0 && tid < 8) {
+    int t = 0;
+    for (int m = 0; m < 32; m++) t += tot[32 * tid + m];
+    p.ocnt[512 + tid] = t;
+  }
+  const Box *bx = p.box;
+  const int nc0 = bx->nc[0], nc1 = bx->nc[1], ncell = bx->ncell;
+  const int *cnt = cnt_of(p, (int)(p.st->params.sweep & 1ull));
+  const int c0 = (blockIdx.x * kOrderThreads + tid) * kOrderPerThread;
+  int bin[kOrderPerThread], at[kOrderPerThread];
+#pragma unroll
+  for (int k = 0; k < kOrderPerThread; k++) {
+    bin[k] = order_bin(cnt, c0 + k, ncell, nc0, nc1);
+    at[k] = bin[k] >= 0 ? atomicAdd(&h[bin[k]], 1) : 0;
+  }
+  __syncthreads();
+  if (h[tid]) {
+    // bin tid = colour * 32 + n - 1 starts after the colour's cells holding more than n
+    int first = 0;
+    for (int m = (tid & 31) + 1; m < 32; m++) first += tot[(tid & ~31) + m];
+    start[tid] = first + atomicAdd(&p.ocnt[256 + tid], h[tid]);
+  }
+  __syncthreads();
+  const int stride = p.ncell_alloc / 8;
+#pragma unroll
+  for (int k = 0; k < kOrderPerThread; k++)
+    if (bin[k] >= 0) p.olist[(bin[k] >> 5) * stride + start[bin[k]] + at[k]] = c0 + k;
+}
 
 // One step of the reference's optimiser after sample j of the sampling loop
 // (opt_nvt src/optimizer.c:23-64, opt_npt :83-148, opt_cavity_nvt :172-212):
@@ -327,6 +414,23 @@ void launch_build(const SysPtrs &p, long long sweep_offset, int num_sms, cudaStr
   (void)num_sms;
   const int blocks = (p.n + 255) / 256;
   k_build<false><<<blocks > 0 ? blocks : 1, 256, 0, s>>>(p, nullptr, nullptr, 0, sweep_offset);
+}
+
+// Both order kernels are programmatic dependents (each waits at its start
+// for the kernel before it), so their launches overlap that kernel's end.
+void launch_order(const SysPtrs &p, cudaStream_t s) {
+  const int cells_per_block = kOrderThreads * kOrderPerThread;
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = dim3((unsigned)((p.ncell_alloc + cells_per_block - 1) / cells_per_block));
+  cfg.blockDim = dim3(kOrderThreads);
+  cfg.stream = s;
+  cudaLaunchAttribute attr[1];
+  attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+  attr[0].val.programmaticStreamSerializationAllowed = 1;
+  cfg.attrs = attr;
+  cfg.numAttrs = 1;
+  cudaLaunchKernelEx(&cfg, k_order_count, p);
+  cudaLaunchKernelEx(&cfg, k_order_scatter, p);
 }
 
 void launch_build_batch(const SysPtrs *reps, const int *nstart, int n_reps, int tot_n, long long sweep_offset,

@@ -358,7 +358,8 @@ class HardSphereSystem:
 
     def set_schedule(self, schedule: int, lanes_per_cell: int = 0) -> None:
         """0: one launch per colour pass; 1: dataflow sweep; 2: every sweep of
-        a call in one block (small NVT systems).  The same chain."""
+        a call in one block (small NVT systems); 3: one launch per colour
+        pass with the cells in occupancy order.  The same chain."""
         _check(self._lib.hsmc_gpu_set_schedule(self._h, schedule, lanes_per_cell), "hsmc_gpu_set_schedule")
 
     def get_schedule(self):

@@ -349,8 +349,11 @@ int hsmc_gpu_autotune(hsmc_ctx *ctx, int sweeps_per_variant, int *lanes_out);
  * to finish the previous pass; 2 = one block, every sweep of a call in one
  * launch with the system in shared memory (systems of up to a few thousand
  * spheres, NVT or NpT with its volume move per sweep; the default up to 128
- * active cells per pass, about 1000 spheres, where it is faster, else 0).
- * All give the same
+ * active cells per pass, about 1000 spheres, where it is faster); 3 = as 0,
+ * but each pass hands out its colour's non-empty cells fullest first, so a
+ * warp's cells hold the same number of spheres (two more launches per
+ * sweep; the default where a pass has more active cells than one wave of
+ * 2-lane groups, else 0).  All give the same
  * chain; hsmc_gpu_autotune picks the fastest.  lanes_per_cell 0 keeps the
  * current mapping (schedule 2 has none; it also runs a cavity run's cavity
  * stage).  Traced and profiled sweeps, and cavity runs recording their

@@ -230,6 +230,38 @@ def test_dataflow_schedule_is_the_pass_barrier_chain(gpu_lib, lanes):
     assert np.array_equal(confs[0][1], confs[1][1])
 
 
+@pytest.mark.parametrize("lanes", [1, 2, 4, 8])
+def test_occupancy_order_is_the_grid_order_chain(gpu_lib, lanes):
+    """The passes handing out each colour's cells fullest first (schedule 3)
+    give the chain of the grid order bit for bit: the cells of one colour are
+    independent and their random numbers are keyed by the cell."""
+    confs = []
+    for schedule in (0, 3):
+        s = gpu_lib.HardSphereSystem(rho=0.8, cells=8, dr_max=0.15, seed=42)
+        s.set_schedule(schedule, lanes)
+        assert s.get_schedule() == (schedule, lanes)
+        c = s.sweep_nvt(27)
+        confs.append((s.download(), c))
+    assert np.array_equal(confs[0][0], confs[1][0])
+    assert np.array_equal(confs[0][1], confs[1][1])
+
+
+def test_occupancy_order_npt_and_switches(gpu_lib):
+    """NpT sweeps (the grid is re-derived after a volume move) and switches
+    between the grid order and the occupancy order within one chain."""
+    finals = []
+    for plan in ((0, 0, 0), (3, 3, 3), (3, 0, 3)):
+        s = gpu_lib.HardSphereSystem(rho=0.7, cells=6, dr_max=0.15, pressure=6.0, dv_max=0.05, seed=9)
+        counts = []
+        for sch in plan:
+            s.set_schedule(sch, 2)
+            counts.append(s.sweep_npt(13).copy())
+        finals.append((s.download(), np.concatenate(counts)))
+    for conf, c in finals[1:]:
+        assert np.array_equal(conf, finals[0][0]) and np.array_equal(c, finals[0][1])
+    assert finals[0][1].reshape(3, -1)[:, 4].sum() > 0  # volume moves were accepted: the grid changed
+
+
 @pytest.mark.parametrize("rho,cells,lt,dr,seed,edge", [
     (0.80, 8, 2, 0.15, 42, 0.0),   # N = 2048 fluid
     (0.50, 7, 2, 0.30, 7, 0.0),    # N = 1372 at the C1 density

@@ -95,11 +95,16 @@ def test_adversarial_screen_decisions_at_large_coordinates(oracle_mod, gpu_lib, 
     g.close()
 
 
-@pytest.mark.parametrize("cfg,sweeps", [(C2, 2), (C5, 1)], ids=["N256k_L67", "N1M_L100"])
-def test_traced_full_size_sweeps_replay_bit_exact(oracle_mod, gpu_lib, cfg, sweeps):
+@pytest.mark.parametrize("cfg,sweeps,schedule", [(C2, 2, None), (C2, 1, 3), (C5, 1, None)],
+                         ids=["N256k_L67", "N256k_L67_occupancy_order", "N1M_L100"])
+def test_traced_full_size_sweeps_replay_bit_exact(oracle_mod, gpu_lib, cfg, sweeps, schedule):
     """Every trial of whole sweeps of the full system (512,000 trials at
-    N = 256,000; 1,048,576 at N = 1,048,576) replayed by the oracle."""
+    N = 256,000; 1,048,576 at N = 1,048,576) replayed by the oracle, at each
+    size's default schedule (the grid order at N = 256,000, the occupancy
+    order at N = 1,048,576) and with the occupancy order at N = 256,000."""
     o, g, _ = prepared(oracle_mod, gpu_lib, cfg, seed=23)
+    if schedule is not None:
+        g.set_schedule(schedule, 0)
     rec, cnt = g.sweeps_traced(sweeps)
     assert len(rec) == o.n * sweeps and cnt[0] == o.n * sweeps
     rec = rec[np.lexsort((rec[:, 2], rec[:, 1], rec[:, 0]))]
