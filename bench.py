@@ -394,16 +394,17 @@ def run_replicas(args):
     # every schedule, timed on the same live batch (the chain is the same for
     # all): reported beside the autotuner's choice
     variant_ms = {}
-    for sch, cb, tile in [(0, 4, 2), (2, 4, 2)] + [(1, c, t) for c in (1, 2, 4, 8) for t in (1, 2, 4, 8)]:
+    for sch, cb, tile in [(0, 4, 2), (3, 4, 2), (2, 4, 2)] + [(1, c, t) for c in (1, 2, 4, 8) for t in (1, 2, 4, 8)]:
         try:
             b.set_schedule(sch, cb, tile)
         except Exception:
             continue
         b.sweeps(8)
         b.sweeps(16)
-        name = {0: "flat", 2: "persistent grid"}.get(sch, f"persistent clusters cb={cb} tile={tile}")
+        name = {0: "flat", 3: "flat, occupancy order", 2: "persistent grid"}.get(
+            sch, f"persistent clusters cb={cb} tile={tile}")
         variant_ms[name] = b.last_timing() / 16
-    schedule = b.autotune(16)  # flat launches, the grid launch or clusters (cluster size and tile)
+    schedule = b.autotune(16)  # flat launches (either order), the grid launch or clusters (cluster size and tile)
     sweeps = args.sweeps
     per = 10
     nb, bin_ = 5, 0.01
@@ -445,6 +446,7 @@ def run_replicas(args):
                                f"{sweeps} sweeps after {args.equil}", "n_particles_total": n_tot,
                    "min_cell_edge": args.cell_edge,
                    "schedule": {0: "flat launches per colour pass, CUDA graphs of 8 sweeps",
+                                3: "flat launches per colour pass, cells in occupancy order, CUDA graphs of 8 sweeps",
                                 1: ("persistent: one launch of thread-block clusters per call, "
                                     f"{schedule[1]} blocks per cluster, tile {schedule[2]}"),
                                 2: "persistent: one cooperative launch over the device per call, "

@@ -138,7 +138,8 @@ class ReplicaBatch:
         sweep of a call in one persistent launch of thread-block clusters, one
         cluster per bundle of replicas; 2: every sweep of a call in one
         cooperative launch over the whole device per cell capacity, with grid
-        barriers between the phases.  The same chain."""
+        barriers between the phases; 3: the flat launches with each pass's
+        cells in occupancy order (fullest first).  The same chain."""
         _check(self._lib.hsmc_batch_set_schedule(self._h, schedule, cluster_blocks, tile),
                "hsmc_batch_set_schedule")
 
@@ -148,7 +149,7 @@ class ReplicaBatch:
         return tuple(int(x) for x in out)
 
     def autotune(self, sweeps_per_variant: int = 16):
-        """Times the three schedules (every cluster size and tile for schedule
+        """Times the four schedules (every cluster size and tile for schedule
         1); keeps the fastest and returns (schedule, cluster_blocks, tile)."""
         out = np.zeros(3, dtype=np.int32)
         _check(self._lib.hsmc_batch_autotune(self._h, sweeps_per_variant, out.ctypes.data), "hsmc_batch_autotune")

@@ -63,6 +63,10 @@ struct hsmc_batch {
     int cap = 8, group = 2, n = 0, tot_groups = 0;
     SysPtrs *d_reps = nullptr;
     int *d_gstart = nullptr, *d_ids = nullptr;
+    // schedule 3: prefix sums of the replicas' cells, the occupancy counts
+    // and one list per pass of (replica, cell) pairs
+    long long n_cells = 0;
+    int *d_cstart = nullptr, *d_ocnt = nullptr, *d_olist = nullptr;
   };
   std::vector<CapClass> classes;
   int max_n = 0, max_ncell = 0;
@@ -86,7 +90,8 @@ struct hsmc_batch {
   cudaEvent_t ev0 = nullptr, ev1 = nullptr;
   double last_ms = 0.0;
   // schedule 1: every sweep of a call in one launch of thread-block
-  // clusters, one cluster per bundle of replicas (batch_persist.cu)
+  // clusters, one cluster per bundle of replicas (batch_persist.cu);
+  // schedule 3: the flat launches with every pass's cells in occupancy order
   int schedule = 0;
   int cluster_blocks = 4, tile = 2;
   struct Bundles {
@@ -170,6 +175,9 @@ void hsmc_batch_destroy(hsmc_batch *b) {
     cudaFree(q.d_reps);
     cudaFree(q.d_ids);
     cudaFree(q.d_gstart);
+    cudaFree(q.d_cstart);
+    cudaFree(q.d_ocnt);
+    cudaFree(q.d_olist);
   }
   cudaFree(b->pos);
   for (int l = 0; l < 2; l++) {
@@ -310,12 +318,13 @@ int hsmc_batch_create(const hsmc_params *params, int n_systems, hsmc_batch **out
   }
   for (int c : {8, 16, 32}) {
     std::vector<SysPtrs> sp;
-    std::vector<int> ids, gs(1, 0);
+    std::vector<int> ids, gs(1, 0), cs(1, 0);
     for (int k = 0; k < n_systems; k++)
       if (caps[k] == c) {
         sp.push_back(b->sp[k]);
         ids.push_back(k);
         gs.push_back(gs.back() + b->hbox[k].ncell / 8);
+        cs.push_back(cs.back() + b->hbox[k].ncell);
       }
     if (sp.empty()) continue;
     hsmc_batch::CapClass cl;
@@ -323,14 +332,20 @@ int hsmc_batch_create(const hsmc_params *params, int n_systems, hsmc_batch **out
     cl.group = c / 4;
     cl.n = (int)sp.size();
     cl.tot_groups = gs.back();
+    cl.n_cells = cs.back();
     b->classes.push_back(cl);
     hsmc_batch::CapClass &q = b->classes.back();
     if ((ce = cudaMalloc(&q.d_reps, sizeof(SysPtrs) * q.n)) || (ce = cudaMalloc(&q.d_ids, sizeof(int) * q.n)) ||
-        (ce = cudaMalloc(&q.d_gstart, sizeof(int) * (q.n + 1))))
+        (ce = cudaMalloc(&q.d_gstart, sizeof(int) * (q.n + 1))) ||
+        (ce = cudaMalloc(&q.d_cstart, sizeof(int) * (q.n + 1))) ||
+        (ce = cudaMalloc(&q.d_ocnt, sizeof(int) * (size_t)kOrderWords)) ||
+        (ce = cudaMalloc(&q.d_olist, sizeof(int) * 2 * 8 * (size_t)q.tot_groups)))
       return fail(ce);
     if ((ce = cudaMemcpy(q.d_reps, sp.data(), sizeof(SysPtrs) * q.n, cudaMemcpyHostToDevice)) ||
         (ce = cudaMemcpy(q.d_ids, ids.data(), sizeof(int) * q.n, cudaMemcpyHostToDevice)) ||
-        (ce = cudaMemcpy(q.d_gstart, gs.data(), sizeof(int) * (q.n + 1), cudaMemcpyHostToDevice)))
+        (ce = cudaMemcpy(q.d_gstart, gs.data(), sizeof(int) * (q.n + 1), cudaMemcpyHostToDevice)) ||
+        (ce = cudaMemcpy(q.d_cstart, cs.data(), sizeof(int) * (q.n + 1), cudaMemcpyHostToDevice)) ||
+        (ce = cudaMemset(q.d_ocnt, 0, sizeof(int) * (size_t)kOrderWords)))
       return fail(ce);
   }
   if ((ce = cudaEventCreate(&b->ev0)) != cudaSuccess) return fail(ce);
@@ -383,6 +398,10 @@ int hsmc_batch_set_steps(hsmc_batch *b, const double *dr_max) {
 
 static void enqueue_batch_sweep(hsmc_batch *b, long long offset) {
   launch_build_batch(b->d_reps, b->d_nstart, b->reps, b->tot_n, offset, b->stream);
+  const bool ordered = b->schedule == 3;
+  if (ordered)
+    for (const hsmc_batch::CapClass &cl : b->classes)
+      launch_order_batch(cl.d_reps, cl.d_cstart, cl.n, cl.n_cells, cl.d_ocnt, cl.d_olist, cl.tot_groups, b->stream);
   for (int k = 0; k < 8; k++)
     for (size_t q = 0; q < b->classes.size(); q++) {
       const hsmc_batch::CapClass &cl = b->classes[q];
@@ -390,7 +409,7 @@ static void enqueue_batch_sweep(hsmc_batch *b, long long offset) {
       const bool clear = q == 0;
       launch_move_pass_batch(cl.d_reps, cl.d_gstart, cl.d_ids, cl.n, cl.tot_groups, cl.cap, k, cl.group,
                              clear ? b->cnt[0] : nullptr, clear ? b->cnt[1] : nullptr, clear ? b->tot_cell : 0,
-                             b->stream);
+                             ordered ? cl.d_olist : nullptr, ordered ? cl.d_ocnt : nullptr, b->stream);
     }
 }
 
@@ -548,7 +567,7 @@ static int build_grids(hsmc_batch *b) {
 }
 
 int hsmc_batch_set_schedule(hsmc_batch *b, int schedule, int cluster_blocks, int tile) {
-  if (!b || schedule < 0 || schedule > 2) return HSMC_ERR_INVALID_ARG;
+  if (!b || schedule < 0 || schedule > 3) return HSMC_ERR_INVALID_ARG;
   if (schedule == 2) {
     int dev = 0, coop = 0;
     BATCH_CUDA(cudaGetDevice(&dev));
@@ -572,6 +591,11 @@ int hsmc_batch_set_schedule(hsmc_batch *b, int schedule, int cluster_blocks, int
     if (cluster_blocks != b->cluster_blocks || tile != b->tile) free_bundles(b);
     b->cluster_blocks = cluster_blocks;
     b->tile = tile;
+  }
+  if ((schedule == 3) != (b->schedule == 3) && b->graph) {  // the flat launches' graph follows the order
+    BATCH_CUDA(cudaStreamSynchronize(b->stream));
+    cudaGraphExecDestroy(b->graph);
+    b->graph = nullptr;
   }
   b->schedule = schedule;
   return HSMC_OK;
@@ -668,7 +692,7 @@ int hsmc_batch_autotune(hsmc_batch *b, int sweeps_per_variant, int out[3]) {
   struct V {
     int s, cb, tile;
   };
-  std::vector<V> vs{{0, b->cluster_blocks, b->tile}, {2, b->cluster_blocks, b->tile}};
+  std::vector<V> vs{{0, b->cluster_blocks, b->tile}, {3, b->cluster_blocks, b->tile}, {2, b->cluster_blocks, b->tile}};
   for (int cb : {1, 2, 4, 8})
     for (int tile : {1, 2, 4}) vs.push_back({1, cb, tile});
   V best = vs[0];
@@ -686,7 +710,7 @@ int hsmc_batch_autotune(hsmc_batch *b, int sweeps_per_variant, int out[3]) {
   int e = hsmc_batch_set_schedule(b, best.s, best.cb, best.tile);
   if (e) return e;
   if (best.s != 1 && (b->cluster_blocks != best.cb || b->tile != best.tile)) {
-    // the flat or grid launches won: keep the cluster shape the batch had before
+    // the flat or grid launches won (either order): keep the cluster shape the batch had before
     free_bundles(b);
     b->cluster_blocks = best.cb;
     b->tile = best.tile;

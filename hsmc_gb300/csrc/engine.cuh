@@ -140,6 +140,12 @@ void launch_build(const SysPtrs &p, long long sweep_offset, int num_sms, cudaStr
 // After a sweep's build: each colour's non-empty cells listed fullest first
 // (SysPtrs::olist), which the colour passes hand out to their warps.
 void launch_order(const SysPtrs &p, cudaStream_t s);
+// The same for the replicas of one cell capacity of a batch: a list per pass
+// of (replica within the class, cell) pairs (olist, 2 ints each, stride
+// entries per pass), counts in ocnt (kOrderWords ints); cstart: prefix sums
+// of the replicas' cells, n_cells their total.
+void launch_order_batch(const SysPtrs *reps, const int *cstart, int n_reps, long long n_cells, int *ocnt,
+                        int *olist, int stride, cudaStream_t s);
 // Flags an uploaded configuration whose ids are not 0..N-1 (ST_BAD_ID) or
 // with a coordinate outside [0, L] (ST_OUT_OF_BOX; NaN included).
 void launch_check_config(const SysPtrs &p, cudaStream_t s);
@@ -165,10 +171,11 @@ void launch_build_batch(const SysPtrs *reps, const int *nstart, int n_reps, int 
                         cudaStream_t s);
 // one launch per cell capacity: reps / gstart / ids over the replicas of
 // that capacity (ids: their index in the batch); pools non-null clears the
-// other layout of the pooled counts on pass 0
+// other layout of the pooled counts on pass 0; olist / ocnt non-null: the
+// class's occupancy lists (launch_order_batch), which the pass follows
 void launch_move_pass_batch(const SysPtrs *reps, const int *gstart, const int *ids, int n_reps, int tot_groups,
                             int cap, int pass, int group, int *cnt_pool0, int *cnt_pool1, long long pool_cells,
-                            cudaStream_t s);
+                            int *olist, int *ocnt, cudaStream_t s);
 void launch_advance_batch(const SysPtrs *reps, int n_reps, int n_sweeps, cudaStream_t s);
 void launch_pair_hist_batch(const SysPtrs *reps, int n_reps, int max_n, double bin, double rmax, int nbins,
                             unsigned long long *counts, cudaStream_t s);

@@ -133,35 +133,76 @@ __global__ void __launch_bounds__(128, PassSmem<G, CAP>::min_blocks)
          c += (long long)gridDim.x * blockDim.x)
       other[c] = 0;
   }
-  int r = -1;
-  if (group < __ldg(gstart + n_reps)) {
-    r = find_rep(gstart, n_reps, group);
+  // One cell of replica r (within the class) by this lane group.
+  auto move_rep_cell = [&](int r, int ac_or_cell, bool listed, PassTally &tt) {
     const SysPtrs p = reps[r];
     const unsigned long long sweep = p.st->params.sweep;
     PassEnv e = pass_env(p, (uint32_t)__ldg(rep_ids + r), (int)(sweep & 1ull));
     e.seq = sweep * 8ull + (unsigned long long)pass;
-    const int colour = p.st->params.perm[pass];
-    const int hx = e.nc[0] >> 1, hy = e.nc[1] >> 1;
-    const int ac = group - __ldg(gstart + r);
-    const int ax = ac % hx, ayz = ac / hx, ay = ayz % hy, az = ayz / hy;
+    int ix, iy, iz;
+    if (listed) {
+      const int c = ac_or_cell, iyz = c / e.nc[0];
+      ix = c - iyz * e.nc[0];
+      iy = iyz % e.nc[1];
+      iz = iyz / e.nc[1];
+    } else {
+      const int colour = p.st->params.perm[pass];
+      const int hx = e.nc[0] >> 1, hy = e.nc[1] >> 1;
+      const int ac = ac_or_cell;
+      const int ax = ac % hx, ayz = ac / hx, ay = ayz % hy, az = ayz / hy;
+      ix = 2 * ax + (colour & 1);
+      iy = 2 * ay + ((colour >> 1) & 1);
+      iz = 2 * az + ((colour >> 2) & 1);
+    }
     bool no_wait = false;
-    move_cell<G, CAP, TRACE, false>(e, m, tid, lane, gl, col0, gmask, 2 * ax + (colour & 1),
-                                    2 * ay + ((colour >> 1) & 1), 2 * az + ((colour >> 2) & 1), t, no_wait);
+    move_cell<G, CAP, TRACE, false>(e, m, tid, lane, gl, col0, gmask, ix, iy, iz, tt, no_wait);
+  };
+  // The lanes of one replica sum their counters together (every lane of the
+  // warp takes part; r < 0: no replica).
+  auto add_rep_tally = [&](int r, const PassTally &tt) {
+    const cg::thread_block_tile<32> tile = cg::tiled_partition<32>(cg::this_thread_block());
+    const auto part = cg::labeled_partition(tile, r);
+    const unsigned a = cg::reduce(part, tt.acc, cg::plus<unsigned>());
+    const unsigned o = cg::reduce(part, tt.rej_o, cg::plus<unsigned>());
+    const unsigned bnd = cg::reduce(part, tt.rej_b, cg::plus<unsigned>());
+    const unsigned rc = cg::reduce(part, tt.rechecks, cg::plus<unsigned>());
+    if (r >= 0 && part.thread_rank() == 0) {
+      DevState *ws = reps[r].st;
+      if (a) atomicAdd(&ws->acc, (unsigned long long)a);
+      if (o) atomicAdd(&ws->rej_overlap, (unsigned long long)o);
+      if (bnd) atomicAdd(&ws->rej_boundary, (unsigned long long)bnd);
+      if (rc) atomicAdd(&ws->rechecks, (unsigned long long)rc);
+    }
+  };
+  if (p1.olist != nullptr) {
+    // Occupancy order (batch schedule 3): list `pass` holds the (replica,
+    // cell) pairs of every replica's cells that move in this pass, fullest
+    // first (k_border_scatter); runs of one cell per lane group of a warp,
+    // run j to block j mod grid, as in a single system's occupancy order.
+    constexpr int GPW = 32 / G;
+    const int total = p1.ocnt[512 + pass];
+    const int *list = p1.olist + 2 * (size_t)pass * (size_t)p1.ncell_alloc;
+    const int nwb = (int)blockDim.x >> 5;
+    const int stride = (int)gridDim.x * nwb * GPW;
+    for (int a = ((int)blockIdx.x + (int)gridDim.x * (tid >> 5)) * GPW + (tid & 31) / G;
+         __any_sync(0xffffffffu, a < total); a += stride) {
+      __syncwarp();  // the previous cell's records are no longer read
+      int r = -1;
+      PassTally tt;
+      if (a < total) {
+        r = list[2 * (size_t)a];
+        move_rep_cell(r, list[2 * (size_t)a + 1], true, tt);
+      }
+      add_rep_tally(r, tt);
+    }
+    return;
   }
-  // the lanes of one replica sum their counters together
-  const cg::thread_block_tile<32> tile = cg::tiled_partition<32>(cg::this_thread_block());
-  const auto part = cg::labeled_partition(tile, r);
-  const unsigned a = cg::reduce(part, t.acc, cg::plus<unsigned>());
-  const unsigned o = cg::reduce(part, t.rej_o, cg::plus<unsigned>());
-  const unsigned bnd = cg::reduce(part, t.rej_b, cg::plus<unsigned>());
-  const unsigned rc = cg::reduce(part, t.rechecks, cg::plus<unsigned>());
-  if (r >= 0 && part.thread_rank() == 0) {
-    DevState *ws = reps[r].st;
-    if (a) atomicAdd(&ws->acc, (unsigned long long)a);
-    if (o) atomicAdd(&ws->rej_overlap, (unsigned long long)o);
-    if (bnd) atomicAdd(&ws->rej_boundary, (unsigned long long)bnd);
-    if (rc) atomicAdd(&ws->rechecks, (unsigned long long)rc);
+  int r = -1;
+  if (group < __ldg(gstart + n_reps)) {
+    r = find_rep(gstart, n_reps, group);
+    move_rep_cell(r, group - __ldg(gstart + r), false, t);
   }
+  add_rep_tally(r, t);
 }
 
 // All eight passes of a sweep in one cooperative launch, without barriers
@@ -403,21 +444,26 @@ static void launch_gc(const SysPtrs &p, int pass, bool trace, int grid, cudaStre
 
 template <int G, int CAP>
 static void launch_batch_gc(const SysPtrs *reps, const int *gstart, const int *ids, int n_reps, int tot_groups,
-                            int pass, int *pool0, int *pool1, long long pool_cells, cudaStream_t s) {
+                            int pass, int *pool0, int *pool1, long long pool_cells, const SysPtrs &order,
+                            cudaStream_t s) {
   const long long threads = (long long)tot_groups * G;
   const int grid = (int)((threads + 127) / 128);
   k_move_pass<G, CAP, false, true><<<grid > 0 ? grid : 1, 128, pass_smem<G, CAP>(), s>>>(
-      SysPtrs{}, reps, gstart, ids, n_reps, pass, pool0, pool1, pool_cells);
+      order, reps, gstart, ids, n_reps, pass, pool0, pool1, pool_cells);
 }
 
 void launch_move_pass_batch(const SysPtrs *reps, const int *gstart, const int *ids, int n_reps, int tot_groups,
                             int cap, int pass, int group, int *cnt_pool0, int *cnt_pool1, long long pool_cells,
-                            cudaStream_t s) {
+                            int *olist, int *ocnt, cudaStream_t s) {
+  SysPtrs order{};  // the occupancy lists of the class (olist null: grid order)
+  order.olist = olist;
+  order.ocnt = ocnt;
+  order.ncell_alloc = tot_groups;  // entries per pass list
 #define HSMC_BATCH_CAP(G)                                                                                  \
   switch (cap) {                                                                                           \
-    case 8: launch_batch_gc<G, 8>(reps, gstart, ids, n_reps, tot_groups, pass, cnt_pool0, cnt_pool1, pool_cells, s); break; \
-    case 16: launch_batch_gc<G, 16>(reps, gstart, ids, n_reps, tot_groups, pass, cnt_pool0, cnt_pool1, pool_cells, s); break; \
-    default: launch_batch_gc<G, 32>(reps, gstart, ids, n_reps, tot_groups, pass, cnt_pool0, cnt_pool1, pool_cells, s); break; \
+    case 8: launch_batch_gc<G, 8>(reps, gstart, ids, n_reps, tot_groups, pass, cnt_pool0, cnt_pool1, pool_cells, order, s); break; \
+    case 16: launch_batch_gc<G, 16>(reps, gstart, ids, n_reps, tot_groups, pass, cnt_pool0, cnt_pool1, pool_cells, order, s); break; \
+    default: launch_batch_gc<G, 32>(reps, gstart, ids, n_reps, tot_groups, pass, cnt_pool0, cnt_pool1, pool_cells, order, s); break; \
   }
   switch (group) {
     case 1: HSMC_BATCH_CAP(1) break;

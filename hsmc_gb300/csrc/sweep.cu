@@ -416,6 +416,91 @@ void launch_build(const SysPtrs &p, long long sweep_offset, int num_sms, cudaStr
   k_build<false><<<blocks > 0 ? blocks : 1, 256, 0, s>>>(p, nullptr, nullptr, 0, sweep_offset);
 }
 
+// Batched replicas (hsmc_batch schedule 3): one list per pass over every
+// replica of one cell capacity.  A replica's cells of the colour that its
+// own colour order moves in pass k go to list k as (replica within the
+// class, cell) pairs, fullest first; bins are pass * 32 + occupancy - 1.
+// cstart: prefix sums of the class's replicas' cells.  The counts (ocnt, the
+// words of SysPtrs::ocnt) are cleared before k_border_count.
+__device__ __forceinline__ int batch_order_bin(const SysPtrs *reps, const int *cstart, int n_reps, int x, int &r,
+                                               int &c) {
+  if (x >= __ldg(cstart + n_reps)) return -1;
+  r = find_rep(cstart, n_reps, x);
+  c = x - __ldg(cstart + r);
+  const DevState *st = reps[r].st;
+  const int layout = (int)(st->params.sweep & 1ull);
+  const int n = (layout ? reps[r].cnt[1] : reps[r].cnt[0])[c];
+  if (n <= 0) return -1;
+  const Box *bx = reps[r].box;
+  const int nc0 = bx->nc[0], nc1 = bx->nc[1];
+  const int iyz = c / nc0;
+  const int colour = cell_colour(c - iyz * nc0, iyz % nc1, iyz / nc1);
+  int k = 0;
+  while (k < 7 && st->params.perm[k] != colour) k++;
+  return 32 * k + (n < 32 ? n : 32) - 1;
+}
+
+__global__ void __launch_bounds__(kOrderThreads) k_border_count(const SysPtrs *reps, const int *cstart, int n_reps,
+                                                                int *ocnt) {
+  __shared__ int h[256];
+  const int tid = (int)threadIdx.x;
+  h[tid] = 0;
+  __syncthreads();
+  const int x0 = (blockIdx.x * kOrderThreads + tid) * kOrderPerThread;
+#pragma unroll
+  for (int k = 0; k < kOrderPerThread; k++) {
+    int r, c;
+    const int b = batch_order_bin(reps, cstart, n_reps, x0 + k, r, c);
+    if (b >= 0) atomicAdd(&h[b], 1);
+  }
+  __syncthreads();
+  if (h[tid]) atomicAdd(&ocnt[tid], h[tid]);
+}
+
+__global__ void __launch_bounds__(kOrderThreads) k_border_scatter(const SysPtrs *reps, const int *cstart, int n_reps,
+                                                                  int *ocnt, int *olist, int stride) {
+  __shared__ int h[256], tot[256], start[256];
+  const int tid = (int)threadIdx.x;
+  h[tid] = 0;
+  tot[tid] = ocnt[tid];
+  __syncthreads();
+  if (blockIdx.x == 0 && tid < 8) {
+    int t = 0;
+    for (int m = 0; m < 32; m++) t += tot[32 * tid + m];
+    ocnt[512 + tid] = t;
+  }
+  const int x0 = (blockIdx.x * kOrderThreads + tid) * kOrderPerThread;
+  int bin[kOrderPerThread], at[kOrderPerThread], rr[kOrderPerThread], cc[kOrderPerThread];
+#pragma unroll
+  for (int k = 0; k < kOrderPerThread; k++) {
+    bin[k] = batch_order_bin(reps, cstart, n_reps, x0 + k, rr[k], cc[k]);
+    at[k] = bin[k] >= 0 ? atomicAdd(&h[bin[k]], 1) : 0;
+  }
+  __syncthreads();
+  if (h[tid]) {
+    int first = 0;
+    for (int m = (tid & 31) + 1; m < 32; m++) first += tot[(tid & ~31) + m];
+    start[tid] = first + atomicAdd(&ocnt[256 + tid], h[tid]);
+  }
+  __syncthreads();
+#pragma unroll
+  for (int k = 0; k < kOrderPerThread; k++)
+    if (bin[k] >= 0) {
+      const size_t e = (size_t)(bin[k] >> 5) * (size_t)stride + (size_t)(start[bin[k]] + at[k]);
+      olist[2 * e] = rr[k];
+      olist[2 * e + 1] = cc[k];
+    }
+}
+
+void launch_order_batch(const SysPtrs *reps, const int *cstart, int n_reps, long long n_cells, int *ocnt,
+                        int *olist, int stride, cudaStream_t s) {
+  const long long per_block = kOrderThreads * kOrderPerThread;
+  const int blocks = (int)((n_cells + per_block - 1) / per_block);
+  cudaMemsetAsync(ocnt, 0, sizeof(int) * (size_t)kOrderWords, s);
+  k_border_count<<<blocks > 0 ? blocks : 1, kOrderThreads, 0, s>>>(reps, cstart, n_reps, ocnt);
+  k_border_scatter<<<blocks > 0 ? blocks : 1, kOrderThreads, 0, s>>>(reps, cstart, n_reps, ocnt, olist, stride);
+}
+
 // Both order kernels are programmatic dependents (each waits at its start
 // for the kernel before it), so their launches overlap that kernel's end.
 void launch_order(const SysPtrs &p, cudaStream_t s) {

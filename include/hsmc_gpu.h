@@ -293,8 +293,12 @@ int hsmc_batch_last_timing(hsmc_batch *b, double *total_ms);
  * launch (per cell capacity) of every block the device holds: each sweep's
  * cell build and eight colour passes over all the replicas' cells, separated
  * by grid-wide barriers whose waits give up after 1 s (HSMC_ERR_TIMEOUT);
- * cluster_blocks and tile are kept but not used.  The chain is the same in
- * all three (sweep_nvt, src/nvt.c:201-209, per replica).
+ * cluster_blocks and tile are kept but not used.  3: the flat launches of 0,
+ * with each pass's cells (over every replica of a cell capacity) listed
+ * fullest first after the build, so a warp's cells hold the same number of
+ * spheres and empty cells take no lanes (two more launches per capacity and
+ * sweep).  The chain is the same in all four (sweep_nvt, src/nvt.c:201-209,
+ * per replica).
  * HSMC_ERR_INVALID_ARG for a cluster shape the device cannot hold, or a
  * device without cooperative launches.  get_schedule: out = {schedule,
  * cluster_blocks, tile}. */

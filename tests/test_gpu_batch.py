@@ -150,6 +150,30 @@ def test_grid_schedule_is_the_flat_chain(gpu_lib):
     _persistent_vs_flat(mixed, [9], [(4, 2)], min_cell_edge="auto", schedule=2)
 
 
+def test_occupancy_order_is_the_flat_chain(gpu_lib):
+    """The flat launches with each pass's cells over every replica listed
+    fullest first (schedule 3): every replica's configuration and counters
+    bit-identical to the grid-order flat launches', over calls of 1, 7 and 16
+    sweeps, with 16- and 32-slot cells in the same batch, and replica 0
+    against a single context with switches between the orders."""
+    rng = np.random.default_rng(13)
+    systems = [(float(rng.uniform(0.3, 0.94)), int(rng.integers(3, 9)), 0.12, 700 + k) for k in range(40)]
+    _persistent_vs_flat(systems, [1, 7, 16], [(4, 2)], schedule=3)
+    mixed = [(0.45, 6, 0.3, 5), (0.80, 6, 0.15, 6), (0.30, 7, 0.4, 7), (0.60, 5, 0.25, 8)]
+    _persistent_vs_flat(mixed, [9], [(4, 2)], min_cell_edge="auto", schedule=3)
+    from hsmc_gb300.batch import ReplicaBatch
+
+    b = ReplicaBatch([(0.80, 6, 0.15, 77), (0.50, 4, 0.30, 78)])
+    s = gpu_lib.HardSphereSystem(rho=0.80, cells=6, dr_max=0.15, seed=77)
+    for sch, n in ((3, 11), (0, 5), (3, 8)):
+        b.set_schedule(sch)
+        c = b.sweeps(n)
+        cs = s.sweep_nvt(n)
+        assert np.array_equal(b.download(0), s.download()) and np.array_equal(c[0], cs), sch
+    b.close()
+    s.close()
+
+
 def test_grid_schedule_replica_zero_and_observables(gpu_lib):
     """Replica 0 under the grid schedule is the single context's chain, the
     layout it leaves serves the observables, and the flat launches continue
@@ -210,13 +234,13 @@ def test_batch_autotune_keeps_the_chain(gpu_lib):
     systems = [(0.7, 5, 0.2, 40 + k) for k in range(6)]
     a = ReplicaBatch(systems)
     sched = a.autotune(8)
-    assert sched[0] in (0, 1) and sched[1] in (1, 2, 4, 8) and sched[2] in (1, 2, 4)
+    assert sched[0] in (0, 1, 2, 3) and sched[1] in (1, 2, 4, 8) and sched[2] in (1, 2, 4)
     assert a.get_schedule() == sched
     a.sweeps(10)
-    # the same tuning sweeps, then the other schedule: the same chain
+    # the same tuning sweeps, then another schedule: the same chain
     b = ReplicaBatch(systems)
     b.autotune(8)
-    b.set_schedule(1 - sched[0], 2, 2)
+    b.set_schedule(1 if sched[0] != 1 else 0, 2, 2)
     b.sweeps(10)
     for k in range(len(systems)):
         assert np.array_equal(a.download(k), b.download(k))
