@@ -422,22 +422,44 @@ void launch_build(const SysPtrs &p, long long sweep_offset, int num_sms, cudaStr
 // class, cell) pairs, fullest first; bins are pass * 32 + occupancy - 1.
 // cstart: prefix sums of the class's replicas' cells.  The counts (ocnt, the
 // words of SysPtrs::ocnt) are cleared before k_border_count.
-__device__ __forceinline__ int batch_order_bin(const SysPtrs *reps, const int *cstart, int n_reps, int x, int &r,
-                                               int &c) {
-  if (x >= __ldg(cstart + n_reps)) return -1;
-  r = find_rep(cstart, n_reps, x);
-  c = x - __ldg(cstart + r);
-  const DevState *st = reps[r].st;
-  const int layout = (int)(st->params.sweep & 1ull);
-  const int n = (layout ? reps[r].cnt[1] : reps[r].cnt[0])[c];
+//
+// What a thread needs of the replica holding its cells: the replica's end
+// in the class's cell numbering, its current counts and grid, and the pass
+// that moves each colour (4 bits per colour).  A thread's cells are
+// consecutive, so it looks a replica up once, and again only when its cells
+// cross into the next one.
+struct OrderRep {
+  int r = -1, first = 0, end = 0, nc0 = 1, nc1 = 1;
+  const int *cnt = nullptr;
+  uint32_t pass_of = 0;
+};
+
+__device__ __forceinline__ void order_rep(const SysPtrs *reps, const int *cstart, int n_reps, int x, OrderRep &v) {
+  v.r = find_rep(cstart, n_reps, x);
+  v.first = __ldg(cstart + v.r);
+  v.end = __ldg(cstart + v.r + 1);
+  const DevState *st = reps[v.r].st;
+  v.cnt = (st->params.sweep & 1ull) ? reps[v.r].cnt[1] : reps[v.r].cnt[0];
+  v.nc0 = reps[v.r].box->nc[0];
+  v.nc1 = reps[v.r].box->nc[1];
+  v.pass_of = 0;
+#pragma unroll
+  for (int k = 0; k < 8; k++) v.pass_of |= (uint32_t)k << (4 * st->params.perm[k]);
+}
+
+// Bin of flat cell x of the class (pass * 32 + min(n, 32) - 1), or -1 for an
+// empty cell or one beyond the class; r and c: its replica and cell.
+__device__ __forceinline__ int batch_order_bin(const SysPtrs *reps, const int *cstart, int n_reps, int n_cells, int x,
+                                               OrderRep &v, int &r, int &c) {
+  if (x >= n_cells) return -1;
+  if (v.r < 0 || x >= v.end) order_rep(reps, cstart, n_reps, x, v);
+  r = v.r;
+  c = x - v.first;
+  const int n = v.cnt[c];
   if (n <= 0) return -1;
-  const Box *bx = reps[r].box;
-  const int nc0 = bx->nc[0], nc1 = bx->nc[1];
-  const int iyz = c / nc0;
-  const int colour = cell_colour(c - iyz * nc0, iyz % nc1, iyz / nc1);
-  int k = 0;
-  while (k < 7 && st->params.perm[k] != colour) k++;
-  return 32 * k + (n < 32 ? n : 32) - 1;
+  const int iyz = c / v.nc0;
+  const int colour = cell_colour(c - iyz * v.nc0, iyz % v.nc1, iyz / v.nc1);
+  return 32 * (int)((v.pass_of >> (4 * colour)) & 7u) + (n < 32 ? n : 32) - 1;
 }
 
 __global__ void __launch_bounds__(kOrderThreads) k_border_count(const SysPtrs *reps, const int *cstart, int n_reps,
@@ -446,11 +468,13 @@ __global__ void __launch_bounds__(kOrderThreads) k_border_count(const SysPtrs *r
   const int tid = (int)threadIdx.x;
   h[tid] = 0;
   __syncthreads();
+  const int n_cells = __ldg(cstart + n_reps);
   const int x0 = (blockIdx.x * kOrderThreads + tid) * kOrderPerThread;
+  OrderRep v;
 #pragma unroll
   for (int k = 0; k < kOrderPerThread; k++) {
     int r, c;
-    const int b = batch_order_bin(reps, cstart, n_reps, x0 + k, r, c);
+    const int b = batch_order_bin(reps, cstart, n_reps, n_cells, x0 + k, v, r, c);
     if (b >= 0) atomicAdd(&h[b], 1);
   }
   __syncthreads();
@@ -469,11 +493,13 @@ __global__ void __launch_bounds__(kOrderThreads) k_border_scatter(const SysPtrs 
     for (int m = 0; m < 32; m++) t += tot[32 * tid + m];
     ocnt[512 + tid] = t;
   }
+  const int n_cells = __ldg(cstart + n_reps);
   const int x0 = (blockIdx.x * kOrderThreads + tid) * kOrderPerThread;
+  OrderRep v;
   int bin[kOrderPerThread], at[kOrderPerThread], rr[kOrderPerThread], cc[kOrderPerThread];
 #pragma unroll
   for (int k = 0; k < kOrderPerThread; k++) {
-    bin[k] = batch_order_bin(reps, cstart, n_reps, x0 + k, rr[k], cc[k]);
+    bin[k] = batch_order_bin(reps, cstart, n_reps, n_cells, x0 + k, v, rr[k], cc[k]);
     at[k] = bin[k] >= 0 ? atomicAdd(&h[bin[k]], 1) : 0;
   }
   __syncthreads();
