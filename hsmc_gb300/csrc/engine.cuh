@@ -87,6 +87,22 @@ __device__ __forceinline__ void vol_proposal(double vol, uint32_t r, double dv_m
   sf = pow(ratio, 1. / 3.);
 }
 
+// Whether the overlap scan of a volume move can be skipped: an expansion
+// (sf > 1) scales every component of every pair's distance up, so it finds
+// an overlap only where the configuration already holds a pair short of
+// contact.  The chain itself leaves such pairs behind only as rounding: the
+// rescale of an accepted volume move (x sf, and the box rebuilt from the
+// density) can put a pair within a few ulp(L) below contact, where the
+// reference's next scan, at a scale factor that close to 1, reports an
+// overlap.  So the scan is skipped only for sf >= 1 + 2^-46 (L + 1), L the
+// longest side (about 1e-12 at L = 100, far above that rounding); an
+// expansion closer to 1, or sf = 1, is scanned.
+__device__ __forceinline__ bool vol_scan_needed(double sf, const double len[3]) {
+  double lmax = len[0] > len[1] ? len[0] : len[1];
+  lmax = len[2] > lmax ? len[2] : lmax;
+  return !(sf >= 1.0 + 1.4210854715202004e-14 * (lmax + 1.0));
+}
+
 // The acceptance bound exp(beta P (V - V') + (N + 1) ln(V'/V)).
 __device__ __forceinline__ double vol_boltz(double pressure, double vol, double vol_new, int n, double ratio) {
   return exp(__dadd_rn(__dmul_rn(pressure, __dsub_rn(vol, vol_new)), __dmul_rn((double)(n + 1), log(ratio))));

@@ -269,14 +269,14 @@ __global__ void k_vol_propose(SysPtrs p, long long offset) {
   st->vol_moves += 1;
 }
 
-// check_overlap(i, sf, sf, sf) for every i (src/moves.c:104-112).  A scale
-// factor >= 1 cannot bring a pair closer than it is, so nothing runs then.
+// check_overlap(i, sf, sf, sf) for every i (src/moves.c:104-112); an
+// expansion clear of 1 needs no scan (vol_scan_needed).
 __global__ void __launch_bounds__(256) k_vol_scan(SysPtrs p) {
   const DevState *st = p.st;
   const double sf = st->vol_sf;
-  if (!(sf < 1.0)) return;
-  if (*(volatile const int *)&st->vol_overlap) return;
   const Box *bx = p.box;
+  if (!vol_scan_needed(sf, bx->len)) return;
+  if (*(volatile const int *)&st->vol_overlap) return;
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= p.n) return;
   const int layout = (int)(st->params.sweep & 1ull);

@@ -388,7 +388,7 @@ __global__ void __launch_bounds__(1024) k_sweep_small(SysPtrs p, int n_sweeps, i
       }
       __syncthreads();
       const double sf = v_sf;
-      if (sf < 1.0) {  // a larger box cannot bring a pair closer
+      if (vol_scan_needed(sf, sb.len)) {  // an expansion clear of 1 is not scanned
         // check_overlap(i, sf, sf, sf) for every i (src/moves.c:104-112)
         const float reach = (float)(1.0 / sf) + 1e-3f;
         int k[3];

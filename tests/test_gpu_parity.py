@@ -136,6 +136,34 @@ def test_rdf_and_virial_counts_bit_exact(oracle_mod, gpu_lib, rho, n, seed, dr):
     assert np.array_equal(gpv, pv.astype(np.uint64))
 
 
+def test_volume_scan_near_unit_scale_factor(oracle_mod, gpu_lib):
+    """A pair 2^-51 short of contact, as the rescale of an accepted volume
+    move can leave one: the reference's scan reports an overlap at sf = 1
+    and at sf = 1 + 2^-52 (an expansion too small to clear the deficit) and
+    none once sf clears it; the device scan gives the same at every sf,
+    expansions included."""
+    o = oracle_mod.OracleSim(rho=0.5, n_cells=4, seed=1, dr_max=0.1)
+    L = o.box()["lx"]
+    s = L / 7
+    y0 = z0 = 3.5 * s
+    pts = [(2.0, y0, z0), (3.0 - 2.0**-51, y0, z0)]  # 1 - 2^-51 apart (both exact)
+    for k in range(7):
+        for j in range(7):
+            for i in range(7):
+                if not (j == 3 and k == 3 and i in (1, 2, 3)):
+                    pts.append(((i + 0.5) * s, (j + 0.5) * s, (k + 0.5) * s))
+    conf = np.zeros((o.n, 4))
+    conf[:, 0] = np.arange(o.n)
+    conf[:, 1:] = pts[: o.n]
+    o.set_config(conf)
+    g = gpu_lib.HardSphereSystem(rho=0.5, cells=4, dr_max=0.1, seed=1, conf=conf)
+    sfs = [0.999, 1.0 - 2.0**-52, 1.0, 1.0 + 2.0**-52, 1.0 + 2.0**-50, 1.0 + 1e-13, 1.0 + 1e-9, 1.001]
+    want = [o.scan_overlap(x) for x in sfs]
+    assert want[:4] == [1, 1, 1, 1] and want[4:] == [0, 0, 0, 0], want
+    assert [g.scan_overlap(x) for x in sfs] == want
+    g.close()
+
+
 @pytest.mark.parametrize("rho,n,seed,dr", CASES)
 def test_thermo_pressure_scan_bit_exact(oracle_mod, gpu_lib, rho, n, seed, dr):
     o, g, _ = fluid(oracle_mod, gpu_lib, rho, n, seed, dr)
