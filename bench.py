@@ -498,9 +498,16 @@ def run_widom(args):
     ok_l = n_learned = 0
     per_sample = []
     samples = 40
+    # the same estimator with a 0.7/0.3 mixture, drawn on the same states:
+    # a larger uniform share lowers the weight (1/alpha) of the rare successes
+    # the network misses
+    alt_alpha = 0.3
+    sw_a = sw2_a = t_a = 0.0
+    n_a = 0
     for _ in range(samples):
         s.sweep_nvt(20)
-        t_l += lw.refresh()
+        t_ref = lw.refresh()
+        t_l += t_ref
         st = lw.insert(ins, alpha=0.1)
         t_l += lw.last_ms()
         sw += st.sum_w
@@ -509,6 +516,11 @@ def run_widom(args):
         ok_l += st.n_ok
         n_learned += st.n_learned
         per_sample.append(st.sum_w / st.n)
+        st_a = lw.insert(ins, alpha=alt_alpha)
+        t_a += lw.last_ms() + t_ref
+        sw_a += st_a.sum_w
+        sw2_a += st_a.sum_w2
+        n_a += st_a.n
         ok_u += lw.uniform(ins)
         t_u += lw.last_ms()
         n_u += ins
@@ -517,6 +529,9 @@ def run_widom(args):
     var_u = p * (1 - p)  # Bernoulli variance of uniform Widom at the same p
     eff_l = 1.0 / (var_l * t_l / n_l)
     eff_u = 1.0 / (var_u * t_u / n_u)
+    p_a = sw_a / n_a
+    var_a = sw2_a / n_a - p_a * p_a
+    eff_a = 1.0 / (var_a * t_a / n_a)
     se_mu_l = math.sqrt(var_l / n_l) / p
     se_mu_u = math.sqrt(var_u / n_u) / p
     line = {
@@ -532,6 +547,9 @@ def run_widom(args):
                     "successes": ok_l, "learned_draws_success_over_p": (ok_l / max(n_learned, 1)) / p},
         "uniform": {"successes": ok_u, "insertions": n_u, "var_per_insertion_at_p": var_u, "gpu_ms": t_u,
                     "se_beta_mu_at_p": se_mu_u},
+        "learned_alpha_0.3": {"efficiency_ratio": eff_a / eff_u, "p_ins": p_a, "beta_mu_ex": -math.log(p_a),
+                              "var_per_insertion": var_a, "gpu_ms": t_a,
+                              "se_beta_mu": math.sqrt(var_a / n_a) / p_a},
         "training": {"kept_outcomes": int(log[-1][0]), "kept_successes": int(log[-1][1]),
                      "insertions_examined": 8 * 125_000_000, "gpu_ms": train_ms},
         "beta_mu_cs": (lambda e: (8 * e - 9 * e * e + 3 * e**3) / (1 - e) ** 3)(math.pi * 0.94 / 6),
