@@ -11,13 +11,16 @@
 // cell and trial, the particle of rank floor(u n) by id, the same FP64
 // proposal and confinement test, and overlap decisions that are the
 // reference's FP64 test (single precision decides only outside the guard
-// band).  A pass runs in rounds, round t making trial t of every active
-// cell that has one: one thread per cell draws and proposes (so one warp's
-// FP64 sequence serves 32 cells: GB300's FP64 pipe is busy per warp
-// instruction), then one warp per cell screens it, lane k on neighbour
-// cell k of the 27, and the cell's thread applies an accepted move at the
-// start of the next round.  A cell's trials stay in order; its neighbours
-// are of other colours, so no other cell writes what it reads.
+// band).  Up to 128 active cells per pass, a group of 32, 16, 8 or 4 lanes
+// per cell makes the cell's trials one after another and a pass has one
+// block barrier, at its end.  Above that a pass runs in rounds, round t
+// making trial t of every active cell that has one: one thread per cell
+// draws and proposes (so one warp's FP64 sequence serves 32 cells: GB300's
+// FP64 pipe is busy per warp instruction), then one warp per cell screens
+// it, lane k on neighbour cell k of the 27, and the cell's thread applies
+// an accepted move at the start of the next round.  Either way a cell's
+// trials stay in order; its neighbours are of other colours, so no other
+// cell writes what it reads.
 //
 // NpT sweeps add vol_move after the passes (src/moves.c:83-153): one thread
 // proposes, the block scans every particle's neighbourhood at the scaled
@@ -32,6 +35,11 @@
 namespace hsmc {
 
 namespace {
+
+// Threads of the block: 512 leave each 128 registers, which the lane groups'
+// trial loop needs without spilling; the rounds below take up to one active
+// cell per thread.
+constexpr int kSmallThreads = 512;
 
 struct SmallSweepSm {
   double *x, *y, *z;     // N positions
@@ -115,8 +123,102 @@ __device__ __forceinline__ double scale_wrap(double x, double sf, double len) {
   return v;
 }
 
+// One colour pass of up to 128 active cells by lane groups (gsz lanes per
+// cell), for k_sweep_small.
+__device__ __forceinline__ void small_pass_groups(const SmallSweepSm &m, const Box &sb, const float *sh_s, int colour,
+                                               unsigned long long seq, int gsz, int n_active, int cap, int frozen,
+                                               unsigned long long seed, double dr, unsigned &acc, unsigned &rej_o,
+                                               unsigned &rej_b) {
+  const int tid = (int)threadIdx.x, lane = tid & 31, wid = tid >> 5, nw = (int)blockDim.x >> 5;
+  const int nc[3] = {sb.nc[0], sb.nc[1], sb.nc[2]};
+  const int hx = nc[0] >> 1, hy = nc[1] >> 1;
+  const double len[3] = {sb.len[0], sb.len[1], sb.len[2]};
+  const double *half = sb.half;
+  const float L32[3] = {sb.len32[0], sb.len32[1], sb.len32[2]};
+  const float iw[3] = {sb.inv_w32[0], sb.inv_w32[1], sb.inv_w32[2]};
+  const float sh[3] = {sh_s[0], sh_s[1], sh_s[2]};
+  const float lo = 1.0f - sb.band, hi = 1.0f + sb.band;
+  const int gl = lane & (gsz - 1), gpw = 32 / gsz;
+  const unsigned gmask = gsz == 32 ? 0xffffffffu : (((1u << gsz) - 1u) << (lane - gl));
+  for (int a = wid * gpw + lane / gsz; a < n_active; a += nw * gpw) {  // the same in the group's lanes
+    const int ax = a % hx, ayz = a / hx, ay = ayz % hy, az = ayz / hy;
+    const int ix = 2 * ax + (colour & 1), iy = 2 * ay + ((colour >> 1) & 1), iz = 2 * az + ((colour >> 2) & 1);
+    const int c = ix + nc[0] * (iy + nc[1] * iz);
+    const int b = m.start[c];
+    int cn = m.start[c + 1] - b;
+    if (cn > cap) cn = 0;  // an overfull cell was flagged above
+    U32x4 dl = {0u, 0u, 0u, 0u};
+    if (gl < cn) dl = draw4(seed, (uint32_t)gl, (uint32_t)c, seq, TAG_MOVE);
+    for (int t = 0; t < cn; t++) {
+      U32x4 r;
+      if (t < gsz) {
+        r.x = __shfl_sync(gmask, dl.x, t, gsz);
+        r.y = __shfl_sync(gmask, dl.y, t, gsz);
+        r.z = __shfl_sync(gmask, dl.z, t, gsz);
+        r.w = __shfl_sync(gmask, dl.w, t, gsz);
+      } else {
+        r = draw4(seed, (uint32_t)t, (uint32_t)c, seq, TAG_MOVE);
+      }
+      const int id = m.ids[b + (int)__umulhi(r.x, (unsigned)cn)];
+      if (id < frozen) continue;  // a cavity is moved by the cavity stage
+      const int ag = gl < 3 ? gl : 2;  // this lane's axis
+      const double xa = ag == 0 ? m.x[id] : (ag == 1 ? m.y[id] : m.z[id]);
+      const double va = propose_axis(xa, centred_offset(ag == 0 ? r.y : (ag == 1 ? r.z : r.w)), dr,
+                                     ag == 0 ? len[0] : (ag == 1 ? len[1] : len[2]));
+      int ca;
+      float ua;
+      axis_cell(__double2float_rn(va), ag == 0 ? sh[0] : (ag == 1 ? sh[1] : sh[2]),
+                ag == 0 ? L32[0] : (ag == 1 ? L32[1] : L32[2]), ag == 0 ? iw[0] : (ag == 1 ? iw[1] : iw[2]),
+                ag == 0 ? nc[0] : (ag == 1 ? nc[1] : nc[2]), ca, ua);
+      const double nx = __shfl_sync(gmask, va, 0, gsz), ny = __shfl_sync(gmask, va, 1, gsz),
+                   nz = __shfl_sync(gmask, va, 2, gsz);
+      const float ux = __shfl_sync(gmask, ua, 0, gsz), uy = __shfl_sync(gmask, ua, 1, gsz),
+                  uz = __shfl_sync(gmask, ua, 2, gsz);
+      const int c0 = __shfl_sync(gmask, ca, 0, gsz), c1 = __shfl_sync(gmask, ca, 1, gsz),
+                c2 = __shfl_sync(gmask, ca, 2, gsz);
+      if (c0 != ix || c1 != iy || c2 != iz) {
+        if (gl == 0) rej_b++;  // the move would leave the active cell
+        continue;
+      }
+      bool ov = false;
+      for (int k = gl; k < 27 && !ov; k += gsz) {
+        int jx = ix + k % 3 - 1, jy = iy + (k / 3) % 3 - 1, jz = iz + k / 9 - 1;
+        float imx = 0.f, imy = 0.f, imz = 0.f;
+        if (jx < 0) { jx += nc[0]; imx = -L32[0]; } else if (jx >= nc[0]) { jx -= nc[0]; imx = L32[0]; }
+        if (jy < 0) { jy += nc[1]; imy = -L32[1]; } else if (jy >= nc[1]) { jy -= nc[1]; imy = L32[1]; }
+        if (jz < 0) { jz += nc[2]; imz = -L32[2]; } else if (jz >= nc[2]) { jz -= nc[2]; imz = L32[2]; }
+        const int nb = jx + nc[0] * (jy + nc[1] * jz);
+        const int qe = m.start[nb + 1];
+        for (int q = m.start[nb]; q < qe && !ov; q++) {
+          const int j = m.ids[q];
+          if (j == id) continue;
+          const float dx = ux - __fadd_rn(m.tx[j], imx), dy = uy - __fadd_rn(m.ty[j], imy),
+                      dz = uz - __fadd_rn(m.tz[j], imz);
+          const float r2 = dx * dx + dy * dy + dz * dz;
+          if (r2 < lo) ov = true;
+          else if (r2 <= hi) ov = ref_r2(nx, ny, nz, m.x[j], m.y[j], m.z[j], len, half) < 1.0;
+        }
+      }
+      if (__ballot_sync(gmask, ov) != 0u) {
+        if (gl == 0) rej_o++;
+      } else {
+        if (gl == 0) {
+          m.x[id] = nx;
+          m.y[id] = ny;
+          m.z[id] = nz;
+          m.tx[id] = ux;
+          m.ty[id] = uy;
+          m.tz[id] = uz;
+          acc++;
+        }
+        __syncwarp(gmask);  // the next trial reads the move
+      }
+    }
+  }
+}
+
 template <bool CAV>
-__global__ void __launch_bounds__(1024) k_sweep_small(SysPtrs p, int n_sweeps, int npt, double margin) {
+__global__ void __launch_bounds__(kSmallThreads) k_sweep_small(SysPtrs p, int n_sweeps, int npt, double margin) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   __shared__ float sh_s[3];
   __shared__ int perm_s[8];
@@ -222,7 +324,22 @@ __global__ void __launch_bounds__(1024) k_sweep_small(SysPtrs p, int n_sweeps, i
     }
     __syncthreads();
 
-    for (int pass = 0; pass < 8; pass++) {
+    // Up to 128 active cells per pass (up to 8 lane groups a warp): a group of
+    // lanes per cell makes the cell's trials one after another, with no
+    // block barrier until the pass ends.  Its lane t draws trial t, three
+    // lanes make the FP64 proposal (an axis each), and the lanes screen the
+    // 27 neighbour cells and the cell's own; the group's first lane applies
+    // an accepted move.  The cells of a colour are independent, so this is
+    // the chain of the rounds below (which serve larger systems), trial for
+    // trial.
+    const int gsz = n_active > 128 ? 0 : (n_active <= nw ? 32 : (n_active <= 2 * nw ? 16 : (n_active <= 4 * nw ? 8 : 4)));
+    for (int pass = 0; gsz > 0 && pass < 8; pass++) {
+      small_pass_groups(m, sb, sh_s, perm_s[pass], s * 8ull + (unsigned long long)pass, gsz, n_active, cap, frozen,
+                        seed, dr, acc, rej_o, rej_b);
+      __syncthreads();  // every move of the pass is seen by the next
+    }
+
+    for (int pass = 0; gsz == 0 && pass < 8; pass++) {
       const int colour = perm_s[pass];
       const unsigned long long seq = s * 8ull + (unsigned long long)pass;
       // this thread's cell (n_active <= blockDim.x)
@@ -487,7 +604,7 @@ __global__ void __launch_bounds__(1024) k_sweep_small(SysPtrs p, int n_sweeps, i
 
 size_t sweep_small_smem(int n, int ncell, int cap) {
   const int na = ncell / 8;  // active cells per pass (even counts per axis)
-  if (n > 65535 || ncell > 65534 || na > 1024) return 0;
+  if (n > 65535 || ncell > 65534 || na > kSmallThreads) return 0;
   // per particle: x, y, z, tx, ty, tz, id; per cell: count, offset; per
   // active cell: trial position, grid coordinates, particle, state, and the
   // draws of up to cap trials
@@ -521,8 +638,8 @@ bool prepare_sweep_small(size_t smem) {
 
 void launch_sweep_small(const SysPtrs &p, int n_sweeps, bool npt, bool cavity, double margin, size_t smem,
                         cudaStream_t s) {
-  if (cavity) k_sweep_small<true><<<1, 1024, smem, s>>>(p, n_sweeps, npt ? 1 : 0, margin);
-  else k_sweep_small<false><<<1, 1024, smem, s>>>(p, n_sweeps, npt ? 1 : 0, margin);
+  if (cavity) k_sweep_small<true><<<1, kSmallThreads, smem, s>>>(p, n_sweeps, npt ? 1 : 0, margin);
+  else k_sweep_small<false><<<1, kSmallThreads, smem, s>>>(p, n_sweeps, npt ? 1 : 0, margin);
 }
 
 }  // namespace hsmc
