@@ -38,7 +38,7 @@ __global__ void __launch_bounds__(256) k_build(SysPtrs p1, const SysPtrs *reps, 
   }
   const SysPtrs p = BATCH ? reps[rep] : p1;
   // the occupancy counts of this sweep's order start from zero (k_order_count
-  // adds to them once this build is complete)
+  // adds to them once the cell build has completed)
   if (!BATCH && p.ocnt != nullptr && blockIdx.x == 0)
     for (int t = threadIdx.x; t < 256; t += blockDim.x) p.ocnt[t] = 0;
   const DevState *st = p.st;
