@@ -19,6 +19,7 @@
 #include <cooperative_groups.h>
 
 #include "cellview.cuh"
+#include "df64.cuh"
 #include "screen.cuh"
 
 namespace cg = cooperative_groups;
@@ -583,55 +584,57 @@ void launch_overlap_replay(const SysPtrs &p, const int *ids, const double *pos_i
 // -------------------------------------------------------------------- q_l
 // Normalised associated Legendre functions by the standard recurrences
 // (Pbar_m^m from Pbar_{m-1}^{m-1}, Pbar_{m+1}^m, then the three-term
-// recurrence in l), with the coefficients tabulated on the host per call.
+// recurrence in l), with the coefficients tabulated on the host per call,
+// as doubles and as double-float pairs (df64.cuh).
 constexpr int QL_LMAX = 12;
 struct QlCoef {
-  double diag[QL_LMAX + 1];                   // sqrt((2m+1)/(2m)), m >= 1
-  double first[QL_LMAX + 1];                  // sqrt(2m+3)
-  double a[QL_LMAX + 1][QL_LMAX + 1];         // a[l][m]
-  double b[QL_LMAX + 1][QL_LMAX + 1];         // b[l][m]
+  F2 neg_diag[QL_LMAX + 1];            // -sqrt((2m+1)/(2m)), m >= 1
+  F2 first[QL_LMAX + 1];               // sqrt(2m+3)
+  F2 a[QL_LMAX + 1][QL_LMAX + 1];      // a[l][m]
+  F2 b[QL_LMAX + 1][QL_LMAX + 1];      // b[l][m]
 };
 __constant__ QlCoef c_ql;
 
 // One bond's contribution to q_lm, m = 0..l (Y_lm by the recurrences of
-// QlCoef; cos m phi, sin m phi by the angle-addition recurrence).
+// QlCoef; cos m phi, sin m phi by the angle-addition recurrence).  The
+// angles' cosines and sines come from FP64 (two reciprocals and a square
+// root); the recurrences and the sums run in double-float arithmetic on the
+// FP32 pipe (about 48 bits: q_l within about 1e-14 of the FP64 recurrences),
+// which bounded this kernel in FP64.
 // LT > 0: l = LT at compile time (the loops unroll and the sums stay in
 // registers); LT = 0: l from the argument.
 template <int LT>
-__device__ __forceinline__ void ql_bond(double dx, double dy, double dz, double r, int l_arg, double *re, double *im) {
+__device__ __forceinline__ void ql_bond(double dx, double dy, double dz, double r, int l_arg, F2 *re, F2 *im) {
   const int l = LT > 0 ? LT : l_arg;
-  const double inv_sqrt_4pi = 0.28209479177387814;
-  // cos and sin of the polar angle and of the azimuth from two reciprocals
-  // (the pipe that FP64 division and square root run on bounds this kernel)
   const double inv_r = 1.0 / r;
   const double rho = sqrt(dx * dx + dy * dy);
   const double inv_rho = rho > 0.0 ? 1.0 / rho : 0.0;
-  const double ct = dz * inv_r, st = rho * inv_r;
-  const double cp = rho > 0.0 ? dx * inv_rho : 1.0, sp = rho > 0.0 ? dy * inv_rho : 0.0;
-  double pmm = inv_sqrt_4pi, cm = 1.0, sm = 0.0;
+  const F2 ct = f2_of(dz * inv_r), st = f2_of(rho * inv_r);
+  const F2 cp = f2_of(rho > 0.0 ? dx * inv_rho : 1.0), sp = f2_of(rho > 0.0 ? dy * inv_rho : 0.0);
+  F2 pmm = f2_of(0.28209479177387814), cm = F2{1.0f, 0.0f}, sm = F2{0.0f, 0.0f};  // 1 / sqrt(4 pi)
 #pragma unroll
   for (int m = 0; m <= (LT > 0 ? LT : QL_LMAX); m++) {
     if (LT == 0 && m > l) break;
     if (m > 0) {
-      pmm *= -c_ql.diag[m] * st;
-      const double c2 = cm * cp - sm * sp;
-      sm = sm * cp + cm * sp;
+      pmm = f2_mul(f2_mul(pmm, c_ql.neg_diag[m]), st);
+      const F2 c2 = f2_sub(f2_mul(cm, cp), f2_mul(sm, sp));
+      sm = f2_add(f2_mul(sm, cp), f2_mul(cm, sp));
       cm = c2;
     }
-    double plm = pmm;
+    F2 plm = pmm;
     if (l > m) {
-      double p2 = pmm, p1 = ct * c_ql.first[m] * pmm;
+      F2 p2 = pmm, p1 = f2_mul(f2_mul(ct, c_ql.first[m]), pmm);
 #pragma unroll
       for (int ll = m + 2; ll <= (LT > 0 ? LT : QL_LMAX); ll++) {
         if (LT == 0 && ll > l) break;
-        const double pn = c_ql.a[ll][m] * (ct * p1 - c_ql.b[ll][m] * p2);
+        const F2 pn = f2_mul(c_ql.a[ll][m], f2_sub(f2_mul(ct, p1), f2_mul(c_ql.b[ll][m], p2)));
         p2 = p1;
         p1 = pn;
       }
       plm = p1;
     }
-    re[m] += plm * cm;
-    im[m] += plm * sm;
+    re[m] = f2_add(re[m], f2_mul(plm, cm));
+    im[m] = f2_add(im[m], f2_mul(plm, sm));
   }
 }
 
@@ -659,9 +662,9 @@ __global__ void __launch_bounds__(128) k_ql(SysPtrs p, Stencil s, int l_arg, dou
   float x32, y32, z32;  // grid coordinates, as the slots hold them
   grid_coords(v, x, y, z, x32, y32, z32);
   constexpr int NM = LT > 0 ? LT + 1 : QL_LMAX + 1;
-  double re[NM], im[NM];
+  F2 re[NM], im[NM];
 #pragma unroll
-  for (int m = 0; m < NM; m++) re[m] = im[m] = 0.0;
+  for (int m = 0; m < NM; m++) re[m] = im[m] = F2{0.0f, 0.0f};
   int bonds = 0;
   const float rc2f = (float)(rc * rc);
   const float err = v.band * (1.0f + rc2f) + 2.4e-7f * (1.0f + rc2f);
@@ -703,7 +706,7 @@ __global__ void __launch_bounds__(128) k_ql(SysPtrs p, Stencil s, int l_arg, dou
 #pragma unroll
     for (int m = 0; m < NM; m++) {
       if (m > l) break;
-      const double a = re[m] * inv, b = im[m] * inv;
+      const double a = f2_value(re[m]) * inv, b = f2_value(im[m]) * inv;
       sum += (m == 0 ? 1.0 : 2.0) * (a * a + b * b);
     }
   }
@@ -728,14 +731,14 @@ void launch_ql(const SysPtrs &p, int l, double rc, int stencil[3], double *per_p
                cudaStream_t st) {
   QlCoef h;
   for (int m = 0; m <= QL_LMAX; m++) {
-    h.diag[m] = m > 0 ? sqrt((2.0 * m + 1.0) / (2.0 * m)) : 0.0;
-    h.first[m] = sqrt(2.0 * m + 3.0);
+    h.neg_diag[m] = f2_of(m > 0 ? -sqrt((2.0 * m + 1.0) / (2.0 * m)) : 0.0);
+    h.first[m] = f2_of(sqrt(2.0 * m + 3.0));
     for (int ll = 0; ll <= QL_LMAX; ll++) {
       const double den = (double)ll * ll - (double)m * m;
-      h.a[ll][m] = den > 0 ? sqrt((4.0 * ll * ll - 1.0) / den) : 0.0;
+      h.a[ll][m] = f2_of(den > 0 ? sqrt((4.0 * ll * ll - 1.0) / den) : 0.0);
       const double nb = (ll - 1.0) * (ll - 1.0) - (double)m * m;
       const double db = 4.0 * (ll - 1.0) * (ll - 1.0) - 1.0;
-      h.b[ll][m] = (nb >= 0 && db > 0) ? sqrt(nb / db) : 0.0;
+      h.b[ll][m] = f2_of((nb >= 0 && db > 0) ? sqrt(nb / db) : 0.0);
     }
   }
   cudaMemcpyToSymbolAsync(c_ql, &h, sizeof(h), 0, cudaMemcpyHostToDevice, st);
