@@ -305,8 +305,8 @@ int hsmc_batch_last_timing(hsmc_batch *b, double *total_ms);
 int hsmc_batch_set_schedule(hsmc_batch *b, int schedule, int cluster_blocks, int tile);
 int hsmc_batch_get_schedule(hsmc_batch *b, int out[3]);
 
-/* Times schedules 0 and 2, and schedule 1 with every cluster size (1, 2, 4,
- * 8) and tile (1, 2, 4), over sweeps_per_variant sweeps each, after an
+/* Times schedules 0, 3 and 2, and schedule 1 with every cluster size (1, 2,
+ * 4, 8) and tile (1, 2, 4), over sweeps_per_variant sweeps each, after an
  * untimed call of 8 sweeps, and keeps the fastest (out as get_schedule).
  * These are ordinary sweeps of every replica's chain. */
 int hsmc_batch_autotune(hsmc_batch *b, int sweeps_per_variant, int out[3]);
