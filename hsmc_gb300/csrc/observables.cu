@@ -647,8 +647,11 @@ __device__ __forceinline__ void ql_bond(double dx, double dy, double dz, double 
 // QL_MAXB; a particle with more adds the rest as it finds them).
 constexpr int QL_MAXB = 64;
 
+// Five blocks an SM for l compiled in (96 registers, no spills): the
+// double-float chains are latency-bound, and more warps hide more of it.
 template <int LT>
-__global__ void __launch_bounds__(128) k_ql(SysPtrs p, Stencil s, int l_arg, double rc, float cut2, double *q_out) {
+__global__ void __launch_bounds__(128, LT > 0 ? 5 : 1) k_ql(SysPtrs p, Stencil s, int l_arg, double rc, float cut2,
+                                                             double *q_out) {
   const int l = LT > 0 ? LT : l_arg;
   __shared__ int bond_id[QL_MAXB][128];
   const CellView v = current_view(p);
